@@ -1,0 +1,200 @@
+"""GB300 HODLR fast direct solver -- Python bindings of the C ABI.
+
+The product is ``libhodlr_gb300.so`` (CUDA, sm_103a) behind the C ABI in
+``include/hodlr_gb300.h``.  This module loads it with ctypes and offers thin
+wrappers that take torch CUDA tensors (torch is only the device-memory and
+stream plumbing here).  There is no CPU fallback: every call goes to the
+library, and loading fails loudly if the library is missing.
+"""
+import ctypes
+import os
+
+from . import build as _build
+
+HODLR_OK = 0
+HODLR_ERR_INVALID_ARG = 1
+HODLR_ERR_CUDA = 2
+HODLR_ERR_SINGULAR_LEAF = 3
+HODLR_ERR_SINGULAR_CAPACITANCE = 4
+HODLR_ERR_NOT_CONVERGED = 5
+HODLR_ERR_NONFINITE_INPUT = 6
+HODLR_ERR_TIMEOUT = 7
+HODLR_ERR_NOT_FACTORED = 8
+HODLR_ERR_OUT_OF_MEMORY = 9
+
+PREC_FP64 = 0
+PREC_MIXED = 1
+RESID_FP64 = 0
+RESID_FP64_EMULATED = 1
+
+LIB_PATH = _build.LIB
+
+
+class HodlrError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("hodlr error %d: %s" % (code, msg))
+        self.code = code
+
+
+class Desc(ctypes.Structure):
+    _fields_ = [("n", ctypes.c_int64), ("leaf", ctypes.c_int32), ("levels", ctypes.c_int32),
+                ("rank", ctypes.c_int32), ("nrhs_max", ctypes.c_int32), ("precision", ctypes.c_int32),
+                ("residual", ctypes.c_int32), ("refine_tol", ctypes.c_double),
+                ("refine_max_iter", ctypes.c_int32), ("flags", ctypes.c_int32), ("stream", ctypes.c_void_p)]
+
+
+class SolveInfo(ctypes.Structure):
+    _fields_ = [("iterations", ctypes.c_int32), ("status", ctypes.c_int32), ("bad_index", ctypes.c_int64),
+                ("rel_residual", ctypes.c_double)]
+
+
+class Grads(ctypes.Structure):
+    _fields_ = [("db", ctypes.c_void_p), ("ldb", ctypes.c_int64), ("dD", ctypes.c_void_p),
+                ("dU", ctypes.c_void_p), ("dV", ctypes.c_void_p), ("ds", ctypes.c_void_p)]
+
+
+# name -> (restype, argtypes); the full exported surface of include/hodlr_gb300.h
+_VP, _I, _I64, _D = ctypes.c_void_p, ctypes.c_int, ctypes.c_int64, ctypes.c_double
+SIGNATURES = {
+    "hodlr_hsolve": (_I, [_I, _I, _I, _I, _I, _VP, _VP, _VP]),
+    "hodlr_hsolve_ex": (_I, [_I, _I, _I, _I, _I, _VP, _VP, _VP, _I, _VP, ctypes.POINTER(SolveInfo)]),
+    "hodlr_create": (_I, [ctypes.POINTER(Desc), ctypes.POINTER(_VP)]),
+    "hodlr_destroy": (_I, [_VP]),
+    "hodlr_set_stream": (_I, [_VP, _VP]),
+    "hodlr_set_leaf_blocks": (_I, [_VP, _VP, _I64, _I64]),
+    "hodlr_set_lowrank": (_I, [_VP, _I, _VP, _I64, _VP, _I64, _VP]),
+    "hodlr_factor": (_I, [_VP]),
+    "hodlr_solve": (_I, [_VP, _VP, _I64, _I, ctypes.POINTER(SolveInfo)]),
+    "hodlr_solve_transpose": (_I, [_VP, _VP, _I64, _I, ctypes.POINTER(SolveInfo)]),
+    "hodlr_matvec": (_I, [_VP, _I, _VP, _I64, _VP, _I64, _I]),
+    "hodlr_adjoint": (_I, [_VP, _VP, _I64, _VP, _I64, _I, ctypes.POINTER(Grads)]),
+    "hodlr_get_factors": (_I, [_VP, _VP, _VP, _VP, _VP, _VP]),
+    "hodlr_generate": (_I, [_VP, ctypes.c_uint64, _D, _I, _D, _VP, _I64, _I]),
+    "hodlr_last_timings": (_I, [_VP, ctypes.POINTER(_D), ctypes.POINTER(_D)]),
+    "hodlr_kernel_launches": (_I64, []),
+    "hodlr_last_error_string": (ctypes.c_char_p, []),
+}
+
+_lib = None
+
+
+def lib(build_if_missing=False):
+    """Load libhodlr_gb300.so.  Raises if it is absent (no fallback path)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            if not build_if_missing:
+                raise ImportError("libhodlr_gb300.so is not built (run __graft_entry__.build() "
+                                  "or python fastsolver2_gb300/build.py)")
+            _build.build()
+        L = ctypes.CDLL(LIB_PATH)
+        for name, (res, args) in SIGNATURES.items():
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = L
+    return _lib
+
+
+def check(code):
+    if code != HODLR_OK:
+        raise HodlrError(code, lib().hodlr_last_error_string().decode())
+    return code
+
+
+def _ptr(t):
+    return ctypes.c_void_p(t.data_ptr()) if t is not None else None
+
+
+def _ld(t):
+    """Leading dimension of a column-major (Fortran-ordered) 2-D tensor."""
+    if t.dim() == 1:
+        return t.shape[0]
+    assert t.stride(0) == 1, "expected a column-major tensor (use .t().contiguous().t())"
+    return t.stride(1)
+
+
+def colmajor(t):
+    """A column-major copy of a 2-D tensor (torch is row-major by default)."""
+    return t.t().contiguous().t()
+
+
+class Solver:
+    """Handle-based factor/solve API (hodlr_create ... hodlr_destroy)."""
+
+    def __init__(self, n, leaf, levels, rank, nrhs_max=1, precision=PREC_FP64, residual=RESID_FP64_EMULATED,
+                 refine_tol=1e-12, refine_max_iter=10, stream=None):
+        self.desc = Desc(n, leaf, levels, rank, nrhs_max, precision, residual, refine_tol, refine_max_iter, 0,
+                         stream)
+        h = ctypes.c_void_p()
+        check(lib().hodlr_create(ctypes.byref(self.desc), ctypes.byref(h)))
+        self.h = h
+        self.n, self.leaf, self.levels, self.rank = n, leaf, levels, rank
+
+    def close(self):
+        if self.h:
+            lib().hodlr_destroy(self.h)
+            self.h = None
+
+    __del__ = close
+
+    def set_leaf_blocks(self, D, ld=None, leaf_stride=None):
+        """D: torch float64 CUDA tensor; default layout = the KTree region (N x m column-major)."""
+        ld = _ld(D) if ld is None else ld
+        stride = self.leaf if leaf_stride is None else leaf_stride
+        check(lib().hodlr_set_leaf_blocks(self.h, _ptr(D), ld, stride))
+
+    def set_lowrank(self, level, U, V, s=None):
+        check(lib().hodlr_set_lowrank(self.h, level, _ptr(U), _ld(U), _ptr(V), _ld(V), _ptr(s)))
+
+    def factor(self):
+        check(lib().hodlr_factor(self.h))
+
+    def solve(self, B, transpose=False):
+        info = SolveInfo()
+        f = lib().hodlr_solve_transpose if transpose else lib().hodlr_solve
+        check(f(self.h, _ptr(B), _ld(B), B.shape[1] if B.dim() == 2 else 1, ctypes.byref(info)))
+        return info
+
+    def matvec(self, X, Y, transpose=False):
+        check(lib().hodlr_matvec(self.h, int(transpose), _ptr(X), _ld(X), _ptr(Y), _ld(Y),
+                                 X.shape[1] if X.dim() == 2 else 1))
+
+    def adjoint(self, x, g, db=None, dD=None, dU=None, dV=None, ds=None):
+        gr = Grads(_ptr(db), _ld(db) if db is not None else 0, _ptr(dD), _ptr(dU), _ptr(dV), _ptr(ds))
+        check(lib().hodlr_adjoint(self.h, _ptr(x), _ld(x), _ptr(g), _ld(g),
+                                  x.shape[1] if x.dim() == 2 else 1, ctypes.byref(gr)))
+
+    def get_factors(self, leaf_lu=None, leaf_ipiv=None, utilde=None, cap_lu=None, cap_ipiv=None):
+        check(lib().hodlr_get_factors(self.h, _ptr(leaf_lu), _ptr(leaf_ipiv), _ptr(utilde), _ptr(cap_lu),
+                                      _ptr(cap_ipiv)))
+
+    def generate(self, seed, shift=4.0, orthonormal=False, decay=0.0, B=None):
+        check(lib().hodlr_generate(self.h, seed, shift, int(orthonormal), decay, _ptr(B),
+                                   _ld(B) if B is not None else 0, B.shape[1] if B is not None else 0))
+
+    def timings(self):
+        f, s = ctypes.c_double(), ctypes.c_double()
+        check(lib().hodlr_last_timings(self.h, ctypes.byref(f), ctypes.byref(s)))
+        return f.value, s.value
+
+
+def hsolve(nrow, nrhs, rank, nPart, LD, K, U, V, precision=PREC_FP64, stream=None):
+    """fastSolver2's hsolve(nrow, nrhs, rank, nPart, LD, K, U, V), in place.
+
+    K, U, V: torch float64 tensors (CUDA, column-major, leading dimension LD)
+    or numpy Fortran-ordered float64 arrays (host; staged by the library)."""
+    def p(a):
+        if a is None:
+            return None
+        if hasattr(a, "data_ptr"):
+            return ctypes.c_void_p(a.data_ptr())
+        return ctypes.c_void_p(a.ctypes.data)
+    info = SolveInfo()
+    check(lib().hodlr_hsolve_ex(nrow, nrhs, rank, nPart, LD, p(K), p(U), p(V), precision, stream,
+                                ctypes.byref(info)))
+    return info
+
+
+def kernel_launches():
+    return lib().hodlr_kernel_launches()

@@ -1,0 +1,38 @@
+// Shared definitions of the GB300 HODLR kernels.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "hodlr_gb300.h"
+
+namespace hodlr {
+
+// Device-side status block of a handle: the first error wins.
+struct DevStatus {
+  int code;
+  int pad;
+  long long index;
+  int done;       // refinement converged flag (predicates correction kernels)
+  int iters;      // corrections applied
+  double resid;   // last relative residual
+};
+
+__device__ __forceinline__ void report_error(DevStatus *st, int code, long long index) {
+  if (st && atomicCAS(&st->code, 0, code) == 0) st->index = index;
+}
+
+template <typename T> __device__ __forceinline__ T dabs(T x) { return x < T(0) ? -x : x; }
+
+// Host-side launch accounting (every kernel launch of the library goes
+// through HODLR_LAUNCH so hodlr_kernel_launches() can report it).
+void count_launch();
+
+#define HODLR_LAUNCH(kernel, grid, block, smem, stream, ...)                 \
+  do {                                                                       \
+    ::hodlr::count_launch();                                                 \
+    kernel<<<(grid), (block), (smem), (stream)>>>(__VA_ARGS__);              \
+  } while (0)
+
+inline int ceil_div(long long a, long long b) { return (int)((a + b - 1) / b); }
+
+}  // namespace hodlr

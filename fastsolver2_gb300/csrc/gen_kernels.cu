@@ -1,0 +1,125 @@
+// Seeded synthetic problem generator (device side).
+//
+// fastSolver2 generates its inputs from per-partition seeds on the CPU
+// (InitMatrixTask src/tasks/init_matrix.cc:35-73, DenseBlockTask
+// src/tasks/dense_block.cc:35-76).  For the large configurations the inputs
+// are generated where they are used, in HBM: a counter-based generator
+// (splitmix64 hashing of (seed, stream, index), Box-Muller) so that any
+// element is a pure function of its coordinates and launches parallelise
+// freely.
+#include <algorithm>
+
+#include "kernels.cuh"
+
+namespace hodlr {
+
+__device__ __forceinline__ unsigned long long mix64(unsigned long long z) {
+  z += 0x9E3779B97F4A7C15ull;
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+
+__device__ __forceinline__ double gauss(unsigned long long seed, unsigned long long stream,
+                                        unsigned long long idx) {
+  const unsigned long long h1 = mix64(seed ^ mix64(stream * 0xD1B54A32D192ED03ull + idx));
+  const unsigned long long h2 = mix64(h1 ^ 0x5851F42D4C957F2Dull);
+  const double u1 = ((double)(h1 >> 11) + 1.0) * 0x1.0p-53;  // (0, 1]
+  const double u2 = (double)(h2 >> 11) * 0x1.0p-53;          // [0, 1)
+  return sqrt(-2.0 * log(u1)) * cospi(2.0 * u2);
+}
+
+__global__ void gaussian_kernel(double *X, long long ld, long long n, int c, unsigned long long seed,
+                                unsigned long long stream, double scale) {
+  const long long total = n * c;
+  for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < total;
+       e += (long long)gridDim.x * blockDim.x) {
+    const long long i = e % n, j = e / n;
+    X[i + j * ld] = scale * gauss(seed, stream, (unsigned long long)e);
+  }
+}
+
+cudaError_t launch_gaussian(double *X, long long ld, long long n, int c, unsigned long long seed,
+                            unsigned long long stream, double scale, cudaStream_t s) {
+  const long long total = n * c;
+  if (total == 0) return cudaSuccess;
+  const int grid = (int)std::min<long long>(ceil_div(total, 256), 152 * 32);
+  HODLR_LAUNCH(gaussian_kernel, grid, 256, 0, s, X, ld, n, c, seed, stream, scale);
+  return cudaGetLastError();
+}
+
+__global__ void gen_leaves_kernel(double *D, int m, long long total, unsigned long long seed, double shift) {
+  const double sc = 1.0 / sqrt((double)m);
+  for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < total;
+       e += (long long)gridDim.x * blockDim.x) {
+    const long long w = e % ((long long)m * m);
+    const int i = (int)(w % m), j = (int)(w / m);
+    D[e] = sc * gauss(seed, 0x1EAFull, (unsigned long long)e) + (i == j ? shift : 0.0);
+  }
+}
+
+cudaError_t launch_gen_leaves(double *D, int m, int nleaf, unsigned long long seed, double shift,
+                              cudaStream_t s) {
+  const long long total = (long long)nleaf * m * m;
+  const int grid = (int)std::min<long long>(ceil_div(total, 256), 152 * 32);
+  HODLR_LAUNCH(gen_leaves_kernel, grid, 256, 0, s, D, m, total, seed, shift);
+  return cudaGetLastError();
+}
+
+// One CTA per Gram matrix: Cholesky G = R^T R in shared memory, then Rinv.
+__global__ void chol_inv_kernel(const double *G, double *Rinv, int r, DevStatus *st) {
+  extern __shared__ double sm[];
+  double *R = sm;          // r x r, upper
+  double *Q = sm + r * r;  // r x r, Rinv
+  const int b = blockIdx.x;
+  const double *g = G + (long long)b * r * r;
+  for (int e = threadIdx.x; e < r * r; e += blockDim.x) {
+    R[e] = g[e];
+    Q[e] = 0.0;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    bool ok = true;
+    for (int j = 0; j < r && ok; ++j) {
+      double d = R[j + j * r];
+      for (int k = 0; k < j; ++k) d -= R[k + j * r] * R[k + j * r];
+      if (!(d > 0.0)) {
+        ok = false;
+        break;
+      }
+      d = sqrt(d);
+      R[j + j * r] = d;
+      for (int c = j + 1; c < r; ++c) {
+        double v = R[j + c * r];
+        for (int k = 0; k < j; ++k) v -= R[k + j * r] * R[k + c * r];
+        R[j + c * r] = v / d;
+      }
+    }
+    if (!ok) {
+      report_error(st, HODLR_ERR_SINGULAR_CAPACITANCE, b);
+    } else {
+      // Rinv: solve R Q = I column by column (upper triangular back substitution)
+      for (int c = 0; c < r; ++c)
+        for (int i = c; i >= 0; --i) {
+          double v = (i == c) ? 1.0 : 0.0;
+          for (int k = i + 1; k <= c; ++k) v -= R[i + k * r] * Q[k + c * r];
+          Q[i + c * r] = v / R[i + i * r];
+        }
+    }
+  }
+  __syncthreads();
+  double *o = Rinv + (long long)b * r * r;
+  for (int e = threadIdx.x; e < r * r; e += blockDim.x) o[e] = Q[e];
+}
+
+cudaError_t launch_chol_inv(const double *G, double *Rinv, int r, int nbatch, DevStatus *st, cudaStream_t s) {
+  const size_t bytes = (size_t)2 * r * r * sizeof(double);
+  if (bytes > 48 * 1024) {
+    cudaError_t e = cudaFuncSetAttribute(chol_inv_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    if (e != cudaSuccess) return e;
+  }
+  HODLR_LAUNCH(chol_inv_kernel, nbatch, 64, bytes, s, G, Rinv, r, st);
+  return cudaGetLastError();
+}
+
+}  // namespace hodlr

@@ -1,0 +1,937 @@
+// C ABI of the GB300 HODLR solver: handle life cycle, the factor / solve
+// sweeps (one launch per kernel per tree depth, captured in CUDA graphs),
+// mixed-precision iterative refinement, the transpose solve / adjoint sweep,
+// and the drop-in for fastSolver2's raw-pointer hsolve.
+//
+// Device layout of a handle (all column-major):
+//   D      [nleaf][m][m]   FP64 leaf blocks                (KTree region)
+//   U, V   [L][n][r]       FP64 per-level factors, ld n    (UTree chunks / VTree)
+//   s      [L][r]          FP64 singular-value scalings
+//   LU     [nleaf][m][m]   leaf LU factors (FP64, or FP32 in the mixed mode)
+//   ipiv   [nleaf][m]      1-based leaf pivots
+//   Ut     n x (L*r)       transformed bases Utilde^(l) = A_c^{-1} U^(l)_c, ld n
+//   capLU  [2^L-1][2r][2r] FP64 capacitance LU of every node, node id 2^l-1+p
+// Level l's U/V/Ut block is the column range [l*r, (l+1)*r) of an n x L*r
+// matrix, i.e. the UTree column layout of the reference (src/tree.cc:61-73)
+// without the right-hand-side columns.
+#include <atomic>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <string>
+#include <tuple>
+#include <vector>
+
+#include "kernels.cuh"
+
+namespace hodlr {
+static std::atomic<long long> g_launches{0};
+void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+}  // namespace hodlr
+
+using namespace hodlr;
+
+static thread_local std::string g_err;
+
+static int set_err(int code, const std::string &msg) {
+  g_err = msg;
+  return code;
+}
+
+#define CK(expr)                                                                              \
+  do {                                                                                        \
+    cudaError_t e_ = (expr);                                                                  \
+    if (e_ != cudaSuccess)                                                                    \
+      return set_err(e_ == cudaErrorMemoryAllocation ? HODLR_ERR_OUT_OF_MEMORY : HODLR_ERR_CUDA, \
+                     std::string(#expr) + ": " + cudaGetErrorString(e_));                     \
+  } while (0)
+
+#define CKS(expr)                  \
+  do {                             \
+    int s_ = (expr);               \
+    if (s_ != HODLR_OK) return s_; \
+  } while (0)
+
+struct GraphEntry {
+  cudaGraphExec_t exec = nullptr;
+  long long kernels = 0;
+};
+
+struct hodlr_ctx {
+  hodlr_desc d{};
+  long long n = 0;
+  int m = 0, L = 0, r = 0, nleaf = 0, nnode = 0, kmax = 0;
+  bool mixed = false;
+  cudaStream_t st = nullptr;
+  bool own_stream = false;
+  // inputs
+  double *D = nullptr, *U = nullptr, *V = nullptr, *s = nullptr;
+  bool has_D = false;
+  std::vector<char> has_level;
+  // factorisation
+  double *LU = nullptr, *Ut = nullptr;
+  float *LU32 = nullptr, *V32 = nullptr, *Ut32 = nullptr;
+  int *ipiv = nullptr;
+  double *capLU = nullptr;
+  int *cap_ipiv = nullptr;
+  bool factored = false;
+  // workspaces
+  double *Tbuf = nullptr, *Wbuf = nullptr, *eta = nullptr, *red = nullptr;
+  double *X64 = nullptr, *R64 = nullptr, *B64 = nullptr, *norms = nullptr, *nwork = nullptr;
+  float *X32 = nullptr;
+  size_t tbuf_elems = 0, eta_elems = 0, red_elems = 0;
+  DevStatus *dst = nullptr, *hst = nullptr;
+  // timing
+  cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+  float factor_ms = 0.f, solve_ms = 0.f;
+  // graphs
+  bool use_graphs = true;
+  int factor_runs = 0;
+  GraphEntry factor_graph;
+  std::map<std::tuple<const double *, long long, int, int>, GraphEntry> solve_graphs;
+  std::map<std::tuple<const double *, long long, int, int>, int> solve_runs;
+  std::vector<void *> allocs;
+
+  template <typename T> T *alloc(size_t count, cudaError_t &err) {
+    void *p = nullptr;
+    if (count == 0) count = 1;
+    err = cudaMalloc(&p, count * sizeof(T));
+    if (err == cudaSuccess) allocs.push_back(p);
+    return static_cast<T *>(p);
+  }
+  double *Ulev(int l) const { return U + (long long)l * n * r; }
+  double *Vlev(int l) const { return V + (long long)l * n * r; }
+  double *slev(int l) const { return s + (long long)l * r; }
+};
+
+static void free_ctx(hodlr_ctx *h) {
+  if (!h) return;
+  for (auto &g : h->solve_graphs)
+    if (g.second.exec) cudaGraphExecDestroy(g.second.exec);
+  if (h->factor_graph.exec) cudaGraphExecDestroy(h->factor_graph.exec);
+  for (void *p : h->allocs) cudaFree(p);
+  if (h->hst) cudaFreeHost(h->hst);
+  for (auto &e : h->ev)
+    if (e) cudaEventDestroy(e);
+  if (h->own_stream && h->st) cudaStreamDestroy(h->st);
+  delete h;
+}
+
+// ----------------------------------------------------------------- sizes
+static void plan_sizes(hodlr_ctx *h) {
+  const long long n = h->n;
+  const int L = h->L, r = h->r, k = h->kmax;
+  size_t tb = (size_t)1 << L;
+  tb = std::max(tb * r * std::max(k, r), (size_t)r * std::max(k, r));
+  size_t et = ((size_t)1 << L) * (size_t)r * r;
+  size_t red = 0;
+  for (int l = 0; l < L; ++l) {
+    const int nb = 2 << l;
+    const long long rows = n >> (l + 1);
+    const size_t ct = (size_t)(l + 1) * r;
+    tb = std::max(tb, (size_t)nb * r * ct);
+    et = std::max(et, ((size_t)1 << l) * 2 * r * (size_t)l * r);
+    et = std::max(et, ((size_t)1 << l) * 2 * r * (size_t)k);
+    red = std::max(red, reduce_workspace_doubles(rows, nb, r, (int)ct, 8));
+    red = std::max(red, reduce_workspace_doubles(rows, nb, r, k, 8));
+    red = std::max(red, reduce_workspace_doubles(rows, nb, r, r, 8));
+  }
+  h->tbuf_elems = tb;
+  h->eta_elems = et;
+  h->red_elems = red;
+}
+
+// ---------------------------------------------------------------- status
+static int sync_status(hodlr_ctx *h, hodlr_solve_info *info) {
+  CK(cudaMemcpyAsync(h->hst, h->dst, sizeof(DevStatus), cudaMemcpyDeviceToHost, h->st));
+  CK(cudaStreamSynchronize(h->st));
+  DevStatus s = *h->hst;
+  if (info) {
+    info->iterations = s.iters;
+    info->status = s.code;
+    info->bad_index = s.index;
+    info->rel_residual = s.resid;
+  }
+  if (s.code != HODLR_OK) {
+    static const char *names[] = {"ok", "invalid argument", "cuda error", "singular leaf block",
+                                  "singular capacitance system", "refinement did not converge",
+                                  "non-finite input", "device wait timed out", "not factored",
+                                  "out of memory"};
+    char buf[160];
+    snprintf(buf, sizeof buf, "%s (index %lld)", (s.code >= 0 && s.code <= 9) ? names[s.code] : "error",
+             s.index);
+    return set_err(s.code, buf);
+  }
+  return HODLR_OK;
+}
+
+static int reset_status(hodlr_ctx *h) {
+  CK(cudaMemsetAsync(h->dst, 0, sizeof(DevStatus), h->st));
+  return HODLR_OK;
+}
+
+// Run fn eagerly, or (after the first eager run of the same key) as a CUDA
+// graph captured from fn.
+template <typename F>
+static int run_graphed(hodlr_ctx *h, GraphEntry &g, int &runs, F fn) {
+  if (!h->use_graphs || runs == 0 || h->st == nullptr) {
+    ++runs;
+    return fn();
+  }
+  if (!g.exec) {
+    long long before = g_launches.load();
+    CK(cudaStreamBeginCapture(h->st, cudaStreamCaptureModeThreadLocal));
+    int rc = fn();
+    cudaGraph_t graph = nullptr;
+    cudaError_t ce = cudaStreamEndCapture(h->st, &graph);
+    if (rc != HODLR_OK) {
+      if (graph) cudaGraphDestroy(graph);
+      return rc;
+    }
+    CK(ce);
+    cudaError_t ie = cudaGraphInstantiate(&g.exec, graph, 0);
+    cudaGraphDestroy(graph);
+    CK(ie);
+    g.kernels = g_launches.load() - before;
+    g_launches.fetch_sub(g.kernels);  // counted on each replay instead
+  }
+  g_launches.fetch_add(g.kernels);
+  CK(cudaGraphLaunch(g.exec, h->st));
+  ++runs;
+  return HODLR_OK;
+}
+
+// ----------------------------------------------------------- the sweeps
+template <typename T> static T *LUptr(hodlr_ctx *h);
+template <> double *LUptr<double>(hodlr_ctx *h) { return h->LU; }
+template <> float *LUptr<float>(hodlr_ctx *h) { return h->LU32; }
+template <typename T> static T *Utptr(hodlr_ctx *h);
+template <> double *Utptr<double>(hodlr_ctx *h) { return h->Ut; }
+template <> float *Utptr<float>(hodlr_ctx *h) { return h->Ut32; }
+template <typename T> static const T *Vptr(hodlr_ctx *h);
+template <> const double *Vptr<double>(hodlr_ctx *h) { return h->V; }
+template <> const float *Vptr<float>(hodlr_ctx *h) { return h->V32; }
+
+// Factorisation sweep: leaf LU, Ut = D^{-1} U (all levels at once), then for
+// depth L-1 .. 0: T = V^T [Ut_d | Ut_u], capacitance LU + eta, Ut_d -= Ut_u eta.
+template <typename T> static int factor_sweep(hodlr_ctx *h) {
+  const long long n = h->n;
+  const int m = h->m, L = h->L, r = h->r;
+  cudaStream_t s = h->st;
+  T *LU = LUptr<T>(h);
+  T *Ut = Utptr<T>(h);
+  const T *Vt = Vptr<T>(h);
+  CK(launch_leaf_getrf<T>(h->D, m, (long long)m * m, LU, h->ipiv, m, h->nleaf, h->dst, s));
+  if (L == 0) return HODLR_OK;
+  if (sizeof(T) == 8)
+    CK(cudaMemcpyAsync(Ut, h->U, sizeof(double) * n * L * r, cudaMemcpyDeviceToDevice, s));
+  else
+    CK((launch_convert<double, float>(h->U, n, reinterpret_cast<float *>(Ut), n, n, L * r, s)));
+  CK(launch_leaf_getrs<T>(LU, h->ipiv, m, h->nleaf, Ut, n, L * r, false, nullptr, s));
+  for (int l = L - 1; l >= 0; --l) {
+    const int nb = 2 << l;
+    const long long rows = n >> (l + 1);
+    const int Cd = l * r, Ct = Cd + r;
+    CK(launch_reduce_tn<T>(Vt + (long long)l * n * r, n, Ut, n, rows, nb, r, Ct, h->Tbuf, h->red, nullptr, s));
+    CapArgs ca{};
+    ca.Tb = h->Tbuf;
+    ca.tb_stride = (long long)r * Ct;
+    ca.scale = h->slev(l);
+    ca.cap_lu = h->capLU;
+    ca.cap_ipiv = h->cap_ipiv;
+    ca.eta = h->eta;
+    ca.r = r;
+    ca.C = Cd;
+    ca.nnode = 1 << l;
+    ca.node_base = (1 << l) - 1;
+    ca.factor = true;
+    ca.trans = false;
+    ca.st = h->dst;
+    CK(launch_capacitance(ca, s));
+    if (Cd > 0) {
+      UpdateArgs ua{};
+      ua.A = Ut + (long long)l * r * n;
+      ua.lda = n;
+      ua.a_bstride = rows;
+      ua.B = h->eta;
+      ua.ldb = 2 * r;
+      ua.b_s1 = 2LL * r * Cd;
+      ua.b_s2 = r;
+      ua.C = Ut;
+      ua.ldc = n;
+      ua.c_bstride = rows;
+      ua.M = (int)rows;
+      ua.N = Cd;
+      ua.K = r;
+      ua.nbatch = nb;
+      ua.alpha = -1.0;
+      CK(launch_update_nn<T>(ua, s));
+    }
+  }
+  return HODLR_OK;
+}
+
+// X := A^{-1} X (or A^{-T} X) with the stored factors, X of type T (n x k, ldx).
+template <typename T>
+static int solve_sweep(hodlr_ctx *h, T *X, long long ldx, int k, bool trans, const int *skip) {
+  const long long n = h->n;
+  const int m = h->m, L = h->L, r = h->r;
+  cudaStream_t s = h->st;
+  T *LU = LUptr<T>(h);
+  T *Ut = Utptr<T>(h);
+  const T *Vt = Vptr<T>(h);
+  if (!trans) CK(launch_leaf_getrs<T>(LU, h->ipiv, m, h->nleaf, X, ldx, k, false, skip, s));
+  for (int step = 0; step < L; ++step) {
+    const int l = trans ? step : L - 1 - step;
+    const int nb = 2 << l;
+    const long long rows = n >> (l + 1);
+    const T *Ared = trans ? Ut + (long long)l * r * n : Vt + (long long)l * n * r;
+    const T *Aupd = trans ? Vt + (long long)l * n * r : Ut + (long long)l * r * n;
+    CK(launch_reduce_tn<T>(Ared, n, X, ldx, rows, nb, r, k, h->Tbuf, h->red, skip, s));
+    CapArgs ca{};
+    ca.Tb = h->Tbuf;
+    ca.tb_stride = (long long)r * k;
+    ca.scale = h->slev(l);
+    ca.cap_lu = h->capLU;
+    ca.cap_ipiv = h->cap_ipiv;
+    ca.eta = h->eta;
+    ca.r = r;
+    ca.C = k;
+    ca.nnode = 1 << l;
+    ca.node_base = (1 << l) - 1;
+    ca.factor = false;
+    ca.trans = trans;
+    ca.st = h->dst;
+    ca.skip = skip;
+    CK(launch_capacitance(ca, s));
+    UpdateArgs ua{};
+    ua.A = Aupd;
+    ua.lda = n;
+    ua.a_bstride = rows;
+    ua.B = h->eta;
+    ua.ldb = 2 * r;
+    ua.b_s1 = 2LL * r * k;
+    ua.b_s2 = r;
+    ua.b_flip = trans ? 1 : 0;
+    ua.scale = trans ? h->slev(l) : nullptr;
+    ua.C = X;
+    ua.ldc = ldx;
+    ua.c_bstride = rows;
+    ua.M = (int)rows;
+    ua.N = k;
+    ua.K = r;
+    ua.nbatch = nb;
+    ua.alpha = -1.0;
+    ua.skip = skip;
+    CK(launch_update_nn<T>(ua, s));
+  }
+  if (trans) CK(launch_leaf_getrs<T>(LU, h->ipiv, m, h->nleaf, X, ldx, k, true, skip, s));
+  return HODLR_OK;
+}
+
+// Y = beta*Y0 + alpha * op(A) X in native FP64 (Y0 == nullptr: Y starts at 0).
+static int matvec_fp64(hodlr_ctx *h, bool trans, const double *X, long long ldx, const double *Y0,
+                       long long ldy0, double *Y, long long ldy, int k, double alpha, const int *skip) {
+  const long long n = h->n;
+  const int m = h->m, L = h->L, r = h->r;
+  cudaStream_t s = h->st;
+  if (Y0)
+    CK(launch_axpy(Y0, ldy0, Y, ldy, n, k, 1.0, false, skip, s));
+  else
+    CK(cudaMemset2DAsync(Y, sizeof(double) * ldy, 0, sizeof(double) * n, k, s));
+  UpdateArgs la{};
+  la.A = h->D;
+  la.lda = m;
+  la.a_bstride = (long long)m * m;
+  la.a_trans = trans ? 1 : 0;
+  la.B = X;
+  la.ldb = ldx;
+  la.b_s1 = 2LL * m;
+  la.b_s2 = m;
+  la.C = Y;
+  la.ldc = ldy;
+  la.c_bstride = m;
+  la.M = m;
+  la.N = k;
+  la.K = m;
+  la.nbatch = h->nleaf;
+  la.alpha = alpha;
+  la.skip = skip;
+  CK(launch_update_nn<double>(la, s));
+  for (int l = 0; l < L; ++l) {
+    const int nb = 2 << l;
+    const long long rows = n >> (l + 1);
+    const double *Ared = trans ? h->Ulev(l) : h->Vlev(l);
+    const double *Aupd = trans ? h->Vlev(l) : h->Ulev(l);
+    CK(launch_reduce_tn<double>(Ared, n, X, ldx, rows, nb, r, k, h->Tbuf, h->red, skip, s));
+    UpdateArgs ua{};
+    ua.A = Aupd;
+    ua.lda = n;
+    ua.a_bstride = rows;
+    ua.B = h->Tbuf;
+    ua.ldb = r;
+    ua.b_s1 = 2LL * r * k;
+    ua.b_s2 = (long long)r * k;
+    ua.b_flip = 1;
+    ua.scale = h->slev(l);
+    ua.C = Y;
+    ua.ldc = ldy;
+    ua.c_bstride = rows;
+    ua.M = (int)rows;
+    ua.N = k;
+    ua.K = r;
+    ua.nbatch = nb;
+    ua.alpha = alpha;
+    ua.skip = skip;
+    CK(launch_update_nn<double>(ua, s));
+  }
+  return HODLR_OK;
+}
+
+// R = B - op(A) X, FP64-accurate, with the handle's residual arithmetic.
+
+static int residual(hodlr_ctx *h, bool trans, const double *X, long long ldx, const double *B, long long ldb,
+                    double *R, long long ldr, int k, const int *skip) {
+  return matvec_fp64(h, trans, X, ldx, B, ldb, R, ldr, k, -1.0, skip);
+}
+
+// Mixed-precision solve with FP64 iterative refinement.  B (FP64, n x k) is
+// overwritten by X.  All control stays on the device: the refinement check
+// sets st->done, which predicates every later kernel, so the whole loop is
+// one stream-ordered (graph-capturable) sequence.
+static int mixed_solve(hodlr_ctx *h, double *B, long long ldb, int k, bool trans) {
+  const long long n = h->n;
+  cudaStream_t s = h->st;
+  const int *done = &h->dst->done;
+  double *bn = h->norms, *rn = h->norms + h->kmax;
+  CK(launch_axpy(B, ldb, h->B64, n, n, k, 1.0, false, nullptr, s));
+  CK(launch_colnorms(h->B64, n, n, k, bn, h->nwork, nullptr, s));
+  CK((launch_convert<double, float>(h->B64, n, h->X32, n, n, k, s)));
+  CKS(solve_sweep<float>(h, h->X32, n, k, trans, nullptr));
+  CK((launch_convert<float, double>(h->X32, n, h->X64, n, n, k, s)));
+  const int maxit = std::max(0, h->d.refine_max_iter);
+  for (int it = 0; it <= maxit; ++it) {
+    CKS(residual(h, trans, h->X64, n, h->B64, n, h->R64, n, k, done));
+    CK(launch_colnorms(h->R64, n, n, k, rn, h->nwork, done, s));
+    CK(launch_refine_check(rn, bn, k, h->d.refine_tol, h->dst, it < maxit ? 1 : 0, s));
+    if (it == maxit) break;
+    CK((launch_convert<double, float>(h->R64, n, h->X32, n, n, k, s)));
+    CKS(solve_sweep<float>(h, h->X32, n, k, trans, done));
+    CK((launch_add_correction<float>(h->X64, n, h->X32, n, h->X64, n, n, k, done, s)));
+  }
+  CK(launch_axpy(h->X64, n, B, ldb, n, k, 1.0, false, nullptr, s));
+  return HODLR_OK;
+}
+
+// ----------------------------------------------------------------- C ABI
+extern "C" {
+
+const char *hodlr_last_error_string(void) { return g_err.c_str(); }
+
+int64_t hodlr_kernel_launches(void) { return (int64_t)g_launches.load(); }
+
+int hodlr_create(const hodlr_desc *desc, hodlr_handle *out) {
+  if (!desc || !out) return set_err(HODLR_ERR_INVALID_ARG, "null argument");
+  *out = nullptr;
+  const hodlr_desc &d = *desc;
+  if (d.leaf < 1 || d.levels < 0 || d.levels > 24 || d.n != ((int64_t)d.leaf << d.levels))
+    return set_err(HODLR_ERR_INVALID_ARG, "need n = leaf * 2^levels, leaf >= 1, 0 <= levels <= 24");
+  if (d.levels > 0 && (d.rank < 1 || d.rank > 64))
+    return set_err(HODLR_ERR_INVALID_ARG, "rank must be in [1, 64]");
+  if (d.levels > 0 && (d.n >> d.levels) < 1) return set_err(HODLR_ERR_INVALID_ARG, "leaf too small");
+  if (d.nrhs_max < 1) return set_err(HODLR_ERR_INVALID_ARG, "nrhs_max must be >= 1");
+  if (d.precision != HODLR_PREC_FP64 && d.precision != HODLR_PREC_MIXED)
+    return set_err(HODLR_ERR_INVALID_ARG, "unknown precision mode");
+  if (d.precision == HODLR_PREC_MIXED && !(d.refine_tol > 0.0))
+    return set_err(HODLR_ERR_INVALID_ARG, "mixed mode needs refine_tol > 0");
+  if ((long long)d.leaf * d.leaf * 8 > (1LL << 31)) return set_err(HODLR_ERR_INVALID_ARG, "leaf too large");
+  hodlr_ctx *h = new hodlr_ctx();
+  h->d = d;
+  h->n = d.n;
+  h->m = d.leaf;
+  h->L = d.levels;
+  h->r = d.levels > 0 ? d.rank : std::max(1, d.rank);
+  h->nleaf = 1 << d.levels;
+  h->nnode = (1 << d.levels) - 1;
+  h->kmax = d.nrhs_max;
+  h->mixed = d.precision == HODLR_PREC_MIXED;
+  h->has_level.assign(h->L, 0);
+  if (d.stream) {
+    h->st = (cudaStream_t)d.stream;
+  } else {
+    cudaError_t e = cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+      delete h;
+      return set_err(HODLR_ERR_CUDA, cudaGetErrorString(e));
+    }
+    h->own_stream = true;
+  }
+  plan_sizes(h);
+  const long long n = h->n;
+  const int m = h->m, L = h->L, r = h->r, k = h->kmax;
+  cudaError_t e = cudaSuccess;
+#define ALLOC(ptr, T, cnt)                                                    \
+  do {                                                                        \
+    ptr = h->alloc<T>((size_t)(cnt), e);                                      \
+    if (e != cudaSuccess) {                                                   \
+      free_ctx(h);                                                            \
+      return set_err(HODLR_ERR_OUT_OF_MEMORY, std::string("cudaMalloc ") + #ptr); \
+    }                                                                         \
+  } while (0)
+  ALLOC(h->D, double, (size_t)h->nleaf * m * m);
+  ALLOC(h->U, double, (size_t)n * L * r);
+  ALLOC(h->V, double, (size_t)n * L * r);
+  ALLOC(h->s, double, (size_t)std::max(1, L) * r);
+  ALLOC(h->ipiv, int, (size_t)n);
+  ALLOC(h->capLU, double, (size_t)std::max(1, h->nnode) * 4 * r * r);
+  ALLOC(h->cap_ipiv, int, (size_t)std::max(1, h->nnode) * 2 * r);
+  if (h->mixed) {
+    ALLOC(h->LU32, float, (size_t)h->nleaf * m * m);
+    ALLOC(h->V32, float, (size_t)n * L * r);
+    ALLOC(h->Ut32, float, (size_t)n * L * r);
+    ALLOC(h->X32, float, (size_t)n * k);
+    ALLOC(h->X64, double, (size_t)n * k);
+    ALLOC(h->R64, double, (size_t)n * k);
+    ALLOC(h->B64, double, (size_t)n * k);
+  } else {
+    ALLOC(h->LU, double, (size_t)h->nleaf * m * m);
+    ALLOC(h->Ut, double, (size_t)n * L * r);
+  }
+  ALLOC(h->Tbuf, double, h->tbuf_elems);
+  ALLOC(h->Wbuf, double, h->tbuf_elems);
+  ALLOC(h->eta, double, h->eta_elems);
+  ALLOC(h->red, double, h->red_elems);
+  ALLOC(h->norms, double, 2 * (size_t)k);
+  ALLOC(h->nwork, double, (size_t)k * 64);
+  ALLOC(h->dst, DevStatus, 1);
+#undef ALLOC
+  if (cudaMallocHost(&h->hst, sizeof(DevStatus)) != cudaSuccess) {
+    free_ctx(h);
+    return set_err(HODLR_ERR_OUT_OF_MEMORY, "cudaMallocHost");
+  }
+  for (auto &ev : h->ev)
+    if (cudaEventCreate(&ev) != cudaSuccess) {
+      free_ctx(h);
+      return set_err(HODLR_ERR_CUDA, "cudaEventCreate");
+    }
+  if (L > 0) {
+    cudaError_t fe = launch_fill(h->s, (long long)L * r, 1.0, h->st);
+    if (fe != cudaSuccess) {
+      free_ctx(h);
+      return set_err(HODLR_ERR_CUDA, cudaGetErrorString(fe));
+    }
+  }
+  if (cudaMemsetAsync(h->dst, 0, sizeof(DevStatus), h->st) != cudaSuccess ||
+      cudaStreamSynchronize(h->st) != cudaSuccess) {
+    free_ctx(h);
+    return set_err(HODLR_ERR_CUDA, "initialisation");
+  }
+  *out = h;
+  return HODLR_OK;
+}
+
+int hodlr_destroy(hodlr_handle h) {
+  if (!h) return HODLR_OK;
+  cudaStreamSynchronize(h->st);
+  free_ctx(h);
+  return HODLR_OK;
+}
+
+int hodlr_set_stream(hodlr_handle h, void *stream) {
+  if (!h) return set_err(HODLR_ERR_INVALID_ARG, "null handle");
+  CK(cudaStreamSynchronize(h->st));
+  if (h->own_stream) cudaStreamDestroy(h->st);
+  h->own_stream = false;
+  if (stream) {
+    h->st = (cudaStream_t)stream;
+  } else {
+    CK(cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking));
+    h->own_stream = true;
+  }
+  return HODLR_OK;
+}
+
+int hodlr_set_leaf_blocks(hodlr_handle h, const double *D, int64_t ld, int64_t leaf_stride) {
+  if (!h || !D) return set_err(HODLR_ERR_INVALID_ARG, "null argument");
+  if (ld < h->m) return set_err(HODLR_ERR_INVALID_ARG, "ld < leaf size");
+  CK(launch_pack_leaves(D, ld, leaf_stride, h->D, h->m, h->nleaf, h->st));
+  h->has_D = true;
+  h->factored = false;
+  return HODLR_OK;
+}
+
+int hodlr_set_lowrank(hodlr_handle h, int level, const double *U, int64_t ldu, const double *V, int64_t ldv,
+                      const double *s) {
+  if (!h || !U || !V) return set_err(HODLR_ERR_INVALID_ARG, "null argument");
+  if (level < 0 || level >= h->L) return set_err(HODLR_ERR_INVALID_ARG, "level out of range");
+  if (ldu < h->n || ldv < h->n) return set_err(HODLR_ERR_INVALID_ARG, "ld < n");
+  CK((launch_convert<double, double>(U, ldu, h->Ulev(level), h->n, h->n, h->r, h->st)));
+  CK((launch_convert<double, double>(V, ldv, h->Vlev(level), h->n, h->n, h->r, h->st)));
+  if (s)
+    CK(cudaMemcpyAsync(h->slev(level), s, sizeof(double) * h->r, cudaMemcpyDefault, h->st));
+  else
+    CK(launch_fill(h->slev(level), h->r, 1.0, h->st));
+  h->has_level[level] = 1;
+  h->factored = false;
+  return HODLR_OK;
+}
+
+int hodlr_factor(hodlr_handle h) {
+  if (!h) return set_err(HODLR_ERR_INVALID_ARG, "null handle");
+  if (!h->has_D) return set_err(HODLR_ERR_NOT_FACTORED, "leaf blocks not set");
+  for (int l = 0; l < h->L; ++l)
+    if (!h->has_level[l]) return set_err(HODLR_ERR_NOT_FACTORED, "low-rank level not set");
+  h->factored = false;
+  CKS(reset_status(h));
+  CK(cudaEventRecord(h->ev[0], h->st));
+  int rc = run_graphed(h, h->factor_graph, h->factor_runs, [&]() -> int {
+    if (h->mixed) {
+      if (h->L > 0)
+        CK((launch_convert<double, float>(h->V, h->n, h->V32, h->n, h->n, h->L * h->r, h->st)));
+      return factor_sweep<float>(h);
+    }
+    return factor_sweep<double>(h);
+  });
+  CKS(rc);
+  CK(cudaEventRecord(h->ev[1], h->st));
+  CKS(sync_status(h, nullptr));
+  cudaEventElapsedTime(&h->factor_ms, h->ev[0], h->ev[1]);
+  h->factored = true;
+  return HODLR_OK;
+}
+
+static int solve_impl(hodlr_handle h, double *B, int64_t ldb, int nrhs, hodlr_solve_info *info, bool trans) {
+  if (!h || !B) return set_err(HODLR_ERR_INVALID_ARG, "null argument");
+  if (!h->factored) return set_err(HODLR_ERR_NOT_FACTORED, "call hodlr_factor first");
+  if (nrhs < 1 || nrhs > h->kmax) return set_err(HODLR_ERR_INVALID_ARG, "nrhs out of range");
+  if (ldb < h->n) return set_err(HODLR_ERR_INVALID_ARG, "ldb < n");
+  CKS(reset_status(h));
+  CK(cudaEventRecord(h->ev[2], h->st));
+  auto key = std::make_tuple((const double *)B, (long long)ldb, nrhs, trans ? 1 : 0);
+  if (h->solve_graphs.size() > 32 && !h->solve_graphs.count(key)) {  // bound the graph cache
+    for (auto &g : h->solve_graphs)
+      if (g.second.exec) cudaGraphExecDestroy(g.second.exec);
+    h->solve_graphs.clear();
+    h->solve_runs.clear();
+  }
+  int rc = run_graphed(h, h->solve_graphs[key], h->solve_runs[key], [&]() -> int {
+    CK(launch_check_finite(B, ldb, h->n, nrhs, h->dst, h->st));
+    if (h->mixed) return mixed_solve(h, B, ldb, nrhs, trans);
+    return solve_sweep<double>(h, B, ldb, nrhs, trans, nullptr);
+  });
+  CKS(rc);
+  CK(cudaEventRecord(h->ev[3], h->st));
+  if (info) {
+    info->iterations = 0;
+    info->rel_residual = -1.0;
+  }
+  int st = sync_status(h, info);
+  cudaEventElapsedTime(&h->solve_ms, h->ev[2], h->ev[3]);
+  if (st != HODLR_OK) return st;
+  if (h->mixed && !h->hst->done) {
+    char buf[128];
+    snprintf(buf, sizeof buf, "refinement stopped at relative residual %.3e after %d corrections",
+             h->hst->resid, h->hst->iters);
+    if (info) info->status = HODLR_ERR_NOT_CONVERGED;
+    return set_err(HODLR_ERR_NOT_CONVERGED, buf);
+  }
+  if (!h->mixed && info) info->rel_residual = -1.0;
+  return HODLR_OK;
+}
+
+int hodlr_solve(hodlr_handle h, double *B, int64_t ldb, int nrhs, hodlr_solve_info *info) {
+  return solve_impl(h, B, ldb, nrhs, info, false);
+}
+
+int hodlr_solve_transpose(hodlr_handle h, double *B, int64_t ldb, int nrhs, hodlr_solve_info *info) {
+  return solve_impl(h, B, ldb, nrhs, info, true);
+}
+
+int hodlr_matvec(hodlr_handle h, int transpose, const double *X, int64_t ldx, double *Y, int64_t ldy, int nrhs) {
+  if (!h || !X || !Y) return set_err(HODLR_ERR_INVALID_ARG, "null argument");
+  if (nrhs < 1 || nrhs > h->kmax) return set_err(HODLR_ERR_INVALID_ARG, "nrhs out of range");
+  if (ldx < h->n || ldy < h->n) return set_err(HODLR_ERR_INVALID_ARG, "ld < n");
+  CKS(reset_status(h));
+  CKS(matvec_fp64(h, transpose != 0, X, ldx, nullptr, 0, Y, ldy, nrhs, 1.0, nullptr));
+  return sync_status(h, nullptr);
+}
+
+int hodlr_adjoint(hodlr_handle h, const double *x, int64_t ldx, const double *g, int64_t ldg, int nrhs,
+                  hodlr_grads *gr) {
+  if (!h || !x || !g || !gr) return set_err(HODLR_ERR_INVALID_ARG, "null argument");
+  if (!h->factored) return set_err(HODLR_ERR_NOT_FACTORED, "call hodlr_factor first");
+  if (nrhs < 1 || nrhs > h->kmax) return set_err(HODLR_ERR_INVALID_ARG, "nrhs out of range");
+  const long long n = h->n;
+  const int m = h->m, L = h->L, r = h->r, k = nrhs;
+  // lambda = A^{-T} g, held in the caller's db if given, else in a scratch buffer
+  double *lam = gr->db;
+  long long ldl = gr->ldb;
+  double *scratch = nullptr;
+  if (!lam) {
+    CK(cudaMallocAsync(&scratch, sizeof(double) * n * k, h->st));
+    lam = scratch;
+    ldl = n;
+  } else if (ldl < n) {
+    return set_err(HODLR_ERR_INVALID_ARG, "grads->ldb < n");
+  }
+  CK(launch_axpy(g, ldg, lam, ldl, n, k, 1.0, false, nullptr, h->st));
+  int rc = solve_impl(h, lam, ldl, k, nullptr, true);
+  if (rc != HODLR_OK) {
+    if (scratch) cudaFreeAsync(scratch, h->st);
+    return rc;
+  }
+  cudaStream_t s = h->st;
+  if (gr->dD) {
+    CK(cudaMemsetAsync(gr->dD, 0, sizeof(double) * h->nleaf * m * m, s));
+    UpdateArgs ua{};
+    ua.A = lam;
+    ua.lda = ldl;
+    ua.a_bstride = m;
+    ua.B = x;
+    ua.ldb = ldx;
+    ua.b_s1 = 2LL * m;
+    ua.b_s2 = m;
+    ua.b_trans = 1;
+    ua.C = gr->dD;
+    ua.ldc = m;
+    ua.c_bstride = (long long)m * m;
+    ua.M = m;
+    ua.N = m;
+    ua.K = k;
+    ua.nbatch = h->nleaf;
+    ua.alpha = -1.0;
+    CK(launch_update_nn<double>(ua, s));
+  }
+  for (int l = 0; l < L && (gr->dU || gr->dV || gr->ds); ++l) {
+    const int nb = 2 << l;
+    const long long rows = n >> (l + 1);
+    CK(launch_reduce_tn<double>(h->Vlev(l), n, x, ldx, rows, nb, r, k, h->Tbuf, h->red, nullptr, s));
+    CK(launch_reduce_tn<double>(h->Ulev(l), n, lam, ldl, rows, nb, r, k, h->Wbuf, h->red, nullptr, s));
+    for (int which = 0; which < 2; ++which) {
+      double *dst = which == 0 ? gr->dU : gr->dV;
+      if (!dst) continue;
+      dst += (long long)l * n * r;
+      CK(cudaMemsetAsync(dst, 0, sizeof(double) * n * r, s));
+      UpdateArgs ua{};
+      ua.A = which == 0 ? lam : x;
+      ua.lda = which == 0 ? ldl : ldx;
+      ua.a_bstride = rows;
+      ua.B = which == 0 ? h->Tbuf : h->Wbuf;
+      ua.ldb = r;
+      ua.b_s1 = 2LL * r * k;
+      ua.b_s2 = (long long)r * k;
+      ua.b_flip = 1;
+      ua.b_trans = 1;
+      ua.scale = h->slev(l);
+      ua.scale_cols = 1;
+      ua.C = dst;
+      ua.ldc = n;
+      ua.c_bstride = rows;
+      ua.M = (int)rows;
+      ua.N = r;
+      ua.K = k;
+      ua.nbatch = nb;
+      ua.alpha = -1.0;
+      CK(launch_update_nn<double>(ua, s));
+    }
+    if (gr->ds) CK(launch_scale_grad(h->Wbuf, h->Tbuf, r, k, nb, gr->ds + (long long)l * r, s));
+  }
+  if (scratch) CK(cudaFreeAsync(scratch, s));
+  CKS(sync_status(h, nullptr));
+  return HODLR_OK;
+}
+
+int hodlr_get_factors(hodlr_handle h, double *leaf_lu, int32_t *leaf_ipiv, double *utilde, double *cap_lu,
+                      int32_t *cap_ipiv) {
+  if (!h) return set_err(HODLR_ERR_INVALID_ARG, "null handle");
+  if (!h->factored) return set_err(HODLR_ERR_NOT_FACTORED, "not factored");
+  const long long n = h->n;
+  const int m = h->m, L = h->L, r = h->r;
+  cudaStream_t s = h->st;
+  if (leaf_lu) {
+    if (h->mixed)
+      CK((launch_convert<float, double>(h->LU32, (long long)h->nleaf * m * m, leaf_lu, (long long)h->nleaf * m * m,
+                                        (long long)h->nleaf * m * m, 1, s)));
+    else
+      CK(cudaMemcpyAsync(leaf_lu, h->LU, sizeof(double) * h->nleaf * m * m, cudaMemcpyDeviceToDevice, s));
+  }
+  if (leaf_ipiv) CK(cudaMemcpyAsync(leaf_ipiv, h->ipiv, sizeof(int) * n, cudaMemcpyDeviceToDevice, s));
+  if (utilde && L > 0) {
+    if (h->mixed)
+      CK((launch_convert<float, double>(h->Ut32, n, utilde, n, n, L * r, s)));
+    else
+      CK(cudaMemcpyAsync(utilde, h->Ut, sizeof(double) * n * L * r, cudaMemcpyDeviceToDevice, s));
+  }
+  if (cap_lu && h->nnode > 0)
+    CK(cudaMemcpyAsync(cap_lu, h->capLU, sizeof(double) * h->nnode * 4 * r * r, cudaMemcpyDeviceToDevice, s));
+  if (cap_ipiv && h->nnode > 0)
+    CK(cudaMemcpyAsync(cap_ipiv, h->cap_ipiv, sizeof(int) * h->nnode * 2 * r, cudaMemcpyDeviceToDevice, s));
+  CK(cudaStreamSynchronize(s));
+  return HODLR_OK;
+}
+
+int hodlr_last_timings(hodlr_handle h, double *factor_ms, double *solve_ms) {
+  if (!h) return set_err(HODLR_ERR_INVALID_ARG, "null handle");
+  if (factor_ms) *factor_ms = h->factor_ms;
+  if (solve_ms) *solve_ms = h->solve_ms;
+  return HODLR_OK;
+}
+
+int hodlr_generate(hodlr_handle h, uint64_t seed, double shift, int orthonormal, double decay, double *B,
+                   int64_t ldb, int nrhs) {
+  if (!h) return set_err(HODLR_ERR_INVALID_ARG, "null handle");
+  const long long n = h->n;
+  const int m = h->m, L = h->L, r = h->r;
+  cudaStream_t s = h->st;
+  CKS(reset_status(h));
+  CK(launch_gen_leaves(h->D, m, h->nleaf, seed, shift, s));
+  h->has_D = true;
+  double *tmp = nullptr;
+  if (orthonormal && L > 0) CK(cudaMallocAsync(&tmp, sizeof(double) * n * r, s));
+  for (int l = 0; l < L; ++l) {
+    const int nb = 2 << l;
+    const long long rows = n >> (l + 1);
+    for (int w = 0; w < 2; ++w) {
+      double *X = w == 0 ? h->Ulev(l) : h->Vlev(l);
+      const unsigned long long stream = 0x100ull + 2ull * l + w;
+      CK(launch_gaussian(X, n, n, r, seed, stream, orthonormal ? 1.0 : 1.0 / std::sqrt((double)rows), s));
+      if (!orthonormal) continue;
+      for (int pass = 0; pass < 2; ++pass) {  // CholeskyQR2 per child block
+        CK(launch_reduce_tn<double>(X, n, X, n, rows, nb, r, r, h->Tbuf, h->red, nullptr, s));
+        CK(launch_chol_inv(h->Tbuf, h->eta, r, nb, h->dst, s));
+        CK(cudaMemsetAsync(tmp, 0, sizeof(double) * n * r, s));
+        UpdateArgs ua{};
+        ua.A = X;
+        ua.lda = n;
+        ua.a_bstride = rows;
+        ua.B = h->eta;
+        ua.ldb = r;
+        ua.b_s1 = 2LL * r * r;
+        ua.b_s2 = (long long)r * r;
+        ua.C = tmp;
+        ua.ldc = n;
+        ua.c_bstride = rows;
+        ua.M = (int)rows;
+        ua.N = r;
+        ua.K = r;
+        ua.nbatch = nb;
+        ua.alpha = 1.0;
+        CK(launch_update_nn<double>(ua, s));
+        CK(cudaMemcpyAsync(X, tmp, sizeof(double) * n * r, cudaMemcpyDeviceToDevice, s));
+      }
+    }
+    std::vector<double> sv(r, 1.0);
+    if (decay > 0)
+      for (int i = 0; i < r; ++i) sv[i] = std::pow(10.0, -decay * i / r);
+    CK(cudaMemcpyAsync(h->slev(l), sv.data(), sizeof(double) * r, cudaMemcpyHostToDevice, s));
+    CK(cudaStreamSynchronize(s));  // sv is pageable host memory
+    h->has_level[l] = 1;
+  }
+  if (tmp) CK(cudaFreeAsync(tmp, s));
+  if (B) CK(launch_gaussian(B, ldb, n, nrhs, seed, 0xBull, 1.0, s));
+  h->factored = false;
+  return sync_status(h, nullptr);
+}
+
+// --------------------------------------------------- reference hsolve
+static int is_device_ptr(const void *p) {
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+}
+
+int hodlr_hsolve_ex(int nrow, int nrhs, int rank, int nPart, int LD, double *K, double *U, double *V,
+                    int precision, void *stream, hodlr_solve_info *info) {
+  if (!K || !U || nrow < 1 || nPart < 1 || nrhs < 1 || LD < nrow)
+    return set_err(HODLR_ERR_INVALID_ARG, "hsolve: bad arguments");
+  if ((nPart & (nPart - 1)) != 0 || nrow % nPart != 0)
+    return set_err(HODLR_ERR_INVALID_ARG, "hsolve: nPart must be a power of two dividing nrow");
+  int L = 0;
+  while ((1 << L) < nPart) ++L;
+  const int m = nrow / nPart;
+  if (L > 0 && (!V || rank < 1 || rank > 64)) return set_err(HODLR_ERR_INVALID_ARG, "hsolve: rank in [1,64]");
+  const int r = L > 0 ? rank : 1;
+  const int ucols = nrhs + L * r;
+  const bool dev = is_device_ptr(K) && is_device_ptr(U) && (L == 0 || is_device_ptr(V));
+  if (stream && !dev) return set_err(HODLR_ERR_INVALID_ARG, "hsolve_ex: a stream needs device pointers");
+  hodlr_desc d{};
+  d.n = nrow;
+  d.leaf = m;
+  d.levels = L;
+  d.rank = r;
+  d.nrhs_max = nrhs;
+  d.precision = precision;
+  d.residual = HODLR_RESID_FP64_EMULATED;
+  d.refine_tol = 1e-12;
+  d.refine_max_iter = 10;
+  d.stream = stream;
+  hodlr_handle h = nullptr;
+  CKS(hodlr_create(&d, &h));
+  double *dK = K, *dU = U, *dV = V;
+  long long ld = LD;
+  int rc = HODLR_OK;
+  std::vector<void *> tmp;
+  auto fail = [&](int code) {
+    for (void *p : tmp) cudaFree(p);
+    hodlr_destroy(h);
+    return code;
+  };
+  if (!dev) {  // stage host buffers through the device, packed (ld = nrow)
+    ld = nrow;
+    const size_t bk = sizeof(double) * nrow * m, bu = sizeof(double) * nrow * ucols,
+                 bv = sizeof(double) * nrow * r;
+    dK = dU = dV = nullptr;
+    if (cudaMalloc(&dK, bk) == cudaSuccess) tmp.push_back(dK);
+    if (cudaMalloc(&dU, bu) == cudaSuccess) tmp.push_back(dU);
+    if (cudaMalloc(&dV, bv) == cudaSuccess) tmp.push_back(dV);
+    if (tmp.size() != 3) return fail(set_err(HODLR_ERR_OUT_OF_MEMORY, "hsolve: staging buffers"));
+    if (cudaMemcpy2DAsync(dK, sizeof(double) * nrow, K, sizeof(double) * LD, sizeof(double) * nrow, m,
+                          cudaMemcpyHostToDevice, h->st) != cudaSuccess ||
+        cudaMemcpy2DAsync(dU, sizeof(double) * nrow, U, sizeof(double) * LD, sizeof(double) * nrow, ucols,
+                          cudaMemcpyHostToDevice, h->st) != cudaSuccess ||
+        (L > 0 && cudaMemcpy2DAsync(dV, sizeof(double) * nrow, V, sizeof(double) * LD, sizeof(double) * nrow, r,
+                                    cudaMemcpyHostToDevice, h->st) != cudaSuccess))
+      return fail(set_err(HODLR_ERR_CUDA, "hsolve: host to device copy"));
+  }
+  if ((rc = hodlr_set_leaf_blocks(h, dK, ld, m)) != HODLR_OK) return fail(rc);
+  for (int l = 0; l < L; ++l)
+    if ((rc = hodlr_set_lowrank(h, l, dU + (long long)(nrhs + l * r) * ld, ld, dV, ld, nullptr)) != HODLR_OK)
+      return fail(rc);
+  if ((rc = hodlr_factor(h)) != HODLR_OK) return fail(rc);
+  if ((rc = hodlr_solve(h, dU, ld, nrhs, info)) != HODLR_OK) return fail(rc);
+  // write back: K <- leaf LU (stacked, ld), U columns nrhs.. <- Utilde
+  cudaStream_t s = h->st;
+  {
+    cudaError_t e = h->mixed ? launch_unpack_leaves<float>(h->LU32, dK, ld, m, m, h->nleaf, s)
+                             : launch_unpack_leaves<double>(h->LU, dK, ld, m, m, h->nleaf, s);
+    if (e != cudaSuccess) return fail(set_err(HODLR_ERR_CUDA, "hsolve: LU write-back"));
+  }
+  if (L > 0) {
+    cudaError_t e;
+    if (h->mixed)
+      e = launch_convert<float, double>(h->Ut32, h->n, dU + (long long)nrhs * ld, ld, h->n, L * r, s);
+    else
+      e = cudaMemcpy2DAsync(dU + (long long)nrhs * ld, sizeof(double) * ld, h->Ut, sizeof(double) * h->n,
+                            sizeof(double) * h->n, L * r, cudaMemcpyDeviceToDevice, s);
+    if (e != cudaSuccess) return fail(set_err(HODLR_ERR_CUDA, "hsolve: Utilde write-back"));
+  }
+  if (!dev) {
+    if (cudaMemcpy2DAsync(K, sizeof(double) * LD, dK, sizeof(double) * nrow, sizeof(double) * nrow, m,
+                          cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+        cudaMemcpy2DAsync(U, sizeof(double) * LD, dU, sizeof(double) * nrow, sizeof(double) * nrow, ucols,
+                          cudaMemcpyDeviceToHost, s) != cudaSuccess)
+      return fail(set_err(HODLR_ERR_CUDA, "hsolve: device to host copy"));
+  }
+  if (cudaStreamSynchronize(s) != cudaSuccess) return fail(set_err(HODLR_ERR_CUDA, "hsolve: sync"));
+  return fail(HODLR_OK);
+}
+
+int hodlr_hsolve(int nrow, int nrhs, int rank, int nPart, int LD, double *K, double *U, double *V) {
+  return hodlr_hsolve_ex(nrow, nrhs, rank, nPart, LD, K, U, V, HODLR_PREC_FP64, nullptr, nullptr);
+}
+
+}  // extern "C"

@@ -1,0 +1,127 @@
+// Launchers of the HODLR kernels (host side).  Every launcher enqueues on
+// the given stream and returns the launch error (if any).
+#pragma once
+#include "common.cuh"
+
+namespace hodlr {
+
+// ------------------------------------------------------------------ leaves
+// K1: LU with partial pivoting of every leaf block.  D: leaf i at
+// D + i*d_stride (FP64, column-major, ld d_ld).  LU: packed [nleaf][m][m]
+// of type T.  ipiv: [nleaf][m], 1-based.  Zero pivots / non-finite entries
+// are reported in *st.
+template <typename T>
+cudaError_t launch_leaf_getrf(const double *D, long long d_ld, long long d_stride, T *LU, int *ipiv,
+                              int m, int nleaf, DevStatus *st, cudaStream_t s);
+
+// K2: X := D_i^{-1} X (or D_i^{-T} X) on the rows of every leaf i for the
+// columns [0, ncols) of X (ld ldx).  skip (device flag, may be NULL): when
+// *skip != 0 the kernel returns immediately.
+template <typename T>
+cudaError_t launch_leaf_getrs(const T *LU, const int *ipiv, int m, int nleaf, T *X, long long ldx,
+                              int ncols, bool trans, const int *skip, cudaStream_t s);
+
+// ----------------------------------------------------------- level steps
+// K3: Out_b = A_b^T X_b (r x C, FP64 result) for batches b in [0, nbatch),
+// A_b / X_b = rows [b*nrows, (b+1)*nrows) of A (N x r, lda) / X (N x C, ldx).
+// Split over row chunks with a deterministic second pass.  Out: [nbatch]
+// blocks of r x C column-major (ld r).  work: scratch of at least
+// reduce_workspace_doubles(...) doubles.
+size_t reduce_workspace_doubles(long long nrows, int nbatch, int r, int C, int elem_bytes);
+template <typename T>
+cudaError_t launch_reduce_tn(const T *A, long long lda, const T *X, long long ldx, long long nrows,
+                             int nbatch, int r, int C, double *out, double *work, const int *skip,
+                             cudaStream_t s);
+
+// K5: C_b += alpha * A_b * diag(scale) * op(B_b) for b in [0, nbatch):
+//   A_b = A + b*a_bstride (M x K, lda), C_b = C + b*c_bstride (M x N, ldc),
+//   B_b = B + (b >> 1) * b_s1 + ((b & 1) ^ b_flip) * b_s2 (FP64), op(B_b) is
+//   K x N: element (q, j) at B_b[q + j*ldb] (b_trans = 0) or B_b[j + q*ldb].
+//   scale (optional, FP64) multiplies the inner index q (scale_cols = 0) or
+//   the output column j (scale_cols = 1).
+struct UpdateArgs {
+  const void *A; long long lda; long long a_bstride; int a_trans;  // a_trans: A_b(i,q) at A_b[q + i*lda]
+  const double *B; long long ldb; long long b_s1, b_s2; int b_flip; int b_trans;
+  const double *scale; int scale_cols;
+  void *C; long long ldc; long long c_bstride;
+  int M, N, K, nbatch;
+  double alpha;
+  const int *skip;
+};
+template <typename T>
+cudaError_t launch_update_nn(const UpdateArgs &a, cudaStream_t s);
+
+// K4: capacitance systems of the nodes at one depth.
+//   T-blocks: Tb + c*tb_stride is child c's r x Ct block (ld r), Ct >= C + (factor ? r : 0).
+//   forward (trans = false):  S = [I, s.T1u; s.T0u, I], RHS = [s.T1d; s.T0d]
+//   transposed:               S^T z = [T0d; T1d]
+//   factor = true: S is built from the T-blocks' last r columns (columns
+//   C..C+r), factorised and stored in cap_lu[node] (2r x 2r, ld 2r) /
+//   cap_ipiv[node]; otherwise the stored factors are used.  The solution
+//   (2r x C per node, ld 2r) is written to eta + node*2r*C.
+struct CapArgs {
+  const double *Tb; long long tb_stride;
+  const double *scale;   // r entries or NULL
+  double *cap_lu; int *cap_ipiv;
+  double *eta;
+  int r, C, nnode, node_base;  // node ids node_base + p
+  bool factor, trans;
+  DevStatus *st;
+  const int *skip;
+};
+cudaError_t launch_capacitance(const CapArgs &a, cudaStream_t s);
+
+// --------------------------------------------------------------- helpers
+// Y[i, j] = (T) X[i, j] for an n x c column-major tile.
+template <typename Tin, typename Tout>
+cudaError_t launch_convert(const Tin *X, long long ldx, Tout *Y, long long ldy, long long n, int c,
+                           cudaStream_t s);
+// Pack leaf blocks (leaf i at D + i*stride, ld) into [nleaf][m][m].
+cudaError_t launch_pack_leaves(const double *D, long long ld, long long stride, double *out, int m,
+                               int nleaf, cudaStream_t s);
+// Inverse of launch_pack_leaves: [nleaf][m][m] (type T) into leaf i at
+// out + i*stride (FP64, ld).
+template <typename T>
+cudaError_t launch_unpack_leaves(const T *in, double *out, long long ld, long long stride, int m, int nleaf,
+                                 cudaStream_t s);
+// Y = X (FP64 copy of an n x c tile), optionally accumulate: Y += alpha*X.
+cudaError_t launch_axpy(const double *X, long long ldx, double *Y, long long ldy, long long n, int c,
+                        double alpha, bool accumulate, const int *skip, cudaStream_t s);
+// Y = X + (double) D  (FP64 accumulate a lower-precision correction), Y may alias X.
+template <typename Td>
+cudaError_t launch_add_correction(const double *X, long long ldx, const Td *D, long long ldd,
+                                  double *Y, long long ldy, long long n, int c, const int *skip,
+                                  cudaStream_t s);
+// Column norms ||X_j||_2 (FP64) into out[j]; deterministic.
+cudaError_t launch_colnorms(const double *X, long long ldx, long long n, int c, double *out,
+                            double *work, const int *skip, cudaStream_t s);
+// Refinement control: rel = max_j rnorm[j]/bnorm[j]; st->resid = rel;
+// if rel <= tol set st->done = 1.  If advance, count an iteration when not done.
+cudaError_t launch_refine_check(const double *rnorm, const double *bnorm, int c, double tol,
+                                DevStatus *st, int advance, cudaStream_t s);
+// Scan X (n x c) for NaN/Inf; report HODLR_ERR_NONFINITE_INPUT with the row.
+cudaError_t launch_check_finite(const double *X, long long ldx, long long n, int c, DevStatus *st,
+                                cudaStream_t s);
+cudaError_t launch_fill(double *X, long long n, double v, cudaStream_t s);
+
+// ds[j] = -sum_b sum_q W_b[j, q] * T_{b^1}[j, q] (blocks r x k, ld r), FP64.
+cudaError_t launch_scale_grad(const double *W, const double *T, int r, int k, int nbatch, double *ds,
+                              cudaStream_t s);
+
+// ------------------------------------------------------------- generator
+// Counter-based N(0,1) samples: X[i + j*ld] = scale * g(seed, stream, i + j*n).
+cudaError_t launch_gaussian(double *X, long long ld, long long n, int c, unsigned long long seed,
+                            unsigned long long stream, double scale, cudaStream_t s);
+// Leaf blocks [nleaf][m][m] = G/sqrt(m) + shift*I.
+cudaError_t launch_gen_leaves(double *D, int m, int nleaf, unsigned long long seed, double shift,
+                              cudaStream_t s);
+// Per-block Cholesky of Gram matrices G_b (r x r, ld r) and the inverse of
+// the upper factor: Rinv_b (r x r, ld r), G = R^T R.  Reports failure in st.
+cudaError_t launch_chol_inv(const double *G, double *Rinv, int r, int nbatch, DevStatus *st,
+                            cudaStream_t s);
+
+// ---------------------------------------------------------- residual (FP64 emulated)
+// R_b -= D_b X_b (leaf part) and R_c -= U_c (s . V_{c^1}^T X_{c^1}) with
+// double-FP32 arithmetic; declared in resid_emul.cu.
+
+}  // namespace hodlr

@@ -1,0 +1,199 @@
+/*
+ * hodlr_gb300.h -- C ABI of the GB300 HODLR (hierarchically off-diagonal
+ * low-rank) fast direct solver.
+ *
+ * The matrix is A = blockdiag(D_leaf) + hierarchical off-diagonal low rank:
+ * for a node p at depth l (root depth 0, leaves at depth L) with children
+ * c0, c1,
+ *     A[c0,c1] = U^(l)_c0 diag(s^(l)) V^(l)_c1^T,
+ *     A[c1,c0] = U^(l)_c1 diag(s^(l)) V^(l)_c0^T,
+ * where U^(l), V^(l) are N x r and X_c denotes the rows of child c.
+ * fastSolver2 is the special case U^(l) = U, V^(l) = V, s = 1 for every l,
+ * i.e. A = U V^T + diag(D) (src/tasks/dense_block.cc:63-75, tests/test.cc:654).
+ *
+ * Conventions (as in the reference, src/ptr_matrix.cc:29-37): FP64,
+ * column-major, explicit leading dimensions.  Every entry point returns an
+ * int status (HODLR_OK = 0); hodlr_last_error_string() describes the last
+ * failure on the calling thread.  Calls on one handle are ordered on the
+ * handle's CUDA stream; a handle is not thread-safe, distinct handles are.
+ */
+#ifndef HODLR_GB300_H
+#define HODLR_GB300_H
+
+#include <stdint.h>
+
+#if defined(__GNUC__)
+#define HODLR_API __attribute__((visibility("default")))
+#else
+#define HODLR_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---------------------------------------------------------------- status */
+enum {
+  HODLR_OK = 0,
+  HODLR_ERR_INVALID_ARG = 1,
+  HODLR_ERR_CUDA = 2,
+  HODLR_ERR_SINGULAR_LEAF = 3,          /* zero pivot in a leaf LU (index = leaf) */
+  HODLR_ERR_SINGULAR_CAPACITANCE = 4,   /* zero pivot in a 2r x 2r system (index = node) */
+  HODLR_ERR_NOT_CONVERGED = 5,          /* refinement hit its iteration cap */
+  HODLR_ERR_NONFINITE_INPUT = 6,        /* NaN/Inf in an input (index = row) */
+  HODLR_ERR_TIMEOUT = 7,                /* a bounded device wait expired */
+  HODLR_ERR_NOT_FACTORED = 8,           /* solve before factor / inputs incomplete */
+  HODLR_ERR_OUT_OF_MEMORY = 9
+};
+
+/* ------------------------------------------------------------- precision */
+enum {
+  HODLR_PREC_FP64 = 0,   /* every step in FP64 */
+  HODLR_PREC_MIXED = 1   /* FP32 leaf LU / low-rank GEMMs, FP64 capacitance,
+                            FP64-accurate residual + iterative refinement */
+};
+
+/* Residual arithmetic of the mixed path. */
+enum {
+  HODLR_RESID_FP64 = 0,          /* native FP64 (DFMA) */
+  HODLR_RESID_FP64_EMULATED = 1  /* FP64-accurate double-FP32 arithmetic on
+                                    the FP32 pipes (error-free products,
+                                    double-word sums) */
+};
+
+typedef struct hodlr_desc {
+  int64_t n;              /* N = leaf * 2^levels */
+  int32_t leaf;           /* m, leaf block size */
+  int32_t levels;         /* L, tree depth (0 = one dense block) */
+  int32_t rank;           /* r, off-diagonal rank (1..64) */
+  int32_t nrhs_max;       /* largest nrhs a solve will be given */
+  int32_t precision;      /* HODLR_PREC_* */
+  int32_t residual;       /* HODLR_RESID_* (mixed path only) */
+  double refine_tol;      /* target max_j ||b_j - A x_j|| / ||b_j|| (mixed), e.g. 1e-12 */
+  int32_t refine_max_iter;/* refinement iteration cap (mixed) */
+  int32_t flags;          /* reserved, 0 */
+  void *stream;           /* cudaStream_t; NULL = legacy default stream */
+} hodlr_desc;
+
+typedef struct hodlr_solve_info {
+  int32_t iterations;     /* refinement corrections applied (0 for FP64) */
+  int32_t status;         /* device status of the call (HODLR_*) */
+  int64_t bad_index;      /* leaf / node / row named by a failing status */
+  double rel_residual;    /* final max_j ||b_j - A x_j|| / ||b_j|| (mixed; -1 if not computed) */
+} hodlr_solve_info;
+
+typedef struct hodlr_ctx *hodlr_handle;
+
+/* Gradients of a scalar loss through x = A^{-1} b, given g = dLoss/dx.
+ * Device pointers; any may be NULL to skip it.  Layouts match the inputs:
+ * dD like the leaf blocks set by hodlr_set_leaf_blocks (packed [leaf][m][m]
+ * column-major), dU[l]/dV[l] N x r column-major with leading dimension n,
+ * ds[l] r entries, db N x nrhs with leading dimension ldb. */
+typedef struct hodlr_grads {
+  double *db;  int64_t ldb;
+  double *dD;
+  double *dU;  /* L blocks of N x r, level l at dU + l*n*r */
+  double *dV;  /* same layout */
+  double *ds;  /* L blocks of r */
+} hodlr_grads;
+
+/* ------------------------------------------------- reference entry point */
+/* Drop-in for fastSolver2's raw-pointer solve
+ *   void hsolve(int nrow, int nrhs, int rank, int nPart, int LD,
+ *               double *K, double *U, double *V)
+ * (src/tasks/leaf_solve.cc:8-10, definition :73-154; called by
+ * LeafSolveTask::cpu_task :69-70).  Same arguments, same in-place result:
+ * K (nrow x nrow/nPart stacked leaf blocks, leading dimension LD) is
+ * overwritten by the leaf LU factors (LAPACK dgesv layout), and U
+ * (nrow x (nrhs + log2(nPart)*rank), leading dimension LD) goes from
+ * [b | U ... U] to [x | Utilde^(0) | ... ], the way hsolve leaves it.
+ * V (nrow x rank, leading dimension LD) is read only; it is shared by all
+ * levels as in the reference.  Pointers may be host or device memory
+ * (host buffers are staged through the device).  Runs on the legacy
+ * default stream in FP64 and returns when the result is in place. */
+HODLR_API int hodlr_hsolve(int nrow, int nrhs, int rank, int nPart, int LD, double *K,
+                 double *U, double *V);
+
+/* hodlr_hsolve with a precision mode and a stream (device pointers only
+ * when stream is not NULL). */
+HODLR_API int hodlr_hsolve_ex(int nrow, int nrhs, int rank, int nPart, int LD,
+                    double *K, double *U, double *V, int precision,
+                    void *stream, hodlr_solve_info *info);
+
+/* ------------------------------------------- factor / solve handle API  */
+/* Replaces HMatrix(nProc, level) + HMatrix::init(U, V, D) + the UTree /
+ * VTree / KTree partitions (src/hmatrix.cc:7-47, src/tree.cc:42-245).      */
+HODLR_API int hodlr_create(const hodlr_desc *desc, hodlr_handle *out);
+HODLR_API int hodlr_destroy(hodlr_handle h);
+HODLR_API int hodlr_set_stream(hodlr_handle h, void *stream);
+
+/* Leaf blocks: leaf i's m x m block starts at D + i*leaf_stride, column-major
+ * with leading dimension ld.  fastSolver2's KTree region (N x m, LD = N,
+ * leaf i at rows i*m) is ld = N, leaf_stride = m
+ * (src/tree.cc:232-245, src/tasks/dense_block.cc:63-75).  Device pointer. */
+HODLR_API int hodlr_set_leaf_blocks(hodlr_handle h, const double *D, int64_t ld,
+                          int64_t leaf_stride);
+
+/* Low-rank factors of level l (0 = root split): U, V are N x r column-major
+ * with leading dimensions ldu, ldv; s is r entries or NULL (= ones).
+ * Replaces the UTree column chunk and VTree::level(i) (src/tree.cc:61-73,
+ * 189-197).  Device pointers. */
+HODLR_API int hodlr_set_lowrank(hodlr_handle h, int level, const double *U, int64_t ldu,
+                      const double *V, int64_t ldv, const double *s);
+
+/* Factorisation: leaf LUs, transformed bases Utilde^(l) = A_c^{-1} U^(l)_c and
+ * the 2r x 2r capacitance LUs of every node -- the work hsolve redoes on
+ * every call with U as extra right-hand sides (src/tasks/leaf_solve.cc:80-153,
+ * src/hmatrix.cc:75-93).  Returns after the device finished (status read). */
+HODLR_API int hodlr_factor(hodlr_handle h);
+
+/* Solve A X = B in place (B device, N x nrhs, leading dimension ldb).  In the
+ * mixed mode this includes FP64 iterative refinement to desc.refine_tol.
+ * Replaces HMatrix::solve (src/hmatrix.cc:49-96).  info may be NULL. */
+HODLR_API int hodlr_solve(hodlr_handle h, double *B, int64_t ldb, int nrhs,
+                hodlr_solve_info *info);
+
+/* Solve A^T X = B in place, reusing the factorisation of A. */
+HODLR_API int hodlr_solve_transpose(hodlr_handle h, double *B, int64_t ldb, int nrhs,
+                          hodlr_solve_info *info);
+
+/* Y = A X (or A^T X) in FP64 from the exact representation (device). */
+HODLR_API int hodlr_matvec(hodlr_handle h, int transpose, const double *X, int64_t ldx,
+                 double *Y, int64_t ldy, int nrhs);
+
+/* Adjoint sweep: lambda = A^{-T} g, then db = lambda and the rank-nrhs outer
+ * products dD_leaf = -lambda_i x_i^T, dU^(l), dV^(l), ds^(l) of
+ * dLoss/dA = -lambda x^T.  x is the forward solution (N x nrhs, ldx),
+ * g = dLoss/dx (N x nrhs, ldg).  Device pointers. */
+HODLR_API int hodlr_adjoint(hodlr_handle h, const double *x, int64_t ldx,
+                  const double *g, int64_t ldg, int nrhs, hodlr_grads *grads);
+
+/* Copy out the factorisation (device pointers; any may be NULL):
+ * leaf LU [nleaf][m][m] column-major + 1-based pivots [nleaf][m],
+ * Utilde (N x L*r, leading dimension N, level l at column l*r),
+ * capacitance LU [nnode][2r][2r] + pivots [nnode][2r] (node of depth l,
+ * position p is 2^l - 1 + p).  FP64 handles only. */
+HODLR_API int hodlr_get_factors(hodlr_handle h, double *leaf_lu, int32_t *leaf_ipiv,
+                      double *utilde, double *cap_lu, int32_t *cap_ipiv);
+
+/* Fill the handle with a seeded synthetic problem on the device
+ * (counter-based Gaussian generator): leaf blocks G/sqrt(m) + shift*I,
+ * per-level U, V ~ N(0,1)/sqrt(n_block) (orthonormal != 0: each child
+ * block's columns orthonormalised instead), s_i = 10^(-decay*i/r) when
+ * decay > 0.  Writes the right-hand side (N x nrhs, ldb) if B != NULL. */
+HODLR_API int hodlr_generate(hodlr_handle h, uint64_t seed, double shift, int orthonormal,
+                   double decay, double *B, int64_t ldb, int nrhs);
+
+/* Milliseconds the last hodlr_factor / hodlr_solve spent on the device
+ * (CUDA events on the handle's stream). */
+HODLR_API int hodlr_last_timings(hodlr_handle h, double *factor_ms, double *solve_ms);
+
+/* Kernels launched by this library since load (for launch accounting). */
+HODLR_API int64_t hodlr_kernel_launches(void);
+
+HODLR_API const char *hodlr_last_error_string(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* HODLR_GB300_H */

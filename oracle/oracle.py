@@ -1,0 +1,233 @@
+"""ctypes front end of the C oracle (TEST INFRASTRUCTURE ONLY).
+
+Only tests/, ``__graft_entry__.smoke()`` and bench.py's CPU-baseline leg
+import this module; it is the checker, never part of the product path.
+
+All matrices are numpy float64 arrays in Fortran (column-major) order, the
+layout fastSolver2 uses throughout (src/ptr_matrix.cc:29-37).
+"""
+import ctypes
+import os
+
+import numpy as np
+
+from . import build as _build
+
+_lib = None
+_ref = None
+
+_dp = ctypes.POINTER(ctypes.c_double)
+_ip = ctypes.POINTER(ctypes.c_int)
+_lp = ctypes.POINTER(ctypes.c_long)
+_i64 = ctypes.c_int64
+
+
+def lib():
+    """Load (building if needed) libhodlr_oracle.so."""
+    global _lib
+    if _lib is None:
+        path = _build.ORACLE_SO
+        if not os.path.exists(path):
+            _build.build_oracle()
+        L = ctypes.CDLL(path)
+        L.orc_seeds.argtypes = [ctypes.c_long, ctypes.c_int, _lp]
+        L.orc_rand_block.argtypes = [ctypes.c_long, ctypes.c_int, ctypes.c_int, _i64, _dp, ctypes.c_int]
+        L.orc_rand_matrix.argtypes = [_lp, ctypes.c_int, ctypes.c_int, ctypes.c_int, _dp, ctypes.c_int]
+        L.orc_dense_blocks.argtypes = [_lp, _lp, _lp, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                       ctypes.c_int, _dp, _i64]
+        L.orc_idamax.argtypes = [ctypes.c_int, _dp]
+        L.orc_idamax.restype = ctypes.c_int
+        L.orc_dgemm.argtypes = [ctypes.c_char, ctypes.c_char, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                ctypes.c_double, _dp, _i64, _dp, _i64, ctypes.c_double, _dp, _i64]
+        L.orc_dgetrf.argtypes = [ctypes.c_int, ctypes.c_int, _dp, _i64, _ip]
+        L.orc_dgetrf.restype = ctypes.c_int
+        L.orc_dgetrf2.argtypes = [ctypes.c_int, ctypes.c_int, _dp, _i64, _ip]
+        L.orc_dgetrf2.restype = ctypes.c_int
+        L.orc_dgetrs.argtypes = [ctypes.c_char, ctypes.c_int, ctypes.c_int, _dp, _i64, _ip, _dp, _i64]
+        L.orc_dgesv.argtypes = [ctypes.c_int, ctypes.c_int, _dp, _i64, _ip, _dp, _i64]
+        L.orc_dgesv.restype = ctypes.c_int
+        L.orc_hsolve.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, _i64, _dp, _dp, _dp]
+        L.orc_hsolve.restype = ctypes.c_int
+        L.orc_hsolve_general.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, _dp, _i64,
+                                         ctypes.POINTER(_dp), _i64, ctypes.POINTER(_dp), ctypes.c_int,
+                                         _dp, _i64, _ip, _dp, _ip]
+        L.orc_hsolve_general.restype = ctypes.c_int
+        L.orc_hsolve_general_mt.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, _dp, _i64,
+                                            ctypes.POINTER(_dp), _i64, ctypes.POINTER(_dp), ctypes.c_int,
+                                            _dp, _i64, ctypes.c_int]
+        L.orc_hsolve_general_mt.restype = ctypes.c_int
+        L.orc_hodlr_matvec.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, _dp, _i64,
+                                       ctypes.POINTER(_dp), _i64, ctypes.POINTER(_dp), _i64,
+                                       ctypes.POINTER(_dp), ctypes.c_int, _dp, _i64, _dp, _i64]
+        _lib = L
+    return _lib
+
+
+def ref_lib():
+    """The verbatim reference hsolve build, or None where it cannot be built."""
+    global _ref
+    if _ref is None:
+        path = _build.REF_SO
+        if not os.path.exists(path):
+            try:
+                path = _build.build_reference()
+            except Exception:
+                path = None
+        if not path or not os.path.exists(path):
+            return None
+        R = ctypes.CDLL(path)
+        R.ref_hsolve.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                 _dp, _dp, _dp]
+        _ref = R
+    return _ref
+
+
+def _p(a):
+    assert a.dtype == np.float64
+    return a.ctypes.data_as(_dp)
+
+
+def _ld(a):
+    """Leading dimension of a Fortran-ordered 2-D array (or a 1-D vector)."""
+    if a.ndim == 1:
+        return a.shape[0]
+    assert a.strides[0] == 8, "expected column-major"
+    return a.strides[1] // 8
+
+
+# ---------------------------------------------------------------- generators
+
+def seeds(master, n):
+    out = (ctypes.c_long * n)()
+    lib().orc_seeds(master, n, out)
+    return np.array(out[:], dtype=np.int64)
+
+
+def rand_matrix(seed_list, base, cols, offset=0):
+    """Matrix(base, level, cols).rand() with the given per-block seeds."""
+    nPart = len(seed_list)
+    A = np.zeros((nPart * base, cols), order="F")
+    s = (ctypes.c_long * nPart)(*[int(x) for x in seed_list])
+    lib().orc_rand_matrix(s, nPart, base, cols, _p(A), offset)
+    return A
+
+
+def dense_blocks(useeds, vseeds, dseeds, m, rank, offset):
+    nleaf = len(useeds)
+    K = np.zeros((nleaf * m, m), order="F")
+    mk = lambda v: (ctypes.c_long * nleaf)(*[int(x) for x in v])
+    lib().orc_dense_blocks(mk(useeds), mk(vseeds), mk(dseeds), nleaf, m, rank, offset, _p(K), _ld(K))
+    return K
+
+
+# ---------------------------------------------------------------- LAPACK
+
+def dgetrf(A):
+    """LU with partial pivoting (netlib DGETRF).  Returns (LU, ipiv 1-based, info)."""
+    A = np.array(A, dtype=np.float64, order="F", copy=True)
+    m, n = A.shape
+    ipiv = np.zeros(min(m, n), dtype=np.int32)
+    info = lib().orc_dgetrf(m, n, _p(A), _ld(A), ipiv.ctypes.data_as(_ip))
+    return A, ipiv, info
+
+
+def dgetrs(LU, ipiv, B, trans="N"):
+    B = np.array(B, dtype=np.float64, order="F", copy=True)
+    if B.ndim == 1:
+        B = B.reshape(-1, 1, order="F")
+    ipiv = np.ascontiguousarray(ipiv, dtype=np.int32)
+    LU = np.asfortranarray(LU)
+    lib().orc_dgetrs(trans.encode(), LU.shape[0], B.shape[1], _p(LU), _ld(LU),
+                     ipiv.ctypes.data_as(_ip), _p(B), _ld(B))
+    return B
+
+
+def dgemm(ta, tb, alpha, A, B, beta, C):
+    A = np.asfortranarray(A)
+    B = np.asfortranarray(B)
+    C = np.array(C, dtype=np.float64, order="F", copy=True)
+    m, n = C.shape
+    k = A.shape[0] if ta in "tT" else A.shape[1]
+    lib().orc_dgemm(ta.encode(), tb.encode(), m, n, k, alpha, _p(A), _ld(A), _p(B), _ld(B), beta, _p(C), _ld(C))
+    return C
+
+
+# ---------------------------------------------------------------- HODLR
+
+def hsolve(nrow, nrhs, rank, nPart, K, U, V):
+    """In-place restated hsolve (src/tasks/leaf_solve.cc:73-154)."""
+    LD = _ld(K)
+    assert _ld(U) == LD and _ld(V) == LD
+    return lib().orc_hsolve(nrow, nrhs, rank, nPart, LD, _p(K), _p(U), _p(V))
+
+
+def ref_hsolve(nrow, nrhs, rank, nPart, K, U, V):
+    """In-place verbatim reference hsolve (None if it is not built here)."""
+    R = ref_lib()
+    if R is None:
+        return None
+    LD = _ld(K)
+    assert _ld(U) == LD and _ld(V) == LD
+    R.ref_hsolve(nrow, nrhs, rank, nPart, LD, _p(K), _p(U), _p(V))
+    return 0
+
+
+def _ptr_array(arrs):
+    return (_dp * len(arrs))(*[_p(a) for a in arrs])
+
+
+def hsolve_general(prob, B, keep_factors=False, nthreads=1):
+    """Solve A X = B for a generalised HODLR problem (see problems.Problem).
+
+    Returns (X, factors-dict or None, info).  The factors dict holds the leaf
+    LU (N x m, stacked as the KTree region), leaf pivots, the transformed
+    bases Utilde[l] (N x r each) and the capacitance LU / pivots by node.
+    """
+    L, m, r, N = prob.levels, prob.leaf, prob.rank, prob.n
+    B = np.asarray(B, dtype=np.float64)
+    if B.ndim == 1:
+        B = B.reshape(-1, 1)
+    k = B.shape[1]
+    W = np.zeros((N, k + L * r), order="F")
+    W[:, :k] = B
+    for l in range(L):
+        W[:, k + l * r:k + (l + 1) * r] = prob.U[l]
+    K = np.array(prob.K, order="F", copy=True)
+    Vs = [np.asfortranarray(v) for v in prob.V]
+    Vp = _ptr_array(Vs)
+    ss = [np.ascontiguousarray(s, dtype=np.float64) for s in prob.s] if prob.s is not None else None
+    sp = _ptr_array(ss) if ss is not None else None
+    ldv = _ld(Vs[0]) if L else N
+    if nthreads > 1 and not keep_factors:
+        info = lib().orc_hsolve_general_mt(m, L, r, _p(K), _ld(K), Vp, ldv, sp, k, _p(W), _ld(W), nthreads)
+        return np.array(W[:, :k]), None, info
+    nnode = (1 << L) - 1
+    leaf_ipiv = np.zeros(N, dtype=np.int32)
+    cap_lu = np.zeros(max(nnode, 1) * 4 * r * r)
+    cap_ipiv = np.zeros(max(nnode, 1) * 2 * r, dtype=np.int32)
+    info = lib().orc_hsolve_general(m, L, r, _p(K), _ld(K), Vp, ldv, sp, k, _p(W), _ld(W),
+                                    leaf_ipiv.ctypes.data_as(_ip), _p(cap_lu), cap_ipiv.ctypes.data_as(_ip))
+    X = np.array(W[:, :k])
+    if not keep_factors:
+        return X, None, info
+    f = dict(leaf_lu=K, leaf_ipiv=leaf_ipiv.reshape(-1, m),
+             utilde=[np.array(W[:, k + l * r:k + (l + 1) * r], order="F") for l in range(L)],
+             cap_lu=cap_lu[:nnode * 4 * r * r].reshape(nnode, 2 * r, 2 * r).transpose(0, 2, 1),
+             cap_ipiv=cap_ipiv[:nnode * 2 * r].reshape(nnode, 2 * r))
+    return X, f, info
+
+
+def hodlr_matvec(prob, X):
+    """Y = A X in FP64 from the exact HODLR representation."""
+    L, m, r = prob.levels, prob.leaf, prob.rank
+    X = np.asfortranarray(np.asarray(X, dtype=np.float64).reshape(prob.n, -1))
+    Y = np.zeros_like(X, order="F")
+    Us = [np.asfortranarray(u) for u in prob.U]
+    Vs = [np.asfortranarray(v) for v in prob.V]
+    K = np.asfortranarray(prob.K)
+    ld = _ld(Us[0]) if L else prob.n
+    ss = [np.ascontiguousarray(s, dtype=np.float64) for s in prob.s] if prob.s is not None else None
+    sp = _ptr_array(ss) if ss is not None else None
+    lib().orc_hodlr_matvec(m, L, r, _p(K), _ld(K), _ptr_array(Us), ld, _ptr_array(Vs), ld, sp,
+                           X.shape[1], _p(X), _ld(X), _p(Y), _ld(Y))
+    return Y

@@ -1,0 +1,86 @@
+"""CPU tests of the C ABI library: it loads, exports exactly what
+include/hodlr_gb300.h declares, and rejects bad arguments on the host
+before touching a device."""
+import ctypes
+import os
+import re
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+HEADER = os.path.join(ROOT, "include", "hodlr_gb300.h")
+
+
+def declared_functions():
+    text = open(HEADER).read()
+    return sorted(set(re.findall(r"HODLR_API\s+[\w\s\*]*?\b(hodlr_\w+)\s*\(", text)))
+
+
+@pytest.fixture(scope="module")
+def fs():
+    import fastsolver2_gb300 as fs
+    fs.lib(build_if_missing=True)
+    return fs
+
+
+def test_header_declares_api():
+    names = declared_functions()
+    for must in ["hodlr_hsolve", "hodlr_create", "hodlr_set_leaf_blocks", "hodlr_set_lowrank", "hodlr_factor",
+                 "hodlr_solve", "hodlr_solve_transpose", "hodlr_adjoint", "hodlr_destroy",
+                 "hodlr_last_error_string"]:
+        assert must in names
+
+
+def test_library_exports_every_declared_symbol(fs):
+    L = fs.lib()
+    for name in declared_functions():
+        assert hasattr(L, name), name
+        assert name in fs.SIGNATURES, name
+
+
+def test_bindings_cover_header(fs):
+    assert set(fs.SIGNATURES) == set(declared_functions())
+
+
+def test_hsolve_rejects_bad_partition(fs):
+    L = fs.lib()
+    buf = (ctypes.c_double * 64)()
+    # nPart not a power of two
+    assert L.hodlr_hsolve(12, 1, 1, 3, 12, buf, buf, buf) == fs.HODLR_ERR_INVALID_ARG
+    # nrow not divisible by nPart
+    assert L.hodlr_hsolve(10, 1, 1, 4, 10, buf, buf, buf) == fs.HODLR_ERR_INVALID_ARG
+    # LD < nrow
+    assert L.hodlr_hsolve(16, 1, 1, 2, 8, buf, buf, buf) == fs.HODLR_ERR_INVALID_ARG
+    # rank out of range
+    assert L.hodlr_hsolve(16, 1, 65, 2, 16, buf, buf, buf) == fs.HODLR_ERR_INVALID_ARG
+    assert b"rank" in L.hodlr_last_error_string()
+
+
+def test_create_rejects_bad_desc(fs):
+    L = fs.lib()
+    h = ctypes.c_void_p()
+    bad = [
+        fs.Desc(100, 10, 3, 4, 1, 0, 0, 1e-12, 10, 0, None),   # n != leaf * 2^levels
+        fs.Desc(80, 10, 3, 0, 1, 0, 0, 1e-12, 10, 0, None),    # rank 0
+        fs.Desc(80, 10, 3, 4, 0, 0, 0, 1e-12, 10, 0, None),    # nrhs_max 0
+        fs.Desc(80, 10, 3, 4, 1, 7, 0, 1e-12, 10, 0, None),    # unknown precision
+        fs.Desc(80, 10, 3, 4, 1, 1, 0, 0.0, 10, 0, None),      # mixed without tolerance
+    ]
+    for d in bad:
+        assert L.hodlr_create(ctypes.byref(d), ctypes.byref(h)) == fs.HODLR_ERR_INVALID_ARG
+        assert not h.value
+
+
+def test_null_handle_calls_fail_cleanly(fs):
+    L = fs.lib()
+    assert L.hodlr_factor(None) == fs.HODLR_ERR_INVALID_ARG
+    assert L.hodlr_solve(None, None, 0, 1, None) == fs.HODLR_ERR_INVALID_ARG
+    assert L.hodlr_destroy(None) == fs.HODLR_OK
+
+
+def test_no_cpu_fallback_when_library_missing(monkeypatch, tmp_path):
+    import fastsolver2_gb300 as fs
+    monkeypatch.setattr(fs, "_lib", None)
+    monkeypatch.setattr(fs, "LIB_PATH", str(tmp_path / "missing.so"))
+    with pytest.raises(ImportError):
+        fs.lib()

@@ -1,0 +1,266 @@
+"""GPU parity tests: the CUDA path (through the C ABI) against the oracle.
+
+Tolerances: leaf / capacitance factors 1e-13 relative (the reference's own
+component tolerance, tests/test.cc:259-260); FP64 solutions 1e-12 relative and
+relative residual <= 1e-10 (the FP64 parity bar); the mixed path must reach
+its refinement target (1e-12).  Pivots must match bit for bit.
+"""
+import numpy as np
+import pytest
+import torch
+
+from oracle import oracle as O
+from oracle import problems as P
+
+pytestmark = pytest.mark.gpu
+
+
+def to_dev(a):
+    a = np.asarray(a, dtype=np.float64)
+    if a.ndim == 1:
+        return torch.from_numpy(a.copy()).cuda()
+    return torch.from_numpy(np.ascontiguousarray(a.T)).cuda().t()
+
+
+def to_host(t):
+    if t.dim() == 1:
+        return t.cpu().numpy()
+    return np.asfortranarray(t.t().cpu().numpy().T)
+
+
+def rel(a, b):
+    return np.linalg.norm(a - b) / np.linalg.norm(b)
+
+
+def make_solver(fs, pr, nrhs=None, precision=0, **kw):
+    s = fs.Solver(pr.n, pr.leaf, pr.levels, pr.rank, nrhs_max=nrhs or pr.nrhs, precision=precision, **kw)
+    keep = [to_dev(pr.K)]
+    s.set_leaf_blocks(keep[0])
+    for l in range(pr.levels):
+        U, V = to_dev(pr.U[l]), to_dev(pr.V[l])
+        sv = to_dev(pr.s[l]) if pr.s is not None else None
+        keep += [U, V, sv]
+        s.set_lowrank(l, U, V, sv)
+    torch.cuda.synchronize()
+    return s
+
+
+@pytest.mark.parametrize("m,L,r", [(64, 2, 8), (128, 3, 32), (256, 2, 16)])
+def test_leaf_lu_matches_oracle(hodlr, m, L, r):
+    pr = P.gaussian_problem(m, L, r, nrhs=1, seed=11)
+    s = make_solver(hodlr, pr)
+    s.factor()
+    nleaf = 1 << L
+    lu = torch.empty(nleaf * m * m, dtype=torch.float64, device="cuda")
+    piv = torch.empty(pr.n, dtype=torch.int32, device="cuda")
+    s.get_factors(leaf_lu=lu, leaf_ipiv=piv)
+    lu = lu.cpu().numpy().reshape(nleaf, m, m)
+    piv = piv.cpu().numpy().reshape(nleaf, m)
+    for i in range(nleaf):
+        LUo, pivo, info = O.dgetrf(pr.leaf_block(i))
+        assert info == 0
+        np.testing.assert_array_equal(piv[i], pivo)
+        assert rel(lu[i].T, LUo) < 1e-13
+
+
+@pytest.mark.parametrize("m,L,r,decay", [(32, 3, 4, None), (64, 4, 8, 6.0)])
+def test_factors_match_oracle(hodlr, m, L, r, decay):
+    pr = P.gaussian_problem(m, L, r, nrhs=1, seed=5, orthonormal=decay is not None, decay=decay,
+                            shift=1.5 if decay else 4.0)
+    s = make_solver(hodlr, pr)
+    s.factor()
+    X, f, info = O.hsolve_general(pr, pr.B, keep_factors=True)
+    assert info == 0
+    nnode = (1 << L) - 1
+    ut = torch.empty((L * r, pr.n), dtype=torch.float64, device="cuda").t()
+    cap = torch.empty(nnode * 4 * r * r, dtype=torch.float64, device="cuda")
+    cpiv = torch.empty(nnode * 2 * r, dtype=torch.int32, device="cuda")
+    s.get_factors(utilde=ut, cap_lu=cap, cap_ipiv=cpiv)
+    ut = to_host(ut)
+    for l in range(L):
+        assert rel(ut[:, l * r:(l + 1) * r], f["utilde"][l]) < 1e-12
+    cap = cap.cpu().numpy().reshape(nnode, 2 * r, 2 * r).transpose(0, 2, 1)
+    np.testing.assert_array_equal(cpiv.cpu().numpy().reshape(nnode, 2 * r), f["cap_ipiv"])
+    assert rel(cap, f["cap_lu"]) < 1e-12
+
+
+@pytest.mark.parametrize("m,L,r,k", [(256, 4, 16, 1), (128, 5, 32, 8), (64, 6, 8, 3), (16, 0, 1, 2)])
+def test_fp64_solve_matches_oracle(hodlr, m, L, r, k):
+    pr = P.gaussian_problem(m, L, r, nrhs=k, seed=3)
+    s = make_solver(hodlr, pr)
+    s.factor()
+    Xo, _, info = O.hsolve_general(pr, pr.B)
+    B = to_dev(pr.B)
+    info_gpu = s.solve(B)
+    X = to_host(B)
+    assert rel(X, Xo) < 1e-12
+    assert P.rel_residual(pr, X) < 1e-10
+    # a second solve replays the captured graph and must give the same bits
+    B2 = to_dev(pr.B)
+    s.solve(B2)
+    assert torch.equal(B2, B) or np.array_equal(to_host(B2), X)
+
+
+@pytest.mark.parametrize("name", ["ref_m16_L2_r3_k1", "ref_m64_L3_r8_k1", "ref_m32_L3_r4_k5",
+                                  "ref_m256_L4_r16_k1", "ref_m400_L2_r10_k1"])
+@pytest.mark.parametrize("where", ["device", "host"])
+def test_hsolve_dropin_matches_golden(hodlr, name, where):
+    import os
+    g = np.load(os.path.join(os.path.dirname(__file__), "golden", name + ".npz"))
+    m, L, r, k = int(g["leaf"]), int(g["levels"]), int(g["rank"]), int(g["nrhs"])
+    pr = P.reference_problem(m, L, r, nrhs=k, master=int(g["master"]), offset=int(g["offset"]))
+    N = pr.n
+    W = np.zeros((N, k + L * r), order="F")
+    W[:, :k] = pr.B
+    for l in range(L):
+        W[:, k + l * r:k + (l + 1) * r] = pr.U[0]
+    K = np.array(pr.K, order="F")
+    V = np.array(pr.V[0], order="F")
+    if where == "device":
+        Kd, Wd, Vd = to_dev(K), to_dev(W), to_dev(V)
+        hodlr.hsolve(N, k, r, 1 << L, N, Kd, Wd, Vd)
+        K, W = to_host(Kd), to_host(Wd)
+    else:
+        hodlr.hsolve(N, k, r, 1 << L, N, K, W, V)
+    assert rel(W[:, :k], g["x"]) < 1e-12
+    if "region" in g:
+        assert rel(W, g["region"]) < 1e-12
+        assert rel(K, g["K"]) < 1e-12
+    else:
+        np.testing.assert_allclose(np.linalg.norm(W, axis=0), g["region_colnorms"], rtol=1e-12)
+        assert rel(W[:64], g["region_head"]) < 1e-12
+        assert rel(K[:64], g["K_head"]) < 1e-12
+
+
+def test_hsolve_matches_restated_oracle_bigger(hodlr):
+    pr = P.reference_problem(128, 6, 12, nrhs=2)
+    N, L, r, k = pr.n, pr.levels, pr.rank, pr.nrhs
+    W = np.zeros((N, k + L * r), order="F")
+    W[:, :k] = pr.B
+    for l in range(L):
+        W[:, k + l * r:k + (l + 1) * r] = pr.U[0]
+    K, V = np.array(pr.K, order="F"), np.array(pr.V[0], order="F")
+    Wo, Ko = W.copy(order="F"), K.copy(order="F")
+    assert O.hsolve(N, k, r, 1 << L, Ko, Wo, V) == 0
+    hodlr.hsolve(N, k, r, 1 << L, N, K, W, V)
+    assert rel(W, Wo) < 1e-12
+
+
+@pytest.mark.parametrize("resid", [0, 1])
+def test_mixed_refinement_reaches_tolerance(hodlr, resid):
+    pr = P.gaussian_problem(128, 6, 32, nrhs=4, seed=9, orthonormal=True, decay=6.0, shift=1.5)
+    s = make_solver(hodlr, pr, precision=hodlr.PREC_MIXED, residual=resid, refine_tol=1e-12)
+    s.factor()
+    B = to_dev(pr.B)
+    info = s.solve(B)
+    X = to_host(B)
+    assert info.rel_residual <= 1e-12
+    assert info.iterations >= 1
+    res = P.rel_residual(pr, X)
+    assert res < 2e-12
+    Xo, _, _ = O.hsolve_general(pr, pr.B)
+    assert rel(X, Xo) < 1e-9
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_transpose_solve(hodlr, precision):
+    pr = P.gaussian_problem(64, 4, 8, nrhs=3, seed=21, orthonormal=True, decay=3.0, shift=2.0)
+    s = make_solver(hodlr, pr, precision=precision)
+    s.factor()
+    B = to_dev(pr.B)
+    s.solve(B, transpose=True)
+    Xd = np.linalg.solve(pr.dense().T, pr.B)
+    assert rel(to_host(B), Xd) < 1e-11
+
+
+@pytest.mark.parametrize("trans", [False, True])
+def test_matvec_fp64(hodlr, trans):
+    pr = P.gaussian_problem(64, 5, 8, nrhs=3, seed=4, orthonormal=True, decay=2.0)
+    s = make_solver(hodlr, pr)
+    X = to_dev(pr.B)
+    Y = torch.zeros_like(X)
+    Y = Y.t().contiguous().t()
+    s.matvec(X, Y, transpose=trans)
+    A = pr.dense()
+    Yd = (A.T if trans else A) @ pr.B
+    assert rel(to_host(Y), Yd) < 1e-13
+
+
+def test_adjoint_matches_dense_gradient(hodlr):
+    m, L, r, k = 64, 5, 6, 1
+    pr = P.gaussian_problem(m, L, r, nrhs=k, seed=13, orthonormal=True, decay=2.0, shift=2.0)
+    N = pr.n
+    A = pr.dense()
+    x = np.linalg.solve(A, pr.B)
+    lam = np.linalg.solve(A.T, x)
+    dA = -lam @ x.T
+    s = make_solver(hodlr, pr)
+    s.factor()
+    xd, gd = to_dev(x), to_dev(x)
+    db = torch.zeros((k, N), dtype=torch.float64, device="cuda").t()
+    dD = torch.zeros((1 << L) * m * m, dtype=torch.float64, device="cuda")
+    dU = torch.zeros(L * N * r, dtype=torch.float64, device="cuda")
+    dV = torch.zeros(L * N * r, dtype=torch.float64, device="cuda")
+    ds = torch.zeros(L * r, dtype=torch.float64, device="cuda")
+    s.adjoint(xd, gd, db=db, dD=dD, dU=dU, dV=dV, ds=ds)
+    assert rel(to_host(db), lam) < 1e-11
+    dD = dD.cpu().numpy().reshape(1 << L, m, m).transpose(0, 2, 1)
+    for i in range(1 << L):
+        blk = dA[i * m:(i + 1) * m, i * m:(i + 1) * m]
+        assert rel(dD[i], blk) < 1e-11
+    dU = dU.cpu().numpy().reshape(L, r, N).transpose(0, 2, 1)
+    dV = dV.cpu().numpy().reshape(L, r, N).transpose(0, 2, 1)
+    ds = ds.cpu().numpy().reshape(L, r)
+    for l in range(L):
+        h = N >> (l + 1)
+        sv = pr.s[l]
+        gU = np.zeros((N, r))
+        gV = np.zeros((N, r))
+        gs = np.zeros(r)
+        for p in range(1 << l):
+            c0 = slice(2 * p * h, (2 * p + 1) * h)
+            c1 = slice((2 * p + 1) * h, (2 * p + 2) * h)
+            for a, b in ((c0, c1), (c1, c0)):
+                blk = dA[a, b]
+                gU[a] += (blk @ pr.V[l][b]) * sv
+                gV[b] += (blk.T @ pr.U[l][a]) * sv
+                gs += np.einsum("iq,ij,jq->q", pr.U[l][a], blk, pr.V[l][b])
+        assert rel(dU[l], gU) < 1e-10
+        assert rel(dV[l], gV) < 1e-10
+        assert rel(ds[l], gs) < 1e-10
+
+
+def test_generated_problem_solves(hodlr):
+    m, L, r, k = 128, 7, 32, 4
+    N = m << L
+    s = hodlr.Solver(N, m, L, r, nrhs_max=k)
+    B = torch.empty((k, N), dtype=torch.float64, device="cuda").t()
+    s.generate(seed=7, shift=4.0, B=B)
+    B0 = B.clone()
+    s.factor()
+    s.solve(B)
+    R = torch.empty_like(B0).t().contiguous().t()
+    s.matvec(B, R)
+    res = torch.linalg.norm(R - B0) / torch.linalg.norm(B0)
+    assert res.item() < 1e-12
+
+
+def test_singular_leaf_reports_status(hodlr):
+    pr = P.gaussian_problem(32, 2, 4, nrhs=1, seed=2)
+    pr.K[2 * 32:3 * 32, :] = 0.0  # leaf 2 all zeros
+    s = make_solver(hodlr, pr)
+    with pytest.raises(hodlr.HodlrError) as e:
+        s.factor()
+    assert e.value.code == hodlr.HODLR_ERR_SINGULAR_LEAF
+
+
+def test_nonfinite_rhs_reports_status(hodlr):
+    pr = P.gaussian_problem(32, 2, 4, nrhs=1, seed=2)
+    s = make_solver(hodlr, pr)
+    s.factor()
+    B = pr.B.copy(order="F")
+    B[17, 0] = np.nan
+    Bd = to_dev(B)
+    with pytest.raises(hodlr.HodlrError) as e:
+        s.solve(Bd)
+    assert e.value.code == hodlr.HODLR_ERR_NONFINITE_INPUT
