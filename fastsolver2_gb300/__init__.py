@@ -108,7 +108,8 @@ def _ptr(t):
 
 def _ld(t):
     """Leading dimension of a column-major (Fortran-ordered) 2-D tensor."""
-    if t.dim() == 1:
+    if t.dim() == 1 or t.shape[1] == 1:
+        assert t.dim() == 1 or t.stride(0) == 1 or t.shape[0] == 1, "expected a column-major tensor"
         return t.shape[0]
     assert t.stride(0) == 1, "expected a column-major tensor (use .t().contiguous().t())"
     return t.stride(1)
