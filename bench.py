@@ -1,0 +1,389 @@
+#!/usr/bin/env python
+"""Benchmark: HODLR factor + solve at N = 2^20 (leaf 128, 13 levels, rank 32,
+64 right-hand sides) on one GB300.
+
+Our arm (default): the mixed-precision path (FP32 leaf LU / low-rank GEMMs,
+FP64 capacitance LU, FP64-accurate residual + iterative refinement to a
+relative residual of 1e-12) on the ill-conditioned Gaussian workload
+(orthonormalised factors, s_i = 10^(-6 i / r), leaf shift 1.5), timed per
+step = factor + solve with inputs resident in HBM.  The plain FP64 GPU path is
+timed on the same inputs beside it.  One JSON line on stdout.
+
+--impl reference: the reference's own CPU algorithm (the oracle's C
+restatement of fastSolver2's hsolve with netlib LU, threaded the way its
+Legion index launch splits subtrees) on the host cores, on a bounded subtree
+sample scaled to the full N by the algorithmic flop count.
+
+Multi-GPU (torchrun): the solve does not shard in this build, so each rank
+solves its own independent system (replicas); the line reports the max over
+ranks.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "HODLR factor+solve ms at N=2^20 (mixed vs FP64 on GPU, rel. resid ≤1e-12)"
+WORKLOAD = dict(n=1 << 20, leaf=128, levels=13, rank=32, nrhs=64)
+SMALL = dict(n=1 << 14, leaf=128, levels=7, rank=32, nrhs=64)
+SEED = 20261203
+
+
+def algo_flops(n, m, L, r, k):
+    """Algorithmic FP64 flop counts of factor and solve (the hsolve one-shot count)."""
+    F = (2 / 3) * n * m * m + 2 * n * m * L * r + sum(
+        2 * n * r * r + 4 * n * r * r * l + (2 ** l) * ((16 / 3) * r ** 3 + 8 * r ** 3 * l) for l in range(L))
+    S = 2 * n * m * k + sum(4 * n * r * k + 8 * (2 ** l) * r * r * k for l in range(L))
+    return F, S
+
+
+def algo_bytes(n, m, L, r, k, w=8):
+    """Compulsory traffic of factor and solve at element width w."""
+    caps = (2 ** L) * (2 * r) ** 2 * w
+    return (2 * n * m + 3 * n * r * L) * w + caps, (n * m + 2 * n * r * L + 2 * n * k) * w + caps
+
+
+def resid_flops(n, m, L, r, k):
+    return 2 * n * m * k + 4 * n * r * k * L
+
+
+# ---------------------------------------------------------------- clocks
+class ClockSampler:
+    """nvidia-smi clock / throttle sampling during the timed region."""
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu):
+        self.gpu = gpu
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.QUERY,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except (OSError, ValueError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax = float(f[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ---------------------------------------------------------------- CPU leg
+def cpu_sample_run(wl, levels_sample, threads):
+    """One run of the oracle port on a subtree sample; returns (seconds, flops, info)."""
+    from oracle import oracle as O
+    from oracle import problems as P
+    pr = P.gaussian_problem(wl["leaf"], levels_sample, wl["rank"], nrhs=wl["nrhs"], seed=SEED,
+                            orthonormal=False, shift=4.0)
+    t0 = time.perf_counter()
+    _, _, info = O.hsolve_general(pr, pr.B, nthreads=threads)
+    dt = time.perf_counter() - t0
+    F, S = algo_flops(pr.n, wl["leaf"], levels_sample, wl["rank"], wl["nrhs"])
+    return dt, F + S, info
+
+
+def cpu_baseline(wl, small, repeats=1):
+    threads = os.cpu_count() or 1
+    Ls = 4 if small else 10
+    F, S = algo_flops(wl["n"], wl["leaf"], wl["levels"], wl["rank"], wl["nrhs"])
+    vals = []
+    for _ in range(repeats):
+        dt, fl, info = cpu_sample_run(wl, Ls, threads)
+        assert info == 0
+        vals.append(dt * (F + S) / fl * 1e3)
+    sample = ("oracle C port of hsolve (netlib LU) on a %d-row subtree (leaf %d, %d levels, rank %d, %d rhs), "
+              "%d threads; scaled to N=%d by the algorithmic flop ratio"
+              % (wl["leaf"] << Ls, wl["leaf"], Ls, wl["rank"], wl["nrhs"], threads, wl["n"]))
+    return float(np.median(vals)), threads, sample
+
+
+def run_reference(args, wl):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    for _ in range(args.warmup):
+        cpu_baseline(wl, args.small)
+    vals = []
+    t_wall = time.perf_counter()
+    for _ in range(args.steps):
+        v, threads, sample = cpu_baseline(wl, args.small)
+        vals.append(v)
+    wall = time.perf_counter() - t_wall
+    value = float(np.mean(vals))
+    line = {"metric": METRIC, "value": value, "unit": "ms", "impl": "reference", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": value, "higher_is_better": False,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded Gaussian)",
+            "config": {"workload": "HODLR N=2^20 leaf 128 L=13 rank 32 nrhs 64 (factor+solve, one-shot hsolve)",
+                       **wl},
+            "cpu_baseline": {"value": value, "unit": "ms", "cores": threads, "kind": "port", "sample": sample},
+            "e2e": {"value": value, "unit": "ms", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "wall_s": wall}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# ---------------------------------------------------------------- GPU arm
+def run_ours(args, wl):
+    import torch
+    import fastsolver2_gb300 as fs
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    fs.lib()
+
+    # CPU baseline first (rank 0, N = 1), before the GPU work starts
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        cpu = cpu_baseline(wl, args.small)
+
+    n, m, L, r, k = wl["n"], wl["leaf"], wl["levels"], wl["rank"], wl["nrhs"]
+    stream = torch.cuda.Stream()
+    sp = stream.cuda_stream
+    dev = "cuda"
+
+    def colmajor(rows, cols):
+        return torch.empty((cols, rows), dtype=torch.float64, device=dev).t()
+
+    launches0 = fs.kernel_launches()
+    with torch.cuda.stream(stream):
+        mixed = fs.Solver(n, m, L, r, nrhs_max=k, precision=fs.PREC_MIXED, residual=args.resid,
+                          refine_tol=1e-12, refine_max_iter=10, stream=sp)
+        B0 = colmajor(n, k)
+        mixed.generate(SEED + rank, shift=1.5, orthonormal=True, decay=6.0, B=B0)
+        B = colmajor(n, k)
+
+        def step():
+            B.copy_(B0)
+            mixed.factor()
+            return mixed.solve(B)
+
+        for _ in range(args.warmup):
+            step()
+        mixed.profile(1)
+        mixed.profile(-1, read=True)
+        for _ in range(2):   # capture the graphs with timing events outside the timed region
+            step()
+        mixed.profile(-1, read=True)
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+        clocks = ClockSampler(local)
+        clocks.start()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        l0 = fs.kernel_launches()
+        t_wall = time.perf_counter()
+        e0.record(stream)
+        iters = []
+        for _ in range(args.steps):
+            info = step()
+            iters.append(info.iterations)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t_wall
+        launches = fs.kernel_launches() - l0
+        clk = clocks.stop()
+        ms = e0.elapsed_time(e1) / args.steps
+        phases = mixed.profile(0, read=True)
+        final_resid_dev = info.rel_residual
+
+        # independent FP64 check of the mixed result: max_j ||b_j - A x_j|| / ||b_j||
+        fp64 = fs.Solver(n, m, L, r, nrhs_max=k, precision=fs.PREC_FP64, stream=sp)
+        fp64.generate(SEED + rank, shift=1.5, orthonormal=True, decay=6.0, B=None)
+        AX = colmajor(n, k)
+        fp64.matvec(B, AX)
+        torch.cuda.synchronize()
+        check = ((B0 - AX).norm(dim=0) / B0.norm(dim=0)).max().item()
+
+        # the plain FP64 GPU path on the same inputs
+        Bd = colmajor(n, k)
+        fp64_ms = []
+        for i in range(args.fp64_steps + 1):
+            Bd.copy_(B0)
+            f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            f0.record(stream)
+            fp64.factor()
+            fp64.solve(Bd)
+            f1.record(stream)
+            torch.cuda.synchronize()
+            if i > 0:
+                fp64_ms.append(f0.elapsed_time(f1))
+        fp64_factor_ms, fp64_solve_ms = fp64.timings()
+        fp64_AX = colmajor(n, k)
+        fp64.matvec(Bd, fp64_AX)
+        torch.cuda.synchronize()
+        fp64_resid = ((B0 - fp64_AX).norm(dim=0) / B0.norm(dim=0)).max().item()
+        del fp64, AX, fp64_AX, Bd
+
+        # end to end through the C ABI with host buffers: H2D of the problem and
+        # the right-hand sides, factor, solve, D2H of the solution
+        e2e = None
+        if not args.no_e2e:
+            nleaf = 1 << L
+            pin = dict(dtype=torch.float64, pin_memory=True)
+            hD = torch.empty(nleaf * m * m, **pin)
+            hU = torch.empty(L * n * r, **pin)
+            hV = torch.empty(L * n * r, **pin)
+            hs = torch.empty(max(L, 1) * r, **pin)
+            hB = torch.empty((k, n), **pin).t()
+            hX = torch.empty((k, n), **pin).t()
+            mixed.get_inputs(D=hD, U=hU, V=hV, s=hs)
+            hB.copy_(B0)
+            torch.cuda.synchronize()
+            lib = fs.lib()
+            Be = colmajor(n, k)
+
+            def e2e_step():
+                fs.check(lib.hodlr_set_leaf_blocks(mixed.h, hD.data_ptr(), m, m * m))
+                for l in range(L):
+                    off = l * n * r * 8
+                    fs.check(lib.hodlr_set_lowrank(mixed.h, l, hU.data_ptr() + off, n, hV.data_ptr() + off, n,
+                                                   hs.data_ptr() + l * r * 8))
+                Be.copy_(hB, non_blocking=True)
+                mixed.factor()
+                mixed.solve(Be)
+                hX.copy_(Be, non_blocking=True)
+                stream.synchronize()
+
+            e2e_step()
+            torch.cuda.synchronize()
+            g0, g1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            g0.record(stream)
+            for _ in range(args.e2e_steps):
+                e2e_step()
+            g1.record(stream)
+            torch.cuda.synchronize()
+            h2d = (hD.numel() + hU.numel() + hV.numel() + L * r + n * k) * 8
+            e2e = {"value": g0.elapsed_time(g1) / args.e2e_steps, "unit": "ms", "h2d_bytes_per_step": h2d,
+                   "d2h_bytes_per_step": n * k * 8}
+
+    # ---- report (max over ranks)
+    if world > 1:
+        t = torch.tensor([ms], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = t.item()
+    F, S = algo_flops(n, m, L, r, k)
+    nres = float(np.mean(iters)) + 1.0
+    total_ms = sum(v[0] for v in phases.values())
+    # dominant phase of the mixed step and its roofline
+    dom = max(phases.items(), key=lambda kv: kv[1][0])
+    phase_flops = {
+        "leaf_lu": (2 / 3) * n * m * m,
+        "leaf_solve": 2 * n * m * L * r + (nres) * 2 * n * m * k,
+        "resid_leaf": nres * 2 * n * m * k,
+        "resid_reduce": nres * 2 * n * r * k * L,
+        "resid_update": nres * 2 * n * r * k * L,
+    }
+    measured = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if os.path.exists(
+        os.path.join(ROOT, "MEASURED_PEAKS.json")) else {}
+    hbm_peak = measured.get("hbm_gbs", 6800.0)
+    dom_name, (dom_ms, dom_n) = dom
+    dom_steps = args.steps  # phases were summed over the timed steps
+    roof = None
+    if dom_name in phase_flops and dom_ms > 0:
+        fl = phase_flops[dom_name] * dom_steps
+        achieved = fl / (dom_ms * 1e-3) / 1e12
+        peak = FP32_PEAK_TFLOPS if dom_name.startswith("resid") and args.resid == 1 else FP64_PEAK_TFLOPS
+        roof = {"kernel": dom_name, "bound": "fp32_simt" if peak == FP32_PEAK_TFLOPS else "fp64_dfma",
+                "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
+                "traffic": None, "avg_launch_ms": dom_ms / max(dom_n, 1),
+                "note": "FP64-equivalent flops; peak = measured FFMA/DFMA issue rate (profiles/fp_peaks.md)"}
+    line = {
+        "metric": METRIC, "value": ms, "unit": "ms", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": ms, "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
+        "data": "synthetic (device counter-based Gaussian generator, seeded)",
+        "config": {"workload": "HODLR N=2^20 leaf 128 L=13 rank 32 nrhs 64, mixed precision + FP64 refinement; "
+                               "orthonormal factors s_i=10^(-6i/32), leaf shift 1.5",
+                   **wl, "parallelism": "replicas" if world > 1 else "single GPU",
+                   "l2": "inputs larger than L2 (>14 GB resident per step)",
+                   "residual": "fp64-emulated (double-FP32)" if args.resid == 1 else "native fp64"},
+        "refine_iterations": float(np.mean(iters)), "rel_resid_device": final_resid_dev,
+        "rel_resid_fp64_check": check,
+        "fp64_ms": float(np.mean(fp64_ms)), "fp64_factor_ms": fp64_factor_ms, "fp64_solve_ms": fp64_solve_ms,
+        "fp64_rel_resid": fp64_resid,
+        "speedup_vs_fp64": float(np.mean(fp64_ms)) / ms,
+        "algorithmic_gflop_per_step": (F + S) / 1e9,
+        "phases_ms_per_step": {kk: v[0] / args.steps for kk, v in phases.items()},
+        "phase_timing_overhead_note": "per-phase CUDA events were recorded inside the timed graphs",
+        "roofline": roof,
+        "clocks": clk, "gpu_launches": launches, "wall_s": wall,
+        "e2e": e2e,
+    }
+    if cpu is not None:
+        line["cpu_baseline"] = {"value": cpu[0], "unit": "ms", "cores": cpu[1], "kind": "port", "sample": cpu[2]}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+# Measured on this machine's GB300 (FFMA / DFMA issue-rate probe, profiles/fp_peaks.md).
+FP32_PEAK_TFLOPS = 70.0
+FP64_PEAK_TFLOPS = 1.198
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--resid", type=int, default=0, help="0 native FP64 residual, 1 FP64-emulated")
+    ap.add_argument("--fp64-steps", type=int, default=3)
+    ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--small", action="store_true", help="N=2^14 smoke-sized workload")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    args = ap.parse_args()
+    wl = SMALL if args.small else WORKLOAD
+    if args.impl == "reference":
+        return run_reference(args, wl)
+    return run_ours(args, wl)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

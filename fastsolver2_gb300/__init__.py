@@ -29,6 +29,9 @@ RESID_FP64_EMULATED = 1
 
 LIB_PATH = _build.LIB
 
+PHASES = ["leaf_lu", "leaf_solve", "reduce", "capacitance", "update", "resid_leaf", "resid_reduce",
+          "resid_update", "misc"]
+
 
 class HodlrError(RuntimeError):
     def __init__(self, code, msg):
@@ -69,7 +72,9 @@ SIGNATURES = {
     "hodlr_matvec": (_I, [_VP, _I, _VP, _I64, _VP, _I64, _I]),
     "hodlr_adjoint": (_I, [_VP, _VP, _I64, _VP, _I64, _I, ctypes.POINTER(Grads)]),
     "hodlr_get_factors": (_I, [_VP, _VP, _VP, _VP, _VP, _VP]),
+    "hodlr_get_inputs": (_I, [_VP, _VP, _I64, _I64, _VP, _VP, _VP]),
     "hodlr_generate": (_I, [_VP, ctypes.c_uint64, _D, _I, _D, _VP, _I64, _I]),
+    "hodlr_profile": (_I, [_VP, _I, _VP, _VP, _I]),
     "hodlr_last_timings": (_I, [_VP, ctypes.POINTER(_D), ctypes.POINTER(_D)]),
     "hodlr_kernel_launches": (_I64, []),
     "hodlr_last_error_string": (ctypes.c_char_p, []),
@@ -173,6 +178,22 @@ class Solver:
     def generate(self, seed, shift=4.0, orthonormal=False, decay=0.0, B=None):
         check(lib().hodlr_generate(self.h, seed, shift, int(orthonormal), decay, _ptr(B),
                                    _ld(B) if B is not None else 0, B.shape[1] if B is not None else 0))
+
+    def get_inputs(self, D=None, ld=None, leaf_stride=None, U=None, V=None, s=None):
+        """Copy the problem out (torch tensors, host or device)."""
+        ld = self.leaf if ld is None else ld
+        stride = self.leaf * self.leaf if leaf_stride is None else leaf_stride
+        check(lib().hodlr_get_inputs(self.h, _ptr(D), ld, stride, _ptr(U), _ptr(V), _ptr(s)))
+
+    def profile(self, enable=-1, read=False):
+        """Switch per-phase timing on/off; with read=True return {phase: (ms, launches)} and reset."""
+        if not read:
+            check(lib().hodlr_profile(self.h, enable, None, None, 0))
+            return None
+        ms = (ctypes.c_double * len(PHASES))()
+        n = (ctypes.c_int64 * len(PHASES))()
+        check(lib().hodlr_profile(self.h, enable, ms, n, len(PHASES)))
+        return {name: (ms[i], n[i]) for i, name in enumerate(PHASES)}
 
     def timings(self):
         f, s = ctypes.c_double(), ctypes.c_double()

@@ -26,11 +26,17 @@ template <typename T> __device__ __forceinline__ T dabs(T x) { return x < T(0) ?
 // Host-side launch accounting (every kernel launch of the library goes
 // through HODLR_LAUNCH so hodlr_kernel_launches() can report it).
 void count_launch();
+// HODLR_DEBUG_SYNC=1 in the environment: synchronise after every launch
+// (outside graph capture) and print the first failing kernel's name.
+bool debug_sync();
+void debug_after_launch(const char *name, cudaStream_t s);
 
 #define HODLR_LAUNCH(kernel, grid, block, smem, stream, ...)                 \
   do {                                                                       \
     ::hodlr::count_launch();                                                 \
+    (void)cudaGetLastError(); /* report this launch's own error only */      \
     kernel<<<(grid), (block), (smem), (stream)>>>(__VA_ARGS__);              \
+    if (::hodlr::debug_sync()) ::hodlr::debug_after_launch(#kernel, stream); \
   } while (0)
 
 inline int ceil_div(long long a, long long b) { return (int)((a + b - 1) / b); }

@@ -24,10 +24,25 @@
 #include <vector>
 
 #include "kernels.cuh"
+#include "resid_emul.cuh"
 
 namespace hodlr {
 static std::atomic<long long> g_launches{0};
 void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+bool debug_sync() {
+  static const bool on = [] {
+    const char *v = getenv("HODLR_DEBUG_SYNC");
+    return v && *v && *v != '0';
+  }();
+  return on;
+}
+void debug_after_launch(const char *name, cudaStream_t s) {
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  cudaStreamIsCapturing(s, &cs);
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess && cs == cudaStreamCaptureStatusNone) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) fprintf(stderr, "hodlr: kernel %s: %s\n", name, cudaGetErrorString(e));
+}
 }  // namespace hodlr
 
 using namespace hodlr;
@@ -53,10 +68,26 @@ static int set_err(int code, const std::string &msg) {
     if (s_ != HODLR_OK) return s_; \
   } while (0)
 
+// Optional per-phase device timing: CUDA events around every launch of a
+// phase (event record nodes inside captured graphs), summed after each call.
+struct PhaseRec {
+  int phase;
+  cudaEvent_t a, b;
+};
+
 struct GraphEntry {
   cudaGraphExec_t exec = nullptr;
   long long kernels = 0;
+  std::vector<PhaseRec> recs;
 };
+
+static void destroy_recs(std::vector<PhaseRec> &v) {
+  for (auto &p : v) {
+    cudaEventDestroy(p.a);
+    cudaEventDestroy(p.b);
+  }
+  v.clear();
+}
 
 struct hodlr_ctx {
   hodlr_desc d{};
@@ -80,6 +111,9 @@ struct hodlr_ctx {
   double *Tbuf = nullptr, *Wbuf = nullptr, *eta = nullptr, *red = nullptr;
   double *X64 = nullptr, *R64 = nullptr, *B64 = nullptr, *norms = nullptr, *nwork = nullptr;
   float *X32 = nullptr;
+  // double-word (hi, lo) copies for the emulated FP64 residual (mixed mode)
+  float2 *D2 = nullptr, *U2 = nullptr, *V2 = nullptr, *X2 = nullptr, *R2 = nullptr, *T2 = nullptr;
+  bool emulated = false;
   size_t tbuf_elems = 0, eta_elems = 0, red_elems = 0;
   DevStatus *dst = nullptr, *hst = nullptr;
   // timing
@@ -92,6 +126,14 @@ struct hodlr_ctx {
   std::map<std::tuple<const double *, long long, int, int>, GraphEntry> solve_graphs;
   std::map<std::tuple<const double *, long long, int, int>, int> solve_runs;
   std::vector<void *> allocs;
+  // phase profiling
+  bool profile = false;
+  std::vector<PhaseRec> *recs = nullptr;     // where launches record, or null
+  std::vector<PhaseRec> *last_recs = nullptr;
+  bool last_eager = false;
+  std::vector<PhaseRec> eager_recs;
+  double phase_ms[HODLR_NUM_PHASES] = {};
+  long long phase_n[HODLR_NUM_PHASES] = {};
 
   template <typename T> T *alloc(size_t count, cudaError_t &err) {
     void *p = nullptr;
@@ -105,11 +147,78 @@ struct hodlr_ctx {
   double *slev(int l) const { return s + (long long)l * r; }
 };
 
+static void clear_graphs(hodlr_ctx *h) {
+  for (auto &g : h->solve_graphs) {
+    if (g.second.exec) cudaGraphExecDestroy(g.second.exec);
+    destroy_recs(g.second.recs);
+  }
+  h->solve_graphs.clear();
+  h->solve_runs.clear();
+  if (h->factor_graph.exec) cudaGraphExecDestroy(h->factor_graph.exec);
+  destroy_recs(h->factor_graph.recs);
+  h->factor_graph = GraphEntry();
+  h->factor_runs = 0;
+  h->last_recs = nullptr;
+}
+
+// Inside stream capture a plain cudaEventRecord only orders streams; the
+// External flag makes it an event-record node that records on every replay.
+static void record_timing_event(cudaEvent_t e, cudaStream_t s) {
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  cudaStreamIsCapturing(s, &cs);
+  if (cs == cudaStreamCaptureStatusActive)
+    cudaEventRecordWithFlags(e, s, cudaEventRecordExternal);
+  else
+    cudaEventRecord(e, s);
+}
+
+struct PhaseScope {
+  hodlr_ctx *h;
+  int ph;
+  cudaEvent_t a = nullptr;
+  PhaseScope(hodlr_ctx *h_, int ph_) : h(h_), ph(ph_) {
+    if (h->profile && h->recs && cudaEventCreate(&a) == cudaSuccess) record_timing_event(a, h->st);
+  }
+  ~PhaseScope() {
+    if (!a) return;
+    cudaEvent_t b;
+    if (cudaEventCreate(&b) != cudaSuccess) {
+      cudaEventDestroy(a);
+      return;
+    }
+    record_timing_event(b, h->st);
+    h->recs->push_back({ph, a, b});
+  }
+};
+
+#define PHASE(h, ph, expr)     \
+  do {                         \
+    PhaseScope ps_((h), (ph)); \
+    CK(expr);                  \
+  } while (0)
+
+// After the stream was synchronised: add the recorded phase times.
+static void collect_phases(hodlr_ctx *h) {
+  if (!h->last_recs) return;
+  for (auto &p : *h->last_recs) {
+    float ms = 0.f;
+    cudaError_t e = cudaEventElapsedTime(&ms, p.a, p.b);
+    if (e == cudaSuccess) {
+      h->phase_ms[p.phase] += ms;
+      h->phase_n[p.phase] += 1;
+    } else {
+      if (debug_sync()) fprintf(stderr, "hodlr: phase %d timing: %s\n", p.phase, cudaGetErrorString(e));
+      (void)cudaGetLastError();
+    }
+  }
+  if (h->last_eager) destroy_recs(*h->last_recs);
+  h->last_recs = nullptr;
+}
+
 static void free_ctx(hodlr_ctx *h) {
   if (!h) return;
-  for (auto &g : h->solve_graphs)
-    if (g.second.exec) cudaGraphExecDestroy(g.second.exec);
-  if (h->factor_graph.exec) cudaGraphExecDestroy(h->factor_graph.exec);
+  clear_graphs(h);
+  destroy_recs(h->eager_recs);
   for (void *p : h->allocs) cudaFree(p);
   if (h->hst) cudaFreeHost(h->hst);
   for (auto &e : h->ev)
@@ -177,12 +286,21 @@ template <typename F>
 static int run_graphed(hodlr_ctx *h, GraphEntry &g, int &runs, F fn) {
   if (!h->use_graphs || runs == 0 || h->st == nullptr) {
     ++runs;
-    return fn();
+    destroy_recs(h->eager_recs);
+    h->recs = &h->eager_recs;
+    h->last_recs = &h->eager_recs;
+    h->last_eager = true;
+    int rc = fn();
+    h->recs = nullptr;
+    return rc;
   }
   if (!g.exec) {
     long long before = g_launches.load();
+    destroy_recs(g.recs);
+    h->recs = &g.recs;
     CK(cudaStreamBeginCapture(h->st, cudaStreamCaptureModeThreadLocal));
     int rc = fn();
+    h->recs = nullptr;
     cudaGraph_t graph = nullptr;
     cudaError_t ce = cudaStreamEndCapture(h->st, &graph);
     if (rc != HODLR_OK) {
@@ -197,6 +315,8 @@ static int run_graphed(hodlr_ctx *h, GraphEntry &g, int &runs, F fn) {
     g_launches.fetch_sub(g.kernels);  // counted on each replay instead
   }
   g_launches.fetch_add(g.kernels);
+  h->last_recs = &g.recs;
+  h->last_eager = false;
   CK(cudaGraphLaunch(g.exec, h->st));
   ++runs;
   return HODLR_OK;
@@ -222,18 +342,18 @@ template <typename T> static int factor_sweep(hodlr_ctx *h) {
   T *LU = LUptr<T>(h);
   T *Ut = Utptr<T>(h);
   const T *Vt = Vptr<T>(h);
-  CK(launch_leaf_getrf<T>(h->D, m, (long long)m * m, LU, h->ipiv, m, h->nleaf, h->dst, s));
+  PHASE(h, HODLR_PHASE_LEAF_LU, launch_leaf_getrf<T>(h->D, m, (long long)m * m, LU, h->ipiv, m, h->nleaf, h->dst, s));
   if (L == 0) return HODLR_OK;
   if (sizeof(T) == 8)
     CK(cudaMemcpyAsync(Ut, h->U, sizeof(double) * n * L * r, cudaMemcpyDeviceToDevice, s));
   else
     CK((launch_convert<double, float>(h->U, n, reinterpret_cast<float *>(Ut), n, n, L * r, s)));
-  CK(launch_leaf_getrs<T>(LU, h->ipiv, m, h->nleaf, Ut, n, L * r, false, nullptr, s));
+  PHASE(h, HODLR_PHASE_LEAF_SOLVE, launch_leaf_getrs<T>(LU, h->ipiv, m, h->nleaf, Ut, n, L * r, false, nullptr, s));
   for (int l = L - 1; l >= 0; --l) {
     const int nb = 2 << l;
     const long long rows = n >> (l + 1);
     const int Cd = l * r, Ct = Cd + r;
-    CK(launch_reduce_tn<T>(Vt + (long long)l * n * r, n, Ut, n, rows, nb, r, Ct, h->Tbuf, h->red, nullptr, s));
+    PHASE(h, HODLR_PHASE_REDUCE, launch_reduce_tn<T>(Vt + (long long)l * n * r, n, Ut, n, rows, nb, r, Ct, h->Tbuf, h->red, nullptr, s));
     CapArgs ca{};
     ca.Tb = h->Tbuf;
     ca.tb_stride = (long long)r * Ct;
@@ -248,7 +368,7 @@ template <typename T> static int factor_sweep(hodlr_ctx *h) {
     ca.factor = true;
     ca.trans = false;
     ca.st = h->dst;
-    CK(launch_capacitance(ca, s));
+    PHASE(h, HODLR_PHASE_CAPACITANCE, launch_capacitance(ca, s));
     if (Cd > 0) {
       UpdateArgs ua{};
       ua.A = Ut + (long long)l * r * n;
@@ -266,7 +386,7 @@ template <typename T> static int factor_sweep(hodlr_ctx *h) {
       ua.K = r;
       ua.nbatch = nb;
       ua.alpha = -1.0;
-      CK(launch_update_nn<T>(ua, s));
+      PHASE(h, HODLR_PHASE_UPDATE, launch_update_nn<T>(ua, s));
     }
   }
   return HODLR_OK;
@@ -281,14 +401,14 @@ static int solve_sweep(hodlr_ctx *h, T *X, long long ldx, int k, bool trans, con
   T *LU = LUptr<T>(h);
   T *Ut = Utptr<T>(h);
   const T *Vt = Vptr<T>(h);
-  if (!trans) CK(launch_leaf_getrs<T>(LU, h->ipiv, m, h->nleaf, X, ldx, k, false, skip, s));
+  if (!trans) PHASE(h, HODLR_PHASE_LEAF_SOLVE, launch_leaf_getrs<T>(LU, h->ipiv, m, h->nleaf, X, ldx, k, false, skip, s));
   for (int step = 0; step < L; ++step) {
     const int l = trans ? step : L - 1 - step;
     const int nb = 2 << l;
     const long long rows = n >> (l + 1);
     const T *Ared = trans ? Ut + (long long)l * r * n : Vt + (long long)l * n * r;
     const T *Aupd = trans ? Vt + (long long)l * n * r : Ut + (long long)l * r * n;
-    CK(launch_reduce_tn<T>(Ared, n, X, ldx, rows, nb, r, k, h->Tbuf, h->red, skip, s));
+    PHASE(h, HODLR_PHASE_REDUCE, launch_reduce_tn<T>(Ared, n, X, ldx, rows, nb, r, k, h->Tbuf, h->red, skip, s));
     CapArgs ca{};
     ca.Tb = h->Tbuf;
     ca.tb_stride = (long long)r * k;
@@ -304,7 +424,7 @@ static int solve_sweep(hodlr_ctx *h, T *X, long long ldx, int k, bool trans, con
     ca.trans = trans;
     ca.st = h->dst;
     ca.skip = skip;
-    CK(launch_capacitance(ca, s));
+    PHASE(h, HODLR_PHASE_CAPACITANCE, launch_capacitance(ca, s));
     UpdateArgs ua{};
     ua.A = Aupd;
     ua.lda = n;
@@ -324,9 +444,9 @@ static int solve_sweep(hodlr_ctx *h, T *X, long long ldx, int k, bool trans, con
     ua.nbatch = nb;
     ua.alpha = -1.0;
     ua.skip = skip;
-    CK(launch_update_nn<T>(ua, s));
+    PHASE(h, HODLR_PHASE_UPDATE, launch_update_nn<T>(ua, s));
   }
-  if (trans) CK(launch_leaf_getrs<T>(LU, h->ipiv, m, h->nleaf, X, ldx, k, true, skip, s));
+  if (trans) PHASE(h, HODLR_PHASE_LEAF_SOLVE, launch_leaf_getrs<T>(LU, h->ipiv, m, h->nleaf, X, ldx, k, true, skip, s));
   return HODLR_OK;
 }
 
@@ -358,13 +478,13 @@ static int matvec_fp64(hodlr_ctx *h, bool trans, const double *X, long long ldx,
   la.nbatch = h->nleaf;
   la.alpha = alpha;
   la.skip = skip;
-  CK(launch_update_nn<double>(la, s));
+  PHASE(h, HODLR_PHASE_RESID_LEAF, launch_update_nn<double>(la, s));
   for (int l = 0; l < L; ++l) {
     const int nb = 2 << l;
     const long long rows = n >> (l + 1);
     const double *Ared = trans ? h->Ulev(l) : h->Vlev(l);
     const double *Aupd = trans ? h->Vlev(l) : h->Ulev(l);
-    CK(launch_reduce_tn<double>(Ared, n, X, ldx, rows, nb, r, k, h->Tbuf, h->red, skip, s));
+    PHASE(h, HODLR_PHASE_RESID_REDUCE, launch_reduce_tn<double>(Ared, n, X, ldx, rows, nb, r, k, h->Tbuf, h->red, skip, s));
     UpdateArgs ua{};
     ua.A = Aupd;
     ua.lda = n;
@@ -384,15 +504,72 @@ static int matvec_fp64(hodlr_ctx *h, bool trans, const double *X, long long ldx,
     ua.nbatch = nb;
     ua.alpha = alpha;
     ua.skip = skip;
-    CK(launch_update_nn<double>(ua, s));
+    PHASE(h, HODLR_PHASE_RESID_UPDATE, launch_update_nn<double>(ua, s));
   }
   return HODLR_OK;
 }
 
-// R = B - op(A) X, FP64-accurate, with the handle's residual arithmetic.
+// R = B - op(A) X with double-word (FP32 pair) arithmetic on the FP32 pipes.
+static int residual_emulated(hodlr_ctx *h, bool trans, const double *X, long long ldx, const double *B,
+                             long long ldb, double *R, long long ldr, int k, const int *skip) {
+  const long long n = h->n;
+  const int m = h->m, L = h->L, r = h->r;
+  cudaStream_t s = h->st;
+  PHASE(h, HODLR_PHASE_MISC, launch_split(X, ldx, h->X2, n, n, k, skip, s));
+  DwUpdateArgs la{};
+  la.A = h->D2;
+  la.lda = m;
+  la.a_bstride = (long long)m * m;
+  la.a_trans = trans ? 1 : 0;
+  la.B = h->X2;
+  la.ldb = n;
+  la.b_s1 = 2LL * m;
+  la.b_s2 = m;
+  la.C = h->R2;
+  la.ldc = n;
+  la.c_bstride = m;
+  la.Cinit = B;
+  la.ldci = ldb;
+  la.M = m;
+  la.N = k;
+  la.K = m;
+  la.nbatch = h->nleaf;
+  la.skip = skip;
+  PHASE(h, HODLR_PHASE_RESID_LEAF, launch_dw_update(la, s));
+  for (int l = 0; l < L; ++l) {
+    const int nb = 2 << l;
+    const long long rows = n >> (l + 1);
+    const float2 *U2l = h->U2 + (long long)l * n * r, *V2l = h->V2 + (long long)l * n * r;
+    PHASE(h, HODLR_PHASE_RESID_REDUCE,
+          launch_dw_reduce(trans ? U2l : V2l, n, h->X2, n, rows, nb, r, k, h->Tbuf, h->red, skip, s));
+    PHASE(h, HODLR_PHASE_MISC, launch_scale_split(h->Tbuf, h->slev(l), r, (long long)nb * r * k, h->T2, skip, s));
+    DwUpdateArgs ua{};
+    ua.A = trans ? V2l : U2l;
+    ua.lda = n;
+    ua.a_bstride = rows;
+    ua.B = h->T2;
+    ua.ldb = r;
+    ua.b_s1 = 2LL * r * k;
+    ua.b_s2 = (long long)r * k;
+    ua.b_flip = 1;
+    ua.C = h->R2;
+    ua.ldc = n;
+    ua.c_bstride = rows;
+    ua.M = (int)rows;
+    ua.N = k;
+    ua.K = r;
+    ua.nbatch = nb;
+    ua.skip = skip;
+    PHASE(h, HODLR_PHASE_RESID_UPDATE, launch_dw_update(ua, s));
+  }
+  PHASE(h, HODLR_PHASE_MISC, launch_merge(h->R2, n, R, ldr, n, k, skip, s));
+  return HODLR_OK;
+}
 
+// R = B - op(A) X, FP64-accurate, with the handle's residual arithmetic.
 static int residual(hodlr_ctx *h, bool trans, const double *X, long long ldx, const double *B, long long ldb,
                     double *R, long long ldr, int k, const int *skip) {
+  if (h->emulated) return residual_emulated(h, trans, X, ldx, B, ldb, R, ldr, k, skip);
   return matvec_fp64(h, trans, X, ldx, B, ldb, R, ldr, k, -1.0, skip);
 }
 
@@ -494,6 +671,15 @@ int hodlr_create(const hodlr_desc *desc, hodlr_handle *out) {
     ALLOC(h->X64, double, (size_t)n * k);
     ALLOC(h->R64, double, (size_t)n * k);
     ALLOC(h->B64, double, (size_t)n * k);
+    if (d.residual == HODLR_RESID_FP64_EMULATED) {
+      h->emulated = true;
+      ALLOC(h->D2, float2, (size_t)h->nleaf * m * m);
+      ALLOC(h->U2, float2, (size_t)n * L * r);
+      ALLOC(h->V2, float2, (size_t)n * L * r);
+      ALLOC(h->X2, float2, (size_t)n * k);
+      ALLOC(h->R2, float2, (size_t)n * k);
+      ALLOC(h->T2, float2, h->tbuf_elems);
+    }
   } else {
     ALLOC(h->LU, double, (size_t)h->nleaf * m * m);
     ALLOC(h->Ut, double, (size_t)n * L * r);
@@ -555,7 +741,17 @@ int hodlr_set_stream(hodlr_handle h, void *stream) {
 int hodlr_set_leaf_blocks(hodlr_handle h, const double *D, int64_t ld, int64_t leaf_stride) {
   if (!h || !D) return set_err(HODLR_ERR_INVALID_ARG, "null argument");
   if (ld < h->m) return set_err(HODLR_ERR_INVALID_ARG, "ld < leaf size");
-  CK(launch_pack_leaves(D, ld, leaf_stride, h->D, h->m, h->nleaf, h->st));
+  const int m = h->m;
+  const long long mm = (long long)m * m;
+  if (ld == m && leaf_stride == mm) {
+    CK(cudaMemcpyAsync(h->D, D, sizeof(double) * mm * h->nleaf, cudaMemcpyDefault, h->st));
+  } else {
+    // column j of every leaf in one strided copy (host or device source)
+    for (int j = 0; j < m; ++j)
+      CK(cudaMemcpy2DAsync(h->D + (long long)j * m, sizeof(double) * mm, D + (long long)j * ld,
+                           sizeof(double) * leaf_stride, sizeof(double) * m, h->nleaf, cudaMemcpyDefault,
+                           h->st));
+  }
   h->has_D = true;
   h->factored = false;
   return HODLR_OK;
@@ -566,8 +762,11 @@ int hodlr_set_lowrank(hodlr_handle h, int level, const double *U, int64_t ldu, c
   if (!h || !U || !V) return set_err(HODLR_ERR_INVALID_ARG, "null argument");
   if (level < 0 || level >= h->L) return set_err(HODLR_ERR_INVALID_ARG, "level out of range");
   if (ldu < h->n || ldv < h->n) return set_err(HODLR_ERR_INVALID_ARG, "ld < n");
-  CK((launch_convert<double, double>(U, ldu, h->Ulev(level), h->n, h->n, h->r, h->st)));
-  CK((launch_convert<double, double>(V, ldv, h->Vlev(level), h->n, h->n, h->r, h->st)));
+  // plain (2-D) copies: the sources may be device or host memory
+  CK(cudaMemcpy2DAsync(h->Ulev(level), sizeof(double) * h->n, U, sizeof(double) * ldu, sizeof(double) * h->n,
+                       h->r, cudaMemcpyDefault, h->st));
+  CK(cudaMemcpy2DAsync(h->Vlev(level), sizeof(double) * h->n, V, sizeof(double) * ldv, sizeof(double) * h->n,
+                       h->r, cudaMemcpyDefault, h->st));
   if (s)
     CK(cudaMemcpyAsync(h->slev(level), s, sizeof(double) * h->r, cudaMemcpyDefault, h->st));
   else
@@ -587,15 +786,26 @@ int hodlr_factor(hodlr_handle h) {
   CK(cudaEventRecord(h->ev[0], h->st));
   int rc = run_graphed(h, h->factor_graph, h->factor_runs, [&]() -> int {
     if (h->mixed) {
+      const long long n = h->n, lr = (long long)h->L * h->r;
       if (h->L > 0)
-        CK((launch_convert<double, float>(h->V, h->n, h->V32, h->n, h->n, h->L * h->r, h->st)));
+        PHASE(h, HODLR_PHASE_MISC, (launch_convert<double, float>(h->V, n, h->V32, n, n, (int)lr, h->st)));
+      if (h->emulated) {
+        const long long dm = (long long)h->nleaf * h->m * h->m;
+        PHASE(h, HODLR_PHASE_MISC, launch_split(h->D, dm, h->D2, dm, dm, 1, nullptr, h->st));
+        if (h->L > 0) {
+          PHASE(h, HODLR_PHASE_MISC, launch_split(h->U, n, h->U2, n, n, (int)lr, nullptr, h->st));
+          PHASE(h, HODLR_PHASE_MISC, launch_split(h->V, n, h->V2, n, n, (int)lr, nullptr, h->st));
+        }
+      }
       return factor_sweep<float>(h);
     }
     return factor_sweep<double>(h);
   });
   CKS(rc);
   CK(cudaEventRecord(h->ev[1], h->st));
-  CKS(sync_status(h, nullptr));
+  int fst = sync_status(h, nullptr);
+  collect_phases(h);
+  CKS(fst);
   cudaEventElapsedTime(&h->factor_ms, h->ev[0], h->ev[1]);
   h->factored = true;
   return HODLR_OK;
@@ -627,6 +837,7 @@ static int solve_impl(hodlr_handle h, double *B, int64_t ldb, int nrhs, hodlr_so
     info->rel_residual = -1.0;
   }
   int st = sync_status(h, info);
+  collect_phases(h);
   cudaEventElapsedTime(&h->solve_ms, h->ev[2], h->ev[3]);
   if (st != HODLR_OK) return st;
   if (h->mixed && !h->hst->done) {
@@ -768,6 +979,46 @@ int hodlr_get_factors(hodlr_handle h, double *leaf_lu, int32_t *leaf_ipiv, doubl
   if (cap_ipiv && h->nnode > 0)
     CK(cudaMemcpyAsync(cap_ipiv, h->cap_ipiv, sizeof(int) * h->nnode * 2 * r, cudaMemcpyDeviceToDevice, s));
   CK(cudaStreamSynchronize(s));
+  return HODLR_OK;
+}
+
+int hodlr_get_inputs(hodlr_handle h, double *D, int64_t ld, int64_t leaf_stride, double *U, double *V,
+                     double *s) {
+  if (!h) return set_err(HODLR_ERR_INVALID_ARG, "null handle");
+  const int m = h->m;
+  const long long mm = (long long)m * m, n = h->n;
+  cudaStream_t st = h->st;
+  if (D) {
+    if (ld < m) return set_err(HODLR_ERR_INVALID_ARG, "ld < leaf size");
+    for (int j = 0; j < m; ++j)
+      CK(cudaMemcpy2DAsync(D + (long long)j * ld, sizeof(double) * leaf_stride, h->D + (long long)j * m,
+                           sizeof(double) * mm, sizeof(double) * m, h->nleaf, cudaMemcpyDefault, st));
+  }
+  const size_t lvl = sizeof(double) * n * h->L * h->r;
+  if (U && lvl) CK(cudaMemcpyAsync(U, h->U, lvl, cudaMemcpyDefault, st));
+  if (V && lvl) CK(cudaMemcpyAsync(V, h->V, lvl, cudaMemcpyDefault, st));
+  if (s && h->L) CK(cudaMemcpyAsync(s, h->s, sizeof(double) * h->L * h->r, cudaMemcpyDefault, st));
+  CK(cudaStreamSynchronize(st));
+  return HODLR_OK;
+}
+
+int hodlr_profile(hodlr_handle h, int enable, double *phase_ms, int64_t *phase_launches, int nphase) {
+  if (!h) return set_err(HODLR_ERR_INVALID_ARG, "null handle");
+  if (phase_ms || phase_launches) {
+    for (int p = 0; p < nphase && p < HODLR_NUM_PHASES; ++p) {
+      if (phase_ms) phase_ms[p] = h->phase_ms[p];
+      if (phase_launches) phase_launches[p] = h->phase_n[p];
+    }
+    for (int p = 0; p < HODLR_NUM_PHASES; ++p) {
+      h->phase_ms[p] = 0.0;
+      h->phase_n[p] = 0;
+    }
+  }
+  if (enable >= 0 && (enable != 0) != h->profile) {
+    CK(cudaStreamSynchronize(h->st));
+    clear_graphs(h);  // captured graphs carry (or lack) the timing events
+    h->profile = enable != 0;
+  }
   return HODLR_OK;
 }
 

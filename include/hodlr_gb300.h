@@ -130,14 +130,15 @@ HODLR_API int hodlr_set_stream(hodlr_handle h, void *stream);
 /* Leaf blocks: leaf i's m x m block starts at D + i*leaf_stride, column-major
  * with leading dimension ld.  fastSolver2's KTree region (N x m, LD = N,
  * leaf i at rows i*m) is ld = N, leaf_stride = m
- * (src/tree.cc:232-245, src/tasks/dense_block.cc:63-75).  Device pointer. */
+ * (src/tree.cc:232-245, src/tasks/dense_block.cc:63-75).  Device or host
+ * pointer (pinned host memory is copied asynchronously on the stream). */
 HODLR_API int hodlr_set_leaf_blocks(hodlr_handle h, const double *D, int64_t ld,
                           int64_t leaf_stride);
 
 /* Low-rank factors of level l (0 = root split): U, V are N x r column-major
  * with leading dimensions ldu, ldv; s is r entries or NULL (= ones).
  * Replaces the UTree column chunk and VTree::level(i) (src/tree.cc:61-73,
- * 189-197).  Device pointers. */
+ * 189-197).  Device or host pointers. */
 HODLR_API int hodlr_set_lowrank(hodlr_handle h, int level, const double *U, int64_t ldu,
                       const double *V, int64_t ldv, const double *s);
 
@@ -176,6 +177,13 @@ HODLR_API int hodlr_adjoint(hodlr_handle h, const double *x, int64_t ldx,
 HODLR_API int hodlr_get_factors(hodlr_handle h, double *leaf_lu, int32_t *leaf_ipiv,
                       double *utilde, double *cap_lu, int32_t *cap_ipiv);
 
+/* Copy out the problem held by the handle (device or host destinations; any
+ * may be NULL): leaf blocks in the layout of hodlr_set_leaf_blocks
+ * (ld, leaf_stride), U and V as L blocks of N x r (leading dimension N,
+ * level l at + l*N*r), s as L blocks of r. */
+HODLR_API int hodlr_get_inputs(hodlr_handle h, double *D, int64_t ld, int64_t leaf_stride, double *U,
+                               double *V, double *s);
+
 /* Fill the handle with a seeded synthetic problem on the device
  * (counter-based Gaussian generator): leaf blocks G/sqrt(m) + shift*I,
  * per-level U, V ~ N(0,1)/sqrt(n_block) (orthonormal != 0: each child
@@ -183,6 +191,27 @@ HODLR_API int hodlr_get_factors(hodlr_handle h, double *leaf_lu, int32_t *leaf_i
  * decay > 0.  Writes the right-hand side (N x nrhs, ldb) if B != NULL. */
 HODLR_API int hodlr_generate(hodlr_handle h, uint64_t seed, double shift, int orthonormal,
                    double decay, double *B, int64_t ldb, int nrhs);
+
+/* Phases of the per-phase device timing (hodlr_profile). */
+enum {
+  HODLR_PHASE_LEAF_LU = 0,       /* K1 leaf getrf */
+  HODLR_PHASE_LEAF_SOLVE = 1,    /* K2 leaf getrs */
+  HODLR_PHASE_REDUCE = 2,        /* K3 A^T X reductions of the sweeps */
+  HODLR_PHASE_CAPACITANCE = 3,   /* K4 capacitance LU / solves */
+  HODLR_PHASE_UPDATE = 4,        /* K5 low-rank updates of the sweeps */
+  HODLR_PHASE_RESID_LEAF = 5,    /* residual: leaf blocks */
+  HODLR_PHASE_RESID_REDUCE = 6,  /* residual: V^T x reductions */
+  HODLR_PHASE_RESID_UPDATE = 7,  /* residual: U (s . t) updates */
+  HODLR_PHASE_MISC = 8,          /* conversions, splits, norms */
+  HODLR_NUM_PHASES = 9
+};
+
+/* Per-phase device timing: enable = 1 / 0 switches CUDA-event timing of
+ * every launch (by phase) on or off (-1 leaves it); if phase_ms /
+ * phase_launches are given, the sums since the last read are copied out
+ * (nphase entries) and reset. */
+HODLR_API int hodlr_profile(hodlr_handle h, int enable, double *phase_ms, int64_t *phase_launches,
+                            int nphase);
 
 /* Milliseconds the last hodlr_factor / hodlr_solve spent on the device
  * (CUDA events on the handle's stream). */
