@@ -203,7 +203,7 @@ def run_ours(args, wl):
 
         for _ in range(args.warmup):
             step()
-        mixed.profile(1)
+        mixed.profile(0 if args.no_phase_timing else 1)
         mixed.profile(-1, read=True)
         for _ in range(2):   # capture the graphs with timing events outside the timed region
             step()
@@ -308,29 +308,43 @@ def run_ours(args, wl):
     F, S = algo_flops(n, m, L, r, k)
     nres = float(np.mean(iters)) + 1.0
     total_ms = sum(v[0] for v in phases.values())
-    # dominant phase of the mixed step and its roofline
-    dom = max(phases.items(), key=lambda kv: kv[1][0])
-    phase_flops = {
-        "leaf_lu": (2 / 3) * n * m * m,
-        "leaf_solve": 2 * n * m * L * r + (nres) * 2 * n * m * k,
-        "resid_leaf": nres * 2 * n * m * k,
-        "resid_reduce": nres * 2 * n * r * k * L,
-        "resid_update": nres * 2 * n * r * k * L,
+    # per-phase algorithmic work of one mixed step (FP64-equivalent flops)
+    nsw = float(np.mean(iters)) + 1.0        # sweeps = residual evaluations per solve
+    cap_f = sum((2 ** l) * ((2 / 3) * (2 * r) ** 3 + 2 * (2 * r) ** 3 + 2 * (2 * r) ** 2 * l * r) for l in range(L))
+    work = {
+        "leaf_lu": (2 / 3) * n * m * m + 2 * n * m * m,
+        "leaf_solve": 2 * n * m * L * r + nsw * 2 * n * m * k,
+        "reduce": sum(2 * n * r * (l + 1) * r for l in range(L)) + nsw * 2 * n * r * k * L,
+        "update": sum(2 * n * r * l * r for l in range(L)) + nsw * 2 * n * r * k * L,
+        "capacitance": cap_f + nsw * sum((2 ** l) * 2 * (2 * r) ** 2 * k for l in range(L)),
+        "resid_leaf": nsw * 2 * n * m * k,
+        "resid_reduce": nsw * 2 * n * r * k * L,
+        "resid_update": nsw * 2 * n * r * k * L,
     }
-    measured = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if os.path.exists(
-        os.path.join(ROOT, "MEASURED_PEAKS.json")) else {}
-    hbm_peak = measured.get("hbm_gbs", 6800.0)
-    dom_name, (dom_ms, dom_n) = dom
-    dom_steps = args.steps  # phases were summed over the timed steps
+    # peaks: FP32 FFMA (measured 70 TFLOP/s); a double-word FMA costs 12 FP32
+    # instructions, so its FP64-equivalent peak is 70/12 TFLOP/s
+    peak_of = {"leaf_lu": FP32_PEAK_TFLOPS, "leaf_solve": FP32_PEAK_TFLOPS, "reduce": FP32_PEAK_TFLOPS,
+               "update": FP32_PEAK_TFLOPS, "capacitance": DW_PEAK_TFLOPS,
+               "resid_leaf": DW_PEAK_TFLOPS if args.resid == 1 else FP64_PEAK_TFLOPS,
+               "resid_reduce": DW_PEAK_TFLOPS if args.resid == 1 else FP64_PEAK_TFLOPS,
+               "resid_update": DW_PEAK_TFLOPS if args.resid == 1 else FP64_PEAK_TFLOPS}
+    phase_report = {}
+    for name, (pms, pn) in phases.items():
+        per_step = pms / args.steps
+        ent = {"ms_per_step": per_step, "launches_per_step": pn / args.steps}
+        if name in work and per_step > 0:
+            ach = work[name] / (per_step * 1e-3) / 1e12
+            ent.update(tflops=ach, peak=peak_of[name], frac=ach / peak_of[name])
+        phase_report[name] = ent
+    dom_name = max(phase_report, key=lambda kk: phase_report[kk]["ms_per_step"])
+    d = phase_report[dom_name]
     roof = None
-    if dom_name in phase_flops and dom_ms > 0:
-        fl = phase_flops[dom_name] * dom_steps
-        achieved = fl / (dom_ms * 1e-3) / 1e12
-        peak = FP32_PEAK_TFLOPS if dom_name.startswith("resid") and args.resid == 1 else FP64_PEAK_TFLOPS
-        roof = {"kernel": dom_name, "bound": "fp32_simt" if peak == FP32_PEAK_TFLOPS else "fp64_dfma",
-                "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
-                "traffic": None, "avg_launch_ms": dom_ms / max(dom_n, 1),
-                "note": "FP64-equivalent flops; peak = measured FFMA/DFMA issue rate (profiles/fp_peaks.md)"}
+    if "tflops" in d:
+        roof = {"kernel": dom_name, "bound": "fp32_cuda_core", "achieved": d["tflops"], "peak": d["peak"],
+                "unit": "TFLOP/s", "frac": d["frac"], "traffic": None,
+                "avg_launch_ms": d["ms_per_step"] / max(d["launches_per_step"], 1),
+                "note": "FP64-equivalent algorithmic flops / CUDA-event phase time; peak = measured FFMA rate "
+                        "(double-word phases: /12 per emulated FMA)"}
     line = {
         "metric": METRIC, "value": ms, "unit": "ms", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": ms, "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
@@ -346,7 +360,7 @@ def run_ours(args, wl):
         "fp64_rel_resid": fp64_resid,
         "speedup_vs_fp64": float(np.mean(fp64_ms)) / ms,
         "algorithmic_gflop_per_step": (F + S) / 1e9,
-        "phases_ms_per_step": {kk: v[0] / args.steps for kk, v in phases.items()},
+        "phases": phase_report,
         "phase_timing_overhead_note": "per-phase CUDA events were recorded inside the timed graphs",
         "roofline": roof,
         "clocks": clk, "gpu_launches": launches, "wall_s": wall,
@@ -364,6 +378,7 @@ def run_ours(args, wl):
 # Measured on this machine's GB300 (FFMA / DFMA issue-rate probe, profiles/fp_peaks.md).
 FP32_PEAK_TFLOPS = 70.0
 FP64_PEAK_TFLOPS = 1.198
+DW_PEAK_TFLOPS = FP32_PEAK_TFLOPS / 12.0
 
 
 def main():
@@ -372,12 +387,14 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--resid", type=int, default=0, help="0 native FP64 residual, 1 FP64-emulated")
+    ap.add_argument("--resid", type=int, default=1, help="0 native FP64 residual, 1 FP64-emulated")
     ap.add_argument("--fp64-steps", type=int, default=3)
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--small", action="store_true", help="N=2^14 smoke-sized workload")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-phase-timing", action="store_true",
+                    help="no per-phase CUDA events in the timed graphs (for profiler runs)")
     args = ap.parse_args()
     wl = SMALL if args.small else WORKLOAD
     if args.impl == "reference":

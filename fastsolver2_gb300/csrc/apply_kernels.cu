@@ -1,0 +1,390 @@
+// Explicit-inverse application kernels.
+//
+// The small dense systems of the sweep (leaf blocks, m x m; capacitance
+// systems, 2r x 2r) are factorised once with partial pivoting (LU, as the
+// reference's dgesv calls do, src/tasks/leaf_solve.cc:89,140) and their
+// inverses A^{-1} = U^{-1} L^{-1} P are formed from the LU factors in the
+// same factorisation pass.  Every later application -- to the L*r columns of
+// the transformed bases, to the right-hand sides of each solve and of every
+// refinement step -- is then a batched GEMM instead of a pair of triangular
+// solves: no per-row synchronisation, full register tiling, and the same
+// flop count as the two triangular solves it replaces.
+#include <algorithm>
+#include <type_traits>
+
+#include "dense_ops.cuh"
+#include "kernels.cuh"
+#include "resid_emul.cuh"
+
+namespace hodlr {
+
+static constexpr size_t kSmemCap = 220 * 1024;
+
+template <typename K>
+static cudaError_t set_smem(K kernel, size_t bytes) {
+  if (bytes <= 48 * 1024) return cudaSuccess;
+  return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+}
+
+// --------------------------------------------------------- leaf inverse
+// Dinv_i = D_i^{-1} from the stored LU factors: getrs against identity
+// column tiles.  grid (tiles, nleaf).
+template <typename T, bool LU_SMEM>
+__global__ void __launch_bounds__(256)
+leaf_inverse_kernel(const T *__restrict__ LU, const int *__restrict__ ipiv, int m, T *Dinv, int ct) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int leaf = blockIdx.y, c0 = blockIdx.x * ct, nc = min(ct, m - c0);
+  T *sX = reinterpret_cast<T *>(smem_raw);
+  int *spiv = reinterpret_cast<int *>(sX + (size_t)m * ct);
+  T *sLU = reinterpret_cast<T *>(reinterpret_cast<uintptr_t>(spiv + m + 3) & ~uintptr_t(15));
+  const T *gLU = LU + (long long)leaf * m * m;
+  for (int i = threadIdx.x; i < m; i += blockDim.x) spiv[i] = ipiv[(long long)leaf * m + i];
+  if (LU_SMEM)
+    for (int e = threadIdx.x; e < m * m; e += blockDim.x) sLU[e] = gLU[e];
+  for (int e = threadIdx.x; e < m * nc; e += blockDim.x) {
+    const int i = e % m, j = e / m;
+    sX[e] = (i == c0 + j) ? T(1) : T(0);
+  }
+  __syncthreads();
+  block_getrs<T, false>(LU_SMEM ? sLU : gLU, m, spiv, m, sX, m, nc);
+  T *out = Dinv + (long long)leaf * m * m + (long long)c0 * m;
+  for (int e = threadIdx.x; e < m * nc; e += blockDim.x) out[e] = sX[e];
+}
+
+template <typename T>
+cudaError_t launch_leaf_inverse(const T *LU, const int *ipiv, int m, int nleaf, T *Dinv, cudaStream_t s) {
+  const size_t lu_bytes = (size_t)m * m * sizeof(T), piv_bytes = (size_t)m * 4 + 16;
+  const bool lu_smem = lu_bytes + piv_bytes + (size_t)m * 8 * sizeof(T) <= kSmemCap;
+  const size_t avail = kSmemCap - piv_bytes - (lu_smem ? lu_bytes : 0);
+  const int ct_max = (int)std::min<size_t>(avail / ((size_t)m * sizeof(T)), 128);
+  const int ntile = ceil_div(m, ct_max), ct = ceil_div(m, ntile);
+  const size_t bytes = (size_t)m * ct * sizeof(T) + piv_bytes + (lu_smem ? lu_bytes : 0);
+  dim3 grid(ntile, nleaf);
+  if (lu_smem) {
+    auto k = leaf_inverse_kernel<T, true>;
+    cudaError_t e = set_smem(k, bytes);
+    if (e != cudaSuccess) return e;
+    HODLR_LAUNCH(k, grid, 256, bytes, s, LU, ipiv, m, Dinv, ct);
+  } else {
+    auto k = leaf_inverse_kernel<T, false>;
+    cudaError_t e = set_smem(k, bytes);
+    if (e != cudaSuccess) return e;
+    HODLR_LAUNCH(k, grid, 256, bytes, s, LU, ipiv, m, Dinv, ct);
+  }
+  return cudaGetLastError();
+}
+template cudaError_t launch_leaf_inverse<double>(const double *, const int *, int, int, double *, cudaStream_t);
+template cudaError_t launch_leaf_inverse<float>(const float *, const int *, int, int, float *, cudaStream_t);
+
+// ----------------------------------------------------------- leaf apply
+// X_i := op(Dinv_i) X_i in place for the rows of every leaf i, columns
+// [0, ncols).  One CTA per (leaf, tile of CT = 8192/M columns): the X tile is
+// staged whole (so the in-place write is safe), Dinv streams through shared
+// memory in 32-column slabs, each thread owns an (M/16) x (CT/16) register
+// tile.
+template <typename T, int M, bool TRANS>
+__global__ void __launch_bounds__(256)
+leaf_apply_kernel(const T *__restrict__ Dinv, T *X, long long ldx, int ncols, const int *skip) {
+  if (skip && *skip) return;
+  constexpr int CT = 8192 / M, KC = 32, RPT = M / 16, CPT = CT / 16;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T *sX = reinterpret_cast<T *>(smem_raw);      // M x CT, ld M
+  T *sA = sX + M * CT;                          // M x KC slab of op(Dinv), [k][i] layout (ld M)
+  const int leaf = blockIdx.y, c0 = blockIdx.x * CT, nc = min(CT, ncols - c0);
+  const T *A = Dinv + (long long)leaf * M * M;
+  T *Xg = X + (long long)leaf * M + (long long)c0 * ldx;
+  const int tid = threadIdx.x, ti = tid & 15, tj = tid >> 4;
+  for (int e = tid; e < M * CT; e += 256) {
+    const int i = e % M, j = e / M;
+    sX[e] = j < nc ? Xg[i + (long long)j * ldx] : T(0);
+  }
+  T acc[RPT][CPT];
+#pragma unroll
+  for (int a = 0; a < RPT; ++a)
+#pragma unroll
+    for (int b = 0; b < CPT; ++b) acc[a][b] = T(0);
+  for (int k0 = 0; k0 < M; k0 += KC) {
+    __syncthreads();
+    // slab: sA[q][i] = op(Dinv)(i, k0 + q)
+    for (int e = tid; e < M * KC; e += 256) {
+      const int i = e % M, q = e / M;
+      sA[q * M + i] = TRANS ? A[(k0 + q) + (long long)i * M] : A[i + (long long)(k0 + q) * M];
+    }
+    __syncthreads();
+#pragma unroll 4
+    for (int q = 0; q < KC; ++q) {
+      T av[RPT], xv[CPT];
+#pragma unroll
+      for (int a = 0; a < RPT; ++a) av[a] = sA[q * M + ti + 16 * a];
+#pragma unroll
+      for (int b = 0; b < CPT; ++b) xv[b] = sX[(k0 + q) + (tj + 16 * b) * M];
+#pragma unroll
+      for (int a = 0; a < RPT; ++a)
+#pragma unroll
+        for (int b = 0; b < CPT; ++b) acc[a][b] += av[a] * xv[b];
+    }
+  }
+#pragma unroll
+  for (int b = 0; b < CPT; ++b) {
+    const int j = tj + 16 * b;
+    if (j >= nc) continue;
+#pragma unroll
+    for (int a = 0; a < RPT; ++a) Xg[ti + 16 * a + (long long)j * ldx] = acc[a][b];
+  }
+}
+
+template <typename T, int M>
+static cudaError_t leaf_apply_m(const T *Dinv, int nleaf, T *X, long long ldx, int ncols, bool trans,
+                                const int *skip, cudaStream_t s) {
+  constexpr int CT = 8192 / M;
+  const size_t bytes = (size_t)M * CT * sizeof(T) + (size_t)M * 32 * sizeof(T);
+  dim3 grid(ceil_div(ncols, CT), nleaf);
+  if (trans) {
+    auto k = leaf_apply_kernel<T, M, true>;
+    cudaError_t e = set_smem(k, bytes);
+    if (e != cudaSuccess) return e;
+    HODLR_LAUNCH(k, grid, 256, bytes, s, Dinv, X, ldx, ncols, skip);
+  } else {
+    auto k = leaf_apply_kernel<T, M, false>;
+    cudaError_t e = set_smem(k, bytes);
+    if (e != cudaSuccess) return e;
+    HODLR_LAUNCH(k, grid, 256, bytes, s, Dinv, X, ldx, ncols, skip);
+  }
+  return cudaGetLastError();
+}
+
+bool leaf_apply_supported(int m) { return m == 64 || m == 128 || m == 256; }
+
+template <typename T>
+cudaError_t launch_leaf_apply(const T *Dinv, int m, int nleaf, T *X, long long ldx, int ncols, bool trans,
+                              const int *skip, cudaStream_t s) {
+  if (ncols <= 0 || nleaf <= 0) return cudaSuccess;
+  switch (m) {
+    case 64: return leaf_apply_m<T, 64>(Dinv, nleaf, X, ldx, ncols, trans, skip, s);
+    case 128: return leaf_apply_m<T, 128>(Dinv, nleaf, X, ldx, ncols, trans, skip, s);
+    case 256: return leaf_apply_m<T, 256>(Dinv, nleaf, X, ldx, ncols, trans, skip, s);
+    default: return cudaErrorInvalidValue;
+  }
+}
+template cudaError_t launch_leaf_apply<double>(const double *, int, int, double *, long long, int, bool,
+                                               const int *, cudaStream_t);
+template cudaError_t launch_leaf_apply<float>(const float *, int, int, float *, long long, int, bool,
+                                              const int *, cudaStream_t);
+
+// ------------------------------------------------------ capacitance factor
+// One CTA per node of a depth: S = [I, s.T1u; s.T0u, I] (FP64), LU with
+// partial pivoting (stored for inspection), then Sinv = S^{-1} (FP64, and a
+// double-word copy when sinv2 is given).
+__global__ void __launch_bounds__(256) cap_factor_kernel(CapFactorArgs a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ int s_info;
+  const int p = blockIdx.x, node = a.node_base + p;
+  const int r = a.r, n2 = 2 * r;
+  double *S = reinterpret_cast<double *>(smem_raw);
+  double *W = S + n2 * n2;  // n2 x 32 identity tile
+  int *piv = reinterpret_cast<int *>(W + n2 * 32);
+  const double *T0 = a.Tb + (long long)(2 * p) * a.tb_stride;
+  const double *T1 = a.Tb + (long long)(2 * p + 1) * a.tb_stride;
+  for (int e = threadIdx.x; e < n2 * n2; e += blockDim.x) {
+    const int i = e % n2, j = e / n2;
+    double v = (i == j) ? 1.0 : 0.0;
+    if (i >= r && j < r) v = (a.scale ? a.scale[i - r] : 1.0) * T0[(i - r) + (long long)(a.ucol + j) * r];
+    if (i < r && j >= r) v = (a.scale ? a.scale[i] : 1.0) * T1[i + (long long)(a.ucol + j - r) * r];
+    S[e] = v;
+  }
+  __syncthreads();
+  block_getrf<double>(S, n2, n2, piv, &s_info);
+  if (s_info && threadIdx.x == 0) report_error(a.st, HODLR_ERR_SINGULAR_CAPACITANCE, node);
+  double *gS = a.cap_lu + (long long)node * n2 * n2;
+  for (int e = threadIdx.x; e < n2 * n2; e += blockDim.x) gS[e] = S[e];
+  for (int e = threadIdx.x; e < n2; e += blockDim.x) a.cap_ipiv[(long long)node * n2 + e] = piv[e];
+  double *gI = a.sinv + (long long)node * n2 * n2;
+  float2 *gI2 = a.sinv2 ? a.sinv2 + (long long)node * n2 * n2 : nullptr;
+  for (int c0 = 0; c0 < n2; c0 += 32) {
+    const int nc = min(32, n2 - c0);
+    for (int e = threadIdx.x; e < n2 * nc; e += blockDim.x) {
+      const int i = e % n2, j = e / n2;
+      W[e] = (i == c0 + j) ? 1.0 : 0.0;
+    }
+    __syncthreads();
+    block_getrs<double, false>(S, n2, piv, n2, W, n2, nc);
+    for (int e = threadIdx.x; e < n2 * nc; e += blockDim.x) {
+      gI[(long long)c0 * n2 + e] = W[e];
+      if (gI2) {
+        const float h = __double2float_rn(W[e]);
+        gI2[(long long)c0 * n2 + e] = make_float2(h, __double2float_rn(W[e] - (double)h));
+      }
+    }
+    __syncthreads();
+  }
+}
+
+cudaError_t launch_cap_factor(const CapFactorArgs &a, cudaStream_t s) {
+  if (a.nnode <= 0) return cudaSuccess;
+  if (a.r < 1 || a.r > 64) return cudaErrorInvalidValue;
+  const int n2 = 2 * a.r;
+  const size_t bytes = (size_t)n2 * n2 * 8 + (size_t)n2 * 32 * 8 + (size_t)n2 * 4 + 16;
+  cudaError_t e = set_smem(cap_factor_kernel, bytes);
+  if (e != cudaSuccess) return e;
+  HODLR_LAUNCH(cap_factor_kernel, a.nnode, 256, bytes, s, a);
+  return cudaGetLastError();
+}
+
+// ------------------------------------------------------- capacitance apply
+// eta_p = op(Sinv_p) RHS_p for the nodes of one depth, RHS_p built from the
+// children's T blocks: forward [s.T1; s.T0] with Sinv, transposed [T0; T1]
+// with Sinv^T.  FP64 (DFMA) or double-word (FP32 pipes, FP64-accurate).
+// grid (column tiles of 32, nnode); each thread owns MT x 4 outputs.
+__device__ __forceinline__ void dw2_fma(float ah, float al, float xh, float xl, float &sh, float &sl) {
+  const float pr = ah * xh;
+  const float e = fmaf(ah, xh, -pr);
+  const float s = sh + pr;
+  const float bb = s - sh;
+  const float t = (sh - (s - bb)) + (pr - bb);
+  sh = s;
+  sl += t + e;
+  sl = fmaf(ah, xl, sl);
+  sl = fmaf(al, xh, sl);
+}
+
+template <int MT, bool DW>
+__global__ void __launch_bounds__(256) cap_apply_kernel(CapApplyArgs a) {
+  if (a.skip && *a.skip) return;
+  using E = typename std::conditional<DW, float2, double>::type;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int r = a.r, n2 = 2 * r;
+  constexpr int NP = MT * 32;  // padded rows
+  E *sS = reinterpret_cast<E *>(smem_raw);   // [q][i], NP x NP (op(Sinv)(i, q) at sS[q*NP + i])
+  E *sR = sS + NP * NP;                      // [q][j], NP x 32
+  const int p = blockIdx.y, c0 = blockIdx.x * 32, nc = min(32, a.C - c0);
+  const int node = a.node_base + p;
+  const double *Sg = a.sinv + (long long)node * n2 * n2;
+  const float2 *Sg2 = a.sinv2 ? a.sinv2 + (long long)node * n2 * n2 : nullptr;
+  for (int e = threadIdx.x; e < NP * NP; e += blockDim.x) {
+    const int i = e % NP, q = e / NP;
+    E v;
+    if constexpr (DW) {
+      v = make_float2(0.f, 0.f);
+      if (i < n2 && q < n2) v = a.trans ? Sg2[q + (long long)i * n2] : Sg2[i + (long long)q * n2];
+    } else {
+      v = 0.0;
+      if (i < n2 && q < n2) v = a.trans ? Sg[q + (long long)i * n2] : Sg[i + (long long)q * n2];
+    }
+    sS[q * NP + i] = v;
+  }
+  const double *T0 = a.Tb + (long long)(2 * p) * a.tb_stride;
+  const double *T1 = a.Tb + (long long)(2 * p + 1) * a.tb_stride;
+  for (int e = threadIdx.x; e < NP * 32; e += blockDim.x) {
+    const int q = e % NP, j = e / NP;
+    double v = 0.0;
+    if (q < n2 && j < nc) {
+      if (!a.trans)
+        v = (q < r) ? (a.scale ? a.scale[q] : 1.0) * T1[q + (long long)(c0 + j) * r]
+                    : (a.scale ? a.scale[q - r] : 1.0) * T0[(q - r) + (long long)(c0 + j) * r];
+      else
+        v = (q < r) ? T0[q + (long long)(c0 + j) * r] : T1[(q - r) + (long long)(c0 + j) * r];
+    }
+    if constexpr (DW) {
+      const float h = __double2float_rn(v);
+      sR[j * NP + q] = make_float2(h, __double2float_rn(v - (double)h));
+    } else {
+      sR[j * NP + q] = v;
+    }
+  }
+  __syncthreads();
+  const int ti = threadIdx.x & 31, tj = threadIdx.x >> 5;
+  double *eta = a.eta + (long long)p * n2 * a.C;
+  if constexpr (DW) {
+    float sh[MT][4], sl[MT][4];
+#pragma unroll
+    for (int u = 0; u < MT; ++u)
+#pragma unroll
+      for (int v = 0; v < 4; ++v) sh[u][v] = sl[u][v] = 0.f;
+    for (int q = 0; q < n2; ++q) {
+      float2 sv[MT];
+#pragma unroll
+      for (int u = 0; u < MT; ++u) sv[u] = sS[q * NP + ti + 32 * u];
+#pragma unroll
+      for (int v = 0; v < 4; ++v) {
+        const float2 rv = sR[(tj + 8 * v) * NP + q];
+#pragma unroll
+        for (int u = 0; u < MT; ++u) dw2_fma(sv[u].x, sv[u].y, rv.x, rv.y, sh[u][v], sl[u][v]);
+      }
+      if ((q & 31) == 31) {
+#pragma unroll
+        for (int u = 0; u < MT; ++u)
+#pragma unroll
+          for (int v = 0; v < 4; ++v) {
+            const float s = sh[u][v] + sl[u][v];
+            sl[u][v] = sl[u][v] - (s - sh[u][v]);
+            sh[u][v] = s;
+          }
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < MT; ++u) {
+      const int i = ti + 32 * u;
+      if (i >= n2) continue;
+#pragma unroll
+      for (int v = 0; v < 4; ++v) {
+        const int j = tj + 8 * v;
+        if (j < nc) eta[i + (long long)(c0 + j) * n2] = (double)sh[u][v] + (double)sl[u][v];
+      }
+    }
+  } else {
+    double acc[MT][4];
+#pragma unroll
+    for (int u = 0; u < MT; ++u)
+#pragma unroll
+      for (int v = 0; v < 4; ++v) acc[u][v] = 0.0;
+    for (int q = 0; q < n2; ++q) {
+      double sv[MT];
+#pragma unroll
+      for (int u = 0; u < MT; ++u) sv[u] = sS[q * NP + ti + 32 * u];
+#pragma unroll
+      for (int v = 0; v < 4; ++v) {
+        const double rv = sR[(tj + 8 * v) * NP + q];
+#pragma unroll
+        for (int u = 0; u < MT; ++u) acc[u][v] = fma(sv[u], rv, acc[u][v]);
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < MT; ++u) {
+      const int i = ti + 32 * u;
+      if (i >= n2) continue;
+#pragma unroll
+      for (int v = 0; v < 4; ++v) {
+        const int j = tj + 8 * v;
+        if (j < nc) eta[i + (long long)(c0 + j) * n2] = acc[u][v];
+      }
+    }
+  }
+}
+
+cudaError_t launch_cap_apply(const CapApplyArgs &a, cudaStream_t s) {
+  if (a.nnode <= 0 || a.C <= 0) return cudaSuccess;
+  if (a.r < 1 || a.r > 64) return cudaErrorInvalidValue;
+  const int n2 = 2 * a.r;
+  const int MT = n2 <= 32 ? 1 : (n2 <= 64 ? 2 : 4);
+  const int NP = MT * 32;
+  const bool dw = a.sinv2 != nullptr;
+  const size_t es = dw ? sizeof(float2) : sizeof(double);
+  const size_t bytes = (size_t)NP * NP * es + (size_t)NP * 32 * es;
+  dim3 grid(ceil_div(a.C, 32), a.nnode);
+#define HODLR_CAPA(MTV, DWV)                                   \
+  {                                                            \
+    auto k = cap_apply_kernel<MTV, DWV>;                       \
+    cudaError_t e = set_smem(k, bytes);                        \
+    if (e != cudaSuccess) return e;                            \
+    HODLR_LAUNCH(k, grid, 256, bytes, s, a);                   \
+  }
+  if (dw) {
+    if (MT == 1) HODLR_CAPA(1, true) else if (MT == 2) HODLR_CAPA(2, true) else HODLR_CAPA(4, true)
+  } else {
+    if (MT == 1) HODLR_CAPA(1, false) else if (MT == 2) HODLR_CAPA(2, false) else HODLR_CAPA(4, false)
+  }
+#undef HODLR_CAPA
+  return cudaGetLastError();
+}
+
+}  // namespace hodlr

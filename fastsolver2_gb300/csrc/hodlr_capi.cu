@@ -106,6 +106,10 @@ struct hodlr_ctx {
   int *ipiv = nullptr;
   double *capLU = nullptr;
   int *cap_ipiv = nullptr;
+  double *Sinv = nullptr;     // [nnode][2r][2r] FP64 capacitance inverses
+  float2 *Sinv2 = nullptr;    // their double-word split (mixed mode)
+  double *Dinv = nullptr;     // [nleaf][m][m] leaf inverses (FP64 mode)
+  float *Dinv32 = nullptr;    // (mixed mode)
   bool factored = false;
   // workspaces
   double *Tbuf = nullptr, *Wbuf = nullptr, *eta = nullptr, *red = nullptr;
@@ -333,8 +337,46 @@ template <typename T> static const T *Vptr(hodlr_ctx *h);
 template <> const double *Vptr<double>(hodlr_ctx *h) { return h->V; }
 template <> const float *Vptr<float>(hodlr_ctx *h) { return h->V32; }
 
-// Factorisation sweep: leaf LU, Ut = D^{-1} U (all levels at once), then for
-// depth L-1 .. 0: T = V^T [Ut_d | Ut_u], capacitance LU + eta, Ut_d -= Ut_u eta.
+template <typename T> static T *Dinvptr(hodlr_ctx *h);
+template <> double *Dinvptr<double>(hodlr_ctx *h) { return h->Dinv; }
+template <> float *Dinvptr<float>(hodlr_ctx *h) { return h->Dinv32; }
+
+// X := D^{-1} X (or D^{-T} X) on every leaf's rows: explicit inverse GEMM when
+// the leaf size has a tuned kernel, LU triangular solves otherwise.
+template <typename T>
+static int leaf_solve(hodlr_ctx *h, T *X, long long ldx, int ncols, bool trans, const int *skip) {
+  T *Dinv = Dinvptr<T>(h);
+  if (Dinv)
+    PHASE(h, HODLR_PHASE_LEAF_SOLVE,
+          launch_leaf_apply<T>(Dinv, h->m, h->nleaf, X, ldx, ncols, trans, skip, h->st));
+  else
+    PHASE(h, HODLR_PHASE_LEAF_SOLVE,
+          launch_leaf_getrs<T>(LUptr<T>(h), h->ipiv, h->m, h->nleaf, X, ldx, ncols, trans, skip, h->st));
+  return HODLR_OK;
+}
+
+// eta = op(Sinv) RHS for the nodes of depth l (RHS from the T blocks).
+static int cap_apply(hodlr_ctx *h, int l, int C, long long tb_stride, bool trans, const int *skip) {
+  CapApplyArgs ca{};
+  ca.Tb = h->Tbuf;
+  ca.tb_stride = tb_stride;
+  ca.scale = h->slev(l);
+  ca.sinv = h->Sinv;
+  ca.sinv2 = h->mixed ? h->Sinv2 : nullptr;
+  ca.eta = h->eta;
+  ca.r = h->r;
+  ca.C = C;
+  ca.nnode = 1 << l;
+  ca.node_base = (1 << l) - 1;
+  ca.trans = trans;
+  ca.skip = skip;
+  PHASE(h, HODLR_PHASE_CAPACITANCE, launch_cap_apply(ca, h->st));
+  return HODLR_OK;
+}
+
+// Factorisation sweep: leaf LU (+ explicit leaf inverses), Ut = D^{-1} U
+// (all levels at once), then for depth L-1 .. 0: T = V^T [Ut_d | Ut_u],
+// capacitance LU + inverse, eta = Sinv [s.T1d; s.T0d], Ut_d -= Ut_u eta.
 template <typename T> static int factor_sweep(hodlr_ctx *h) {
   const long long n = h->n;
   const int m = h->m, L = h->L, r = h->r;
@@ -343,33 +385,37 @@ template <typename T> static int factor_sweep(hodlr_ctx *h) {
   T *Ut = Utptr<T>(h);
   const T *Vt = Vptr<T>(h);
   PHASE(h, HODLR_PHASE_LEAF_LU, launch_leaf_getrf<T>(h->D, m, (long long)m * m, LU, h->ipiv, m, h->nleaf, h->dst, s));
+  if (Dinvptr<T>(h))
+    PHASE(h, HODLR_PHASE_LEAF_LU, launch_leaf_inverse<T>(LU, h->ipiv, m, h->nleaf, Dinvptr<T>(h), s));
   if (L == 0) return HODLR_OK;
   if (sizeof(T) == 8)
     CK(cudaMemcpyAsync(Ut, h->U, sizeof(double) * n * L * r, cudaMemcpyDeviceToDevice, s));
   else
-    CK((launch_convert<double, float>(h->U, n, reinterpret_cast<float *>(Ut), n, n, L * r, s)));
-  PHASE(h, HODLR_PHASE_LEAF_SOLVE, launch_leaf_getrs<T>(LU, h->ipiv, m, h->nleaf, Ut, n, L * r, false, nullptr, s));
+    PHASE(h, HODLR_PHASE_MISC,
+          (launch_convert<double, float>(h->U, n, reinterpret_cast<float *>(Ut), n, n, L * r, s)));
+  CKS(leaf_solve<T>(h, Ut, n, L * r, false, nullptr));
   for (int l = L - 1; l >= 0; --l) {
     const int nb = 2 << l;
     const long long rows = n >> (l + 1);
     const int Cd = l * r, Ct = Cd + r;
-    PHASE(h, HODLR_PHASE_REDUCE, launch_reduce_tn<T>(Vt + (long long)l * n * r, n, Ut, n, rows, nb, r, Ct, h->Tbuf, h->red, nullptr, s));
-    CapArgs ca{};
-    ca.Tb = h->Tbuf;
-    ca.tb_stride = (long long)r * Ct;
-    ca.scale = h->slev(l);
-    ca.cap_lu = h->capLU;
-    ca.cap_ipiv = h->cap_ipiv;
-    ca.eta = h->eta;
-    ca.r = r;
-    ca.C = Cd;
-    ca.nnode = 1 << l;
-    ca.node_base = (1 << l) - 1;
-    ca.factor = true;
-    ca.trans = false;
-    ca.st = h->dst;
-    PHASE(h, HODLR_PHASE_CAPACITANCE, launch_capacitance(ca, s));
+    PHASE(h, HODLR_PHASE_REDUCE,
+          launch_reduce_tn<T>(Vt + (long long)l * n * r, n, Ut, n, rows, nb, r, Ct, h->Tbuf, h->red, nullptr, s));
+    CapFactorArgs cf{};
+    cf.Tb = h->Tbuf;
+    cf.tb_stride = (long long)r * Ct;
+    cf.scale = h->slev(l);
+    cf.ucol = Cd;
+    cf.cap_lu = h->capLU;
+    cf.cap_ipiv = h->cap_ipiv;
+    cf.sinv = h->Sinv;
+    cf.sinv2 = h->mixed ? h->Sinv2 : nullptr;
+    cf.r = r;
+    cf.nnode = 1 << l;
+    cf.node_base = (1 << l) - 1;
+    cf.st = h->dst;
+    PHASE(h, HODLR_PHASE_CAPACITANCE, launch_cap_factor(cf, s));
     if (Cd > 0) {
+      CKS(cap_apply(h, l, Cd, (long long)r * Ct, false, nullptr));
       UpdateArgs ua{};
       ua.A = Ut + (long long)l * r * n;
       ua.lda = n;
@@ -396,12 +442,11 @@ template <typename T> static int factor_sweep(hodlr_ctx *h) {
 template <typename T>
 static int solve_sweep(hodlr_ctx *h, T *X, long long ldx, int k, bool trans, const int *skip) {
   const long long n = h->n;
-  const int m = h->m, L = h->L, r = h->r;
+  const int L = h->L, r = h->r;
   cudaStream_t s = h->st;
-  T *LU = LUptr<T>(h);
   T *Ut = Utptr<T>(h);
   const T *Vt = Vptr<T>(h);
-  if (!trans) PHASE(h, HODLR_PHASE_LEAF_SOLVE, launch_leaf_getrs<T>(LU, h->ipiv, m, h->nleaf, X, ldx, k, false, skip, s));
+  if (!trans) CKS(leaf_solve<T>(h, X, ldx, k, false, skip));
   for (int step = 0; step < L; ++step) {
     const int l = trans ? step : L - 1 - step;
     const int nb = 2 << l;
@@ -409,22 +454,7 @@ static int solve_sweep(hodlr_ctx *h, T *X, long long ldx, int k, bool trans, con
     const T *Ared = trans ? Ut + (long long)l * r * n : Vt + (long long)l * n * r;
     const T *Aupd = trans ? Vt + (long long)l * n * r : Ut + (long long)l * r * n;
     PHASE(h, HODLR_PHASE_REDUCE, launch_reduce_tn<T>(Ared, n, X, ldx, rows, nb, r, k, h->Tbuf, h->red, skip, s));
-    CapArgs ca{};
-    ca.Tb = h->Tbuf;
-    ca.tb_stride = (long long)r * k;
-    ca.scale = h->slev(l);
-    ca.cap_lu = h->capLU;
-    ca.cap_ipiv = h->cap_ipiv;
-    ca.eta = h->eta;
-    ca.r = r;
-    ca.C = k;
-    ca.nnode = 1 << l;
-    ca.node_base = (1 << l) - 1;
-    ca.factor = false;
-    ca.trans = trans;
-    ca.st = h->dst;
-    ca.skip = skip;
-    PHASE(h, HODLR_PHASE_CAPACITANCE, launch_capacitance(ca, s));
+    CKS(cap_apply(h, l, k, (long long)r * k, trans, skip));
     UpdateArgs ua{};
     ua.A = Aupd;
     ua.lda = n;
@@ -446,7 +476,7 @@ static int solve_sweep(hodlr_ctx *h, T *X, long long ldx, int k, bool trans, con
     ua.skip = skip;
     PHASE(h, HODLR_PHASE_UPDATE, launch_update_nn<T>(ua, s));
   }
-  if (trans) PHASE(h, HODLR_PHASE_LEAF_SOLVE, launch_leaf_getrs<T>(LU, h->ipiv, m, h->nleaf, X, ldx, k, true, skip, s));
+  if (trans) CKS(leaf_solve<T>(h, X, ldx, k, true, skip));
   return HODLR_OK;
 }
 
@@ -663,6 +693,14 @@ int hodlr_create(const hodlr_desc *desc, hodlr_handle *out) {
   ALLOC(h->ipiv, int, (size_t)n);
   ALLOC(h->capLU, double, (size_t)std::max(1, h->nnode) * 4 * r * r);
   ALLOC(h->cap_ipiv, int, (size_t)std::max(1, h->nnode) * 2 * r);
+  ALLOC(h->Sinv, double, (size_t)std::max(1, h->nnode) * 4 * r * r);
+  if (h->mixed) ALLOC(h->Sinv2, float2, (size_t)std::max(1, h->nnode) * 4 * r * r);
+  if (leaf_apply_supported(m)) {
+    if (h->mixed)
+      ALLOC(h->Dinv32, float, (size_t)h->nleaf * m * m);
+    else
+      ALLOC(h->Dinv, double, (size_t)h->nleaf * m * m);
+  }
   if (h->mixed) {
     ALLOC(h->LU32, float, (size_t)h->nleaf * m * m);
     ALLOC(h->V32, float, (size_t)n * L * r);

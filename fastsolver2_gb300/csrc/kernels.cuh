@@ -71,6 +71,43 @@ struct CapArgs {
 };
 cudaError_t launch_capacitance(const CapArgs &a, cudaStream_t s);
 
+// Explicit inverses of the leaf blocks from their LU factors ([nleaf][m][m]).
+template <typename T>
+cudaError_t launch_leaf_inverse(const T *LU, const int *ipiv, int m, int nleaf, T *Dinv, cudaStream_t s);
+// X_i := op(Dinv_i) X_i on the rows of every leaf (m in {64, 128, 256}).
+bool leaf_apply_supported(int m);
+template <typename T>
+cudaError_t launch_leaf_apply(const T *Dinv, int m, int nleaf, T *X, long long ldx, int ncols, bool trans,
+                              const int *skip, cudaStream_t s);
+
+// Capacitance factorisation of the nodes of one depth: S from the T blocks'
+// columns [ucol, ucol + r), FP64 LU (stored in cap_lu / cap_ipiv) and the FP64
+// inverse Sinv (plus its double-word split in sinv2 when given).
+struct CapFactorArgs {
+  const double *Tb; long long tb_stride;
+  const double *scale;
+  int ucol;
+  double *cap_lu; int *cap_ipiv;
+  double *sinv; float2 *sinv2;
+  int r, nnode, node_base;
+  DevStatus *st;
+};
+cudaError_t launch_cap_factor(const CapFactorArgs &a, cudaStream_t s);
+
+// eta_p = op(Sinv_p) RHS_p (2r x C per node, ld 2r) with RHS_p built from the
+// T blocks (forward: [s.T1; s.T0], transposed: [T0; T1]).  Double-word
+// arithmetic on the FP32 pipes when sinv2 is given, DFMA otherwise.
+struct CapApplyArgs {
+  const double *Tb; long long tb_stride;
+  const double *scale;
+  const double *sinv; const float2 *sinv2;
+  double *eta;
+  int r, C, nnode, node_base;
+  bool trans;
+  const int *skip;
+};
+cudaError_t launch_cap_apply(const CapApplyArgs &a, cudaStream_t s);
+
 // --------------------------------------------------------------- helpers
 // Y[i, j] = (T) X[i, j] for an n x c column-major tile.
 template <typename Tin, typename Tout>
