@@ -41,4 +41,20 @@ void debug_after_launch(const char *name, cudaStream_t s);
 
 inline int ceil_div(long long a, long long b) { return (int)((a + b - 1) / b); }
 
+// Launch shape of an n x c column-major elementwise pass: blockIdx.y strides
+// over columns, x over rows (no 64-bit index division in the kernels).
+inline dim3 grid2d(long long n, int c) {
+  const int y = c < 1 ? 1 : (c > 65535 ? 65535 : c);
+  long long x = (n + 255) / 256;
+  const long long cap = 4864 / y > 0 ? 4864 / y : 1;
+  if (x > cap) x = cap;
+  if (x < 1) x = 1;
+  return dim3((unsigned)x, (unsigned)y);
+}
+
+#define HODLR_FOR_2D(i, j, n, c)                                                     \
+  for (long long j = blockIdx.y; j < (long long)(c); j += gridDim.y)                \
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < (n);    \
+         i += (long long)gridDim.x * blockDim.x)
+
 }  // namespace hodlr

@@ -90,6 +90,48 @@ __device__ void block_getrf(T *A, int lda, int m, int *piv, int *info) {
   __syncthreads();
 }
 
+// In-place inverse from the LU factors and pivots of block_getrf, in the
+// order of LAPACK DGETRI's unblocked path: inv(U) column by column (DTRTI2),
+// then inv(A) inv(L)... solved right to left, then the column interchanges
+// undone in reverse.  work: n scratch entries (shared memory).
+template <typename T>
+__device__ void block_getri(T *A, int lda, int n, const int *piv, T *work) {
+  const int tid = threadIdx.x, nt = blockDim.x;
+  auto a = [&](int i, int j) -> T & { return A[i + (long long)j * lda]; };
+  // 1. inv(U): A[0:j, j] = -inv(U)[j,j] * inv(U)[0:j,0:j] * A[0:j, j]
+  for (int j = 0; j < n; ++j) {
+    for (int i = tid; i < j; i += nt) work[i] = a(i, j);
+    __syncthreads();
+    const T dj = T(1) / a(j, j);
+    for (int i = tid; i < j; i += nt) {
+      T acc = T(0);
+      for (int k = i; k < j; ++k) acc += a(i, k) * work[k];
+      a(i, j) = -dj * acc;
+    }
+    __syncthreads();
+    if (tid == 0) a(j, j) = dj;
+    __syncthreads();
+  }
+  // 2. solve X L = inv(U) for X, columns n-2 .. 0
+  for (int j = n - 2; j >= 0; --j) {
+    for (int i = j + 1 + tid; i < n; i += nt) work[i] = a(i, j);
+    __syncthreads();
+    for (int i = tid; i < n; i += nt) {
+      T acc = (i > j) ? T(0) : a(i, j);
+      for (int k = j + 1; k < n; ++k) acc -= a(i, k) * work[k];
+      a(i, j) = acc;
+    }
+    __syncthreads();
+  }
+  // 3. undo the row interchanges of P as column interchanges, in reverse
+  for (int i = tid; i < n; i += nt)
+    for (int j = n - 2; j >= 0; --j) {
+      const int jp = piv[j] - 1;
+      if (jp != j) swap_vals(a(i, j), a(i, jp));
+    }
+  __syncthreads();
+}
+
 // Row interchanges of a column tile, in LAPACK DLASWP order (forward) or
 // reversed (backward).
 template <typename T>

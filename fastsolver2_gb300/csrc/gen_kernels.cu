@@ -31,12 +31,7 @@ __device__ __forceinline__ double gauss(unsigned long long seed, unsigned long l
 
 __global__ void gaussian_kernel(double *X, long long ld, long long n, int c, unsigned long long seed,
                                 unsigned long long stream, double scale) {
-  const long long total = n * c;
-  for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < total;
-       e += (long long)gridDim.x * blockDim.x) {
-    const long long i = e % n, j = e / n;
-    X[i + j * ld] = scale * gauss(seed, stream, (unsigned long long)e);
-  }
+  HODLR_FOR_2D(i, j, n, c) X[i + j * ld] = scale * gauss(seed, stream, (unsigned long long)(i + j * n));
 }
 
 cudaError_t launch_gaussian(double *X, long long ld, long long n, int c, unsigned long long seed,

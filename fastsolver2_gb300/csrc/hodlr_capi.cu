@@ -384,9 +384,11 @@ template <typename T> static int factor_sweep(hodlr_ctx *h) {
   T *LU = LUptr<T>(h);
   T *Ut = Utptr<T>(h);
   const T *Vt = Vptr<T>(h);
-  PHASE(h, HODLR_PHASE_LEAF_LU, launch_leaf_getrf<T>(h->D, m, (long long)m * m, LU, h->ipiv, m, h->nleaf, h->dst, s));
-  if (Dinvptr<T>(h))
-    PHASE(h, HODLR_PHASE_LEAF_LU, launch_leaf_inverse<T>(LU, h->ipiv, m, h->nleaf, Dinvptr<T>(h), s));
+  T *Dinv = Dinvptr<T>(h);
+  const bool fused = Dinv && leaf_getrf_fused_inverse(m, sizeof(T));
+  PHASE(h, HODLR_PHASE_LEAF_LU,
+        launch_leaf_getrf<T>(h->D, m, (long long)m * m, LU, h->ipiv, m, h->nleaf, h->dst, fused ? Dinv : nullptr, s));
+  if (Dinv && !fused) PHASE(h, HODLR_PHASE_LEAF_LU, launch_leaf_inverse<T>(LU, h->ipiv, m, h->nleaf, Dinv, s));
   if (L == 0) return HODLR_OK;
   if (sizeof(T) == 8)
     CK(cudaMemcpyAsync(Ut, h->U, sizeof(double) * n * L * r, cudaMemcpyDeviceToDevice, s));

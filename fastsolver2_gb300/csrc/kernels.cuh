@@ -10,9 +10,12 @@ namespace hodlr {
 // D + i*d_stride (FP64, column-major, ld d_ld).  LU: packed [nleaf][m][m]
 // of type T.  ipiv: [nleaf][m], 1-based.  Zero pivots / non-finite entries
 // are reported in *st.
+// Dinv (may be NULL): also write the explicit inverses, formed from the
+// factors while they are still in shared memory (leaf_getrf_fused_inverse).
+bool leaf_getrf_fused_inverse(int m, int elem_bytes);
 template <typename T>
 cudaError_t launch_leaf_getrf(const double *D, long long d_ld, long long d_stride, T *LU, int *ipiv,
-                              int m, int nleaf, DevStatus *st, cudaStream_t s);
+                              int m, int nleaf, DevStatus *st, T *Dinv, cudaStream_t s);
 
 // K2: X := D_i^{-1} X (or D_i^{-T} X) on the rows of every leaf i for the
 // columns [0, ncols) of X (ld ldx).  skip (device flag, may be NULL): when

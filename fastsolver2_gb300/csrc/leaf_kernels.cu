@@ -15,7 +15,7 @@ namespace hodlr {
 template <typename T, bool SMEM>
 __global__ void __launch_bounds__(256)
 leaf_getrf_kernel(const double *__restrict__ D, long long d_ld, long long d_stride, T *LU, int *ipiv,
-                  int m, DevStatus *st) {
+                  int m, DevStatus *st, T *Dinv) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ int s_bad;
   __shared__ int s_info;
@@ -40,8 +40,14 @@ leaf_getrf_kernel(const double *__restrict__ D, long long d_ld, long long d_stri
   }
   block_getrf<T>(A, m, m, ipiv + (long long)leaf * m, &s_info);
   if (s_info && threadIdx.x == 0) report_error(st, HODLR_ERR_SINGULAR_LEAF, leaf);
-  if (SMEM)
+  if (SMEM) {
     for (int e = threadIdx.x; e < m * m; e += blockDim.x) LUg[e] = A[e];
+    if (Dinv) {  // explicit inverse from the factors still in shared memory
+      block_getri<T>(A, m, m, ipiv + (long long)leaf * m, A + (size_t)m * m);
+      T *out = Dinv + (long long)leaf * m * m;
+      for (int e = threadIdx.x; e < m * m; e += blockDim.x) out[e] = A[e];
+    }
+  }
 }
 
 template <typename T, bool TRANS, bool LU_SMEM>
@@ -81,17 +87,23 @@ static cudaError_t set_smem(K kernel, size_t bytes) {
   return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
 }
 
+bool leaf_getrf_fused_inverse(int m, int elem_bytes) {
+  return (size_t)m * (m + 1) * elem_bytes <= kSmemCap;
+}
+
 template <typename T>
 cudaError_t launch_leaf_getrf(const double *D, long long d_ld, long long d_stride, T *LU, int *ipiv,
-                              int m, int nleaf, DevStatus *st, cudaStream_t s) {
-  const size_t bytes = (size_t)m * m * sizeof(T);
+                              int m, int nleaf, DevStatus *st, T *Dinv, cudaStream_t s) {
+  const size_t bytes = (size_t)m * (m + 1) * sizeof(T);
   if (bytes <= kSmemCap) {
     auto k = leaf_getrf_kernel<T, true>;
     cudaError_t e = set_smem(k, bytes);
     if (e != cudaSuccess) return e;
-    HODLR_LAUNCH(k, nleaf, 256, bytes, s, D, d_ld, d_stride, LU, ipiv, m, st);
+    HODLR_LAUNCH(k, nleaf, 256, bytes, s, D, d_ld, d_stride, LU, ipiv, m, st, Dinv);
   } else {
-    HODLR_LAUNCH((leaf_getrf_kernel<T, false>), nleaf, 256, 0, s, D, d_ld, d_stride, LU, ipiv, m, st);
+    if (Dinv) return cudaErrorInvalidValue;  // caller forms the inverse separately
+    HODLR_LAUNCH((leaf_getrf_kernel<T, false>), nleaf, 256, 0, s, D, d_ld, d_stride, LU, ipiv, m, st,
+                 (T *)nullptr);
   }
   return cudaGetLastError();
 }
@@ -130,9 +142,9 @@ cudaError_t launch_leaf_getrs(const T *LU, const int *ipiv, int m, int nleaf, T 
 }
 
 template cudaError_t launch_leaf_getrf<double>(const double *, long long, long long, double *, int *, int,
-                                               int, DevStatus *, cudaStream_t);
+                                               int, DevStatus *, double *, cudaStream_t);
 template cudaError_t launch_leaf_getrf<float>(const double *, long long, long long, float *, int *, int,
-                                              int, DevStatus *, cudaStream_t);
+                                              int, DevStatus *, float *, cudaStream_t);
 template cudaError_t launch_leaf_getrs<double>(const double *, const int *, int, int, double *, long long,
                                                int, bool, const int *, cudaStream_t);
 template cudaError_t launch_leaf_getrs<float>(const float *, const int *, int, int, float *, long long, int,

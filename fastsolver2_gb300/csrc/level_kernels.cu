@@ -300,12 +300,7 @@ cudaError_t launch_capacitance(const CapArgs &a, cudaStream_t s) {
 // --------------------------------------------------------------- helpers
 template <typename Tin, typename Tout>
 __global__ void convert_kernel(const Tin *X, long long ldx, Tout *Y, long long ldy, long long n, int c) {
-  const long long total = n * c;
-  for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < total;
-       e += (long long)gridDim.x * blockDim.x) {
-    const long long i = e % n, j = e / n;
-    Y[i + j * ldy] = (Tout)X[i + j * ldx];
-  }
+  HODLR_FOR_2D(i, j, n, c) Y[i + j * ldy] = (Tout)X[i + j * ldx];
 }
 
 static int grid_for(long long total) {
@@ -316,7 +311,7 @@ template <typename Tin, typename Tout>
 cudaError_t launch_convert(const Tin *X, long long ldx, Tout *Y, long long ldy, long long n, int c,
                            cudaStream_t s) {
   if (n * c == 0) return cudaSuccess;
-  HODLR_LAUNCH((convert_kernel<Tin, Tout>), grid_for(n * c), 256, 0, s, X, ldx, Y, ldy, n, c);
+  HODLR_LAUNCH((convert_kernel<Tin, Tout>), grid2d(n, c), 256, 0, s, X, ldx, Y, ldy, n, c);
   return cudaGetLastError();
 }
 template cudaError_t launch_convert<double, float>(const double *, long long, float *, long long, long long,
@@ -371,10 +366,7 @@ template cudaError_t launch_unpack_leaves<float>(const float *, double *, long l
 __global__ void axpy_kernel(const double *X, long long ldx, double *Y, long long ldy, long long n, int c,
                             double alpha, int accumulate, const int *skip) {
   if (skip && *skip) return;
-  const long long total = n * c;
-  for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < total;
-       e += (long long)gridDim.x * blockDim.x) {
-    const long long i = e % n, j = e / n;
+  HODLR_FOR_2D(i, j, n, c) {
     const double v = X[i + j * ldx];
     double *y = Y + i + j * ldy;
     *y = accumulate ? *y + alpha * v : alpha * v;
@@ -384,7 +376,7 @@ __global__ void axpy_kernel(const double *X, long long ldx, double *Y, long long
 cudaError_t launch_axpy(const double *X, long long ldx, double *Y, long long ldy, long long n, int c,
                         double alpha, bool accumulate, const int *skip, cudaStream_t s) {
   if (n * c == 0) return cudaSuccess;
-  HODLR_LAUNCH(axpy_kernel, grid_for(n * c), 256, 0, s, X, ldx, Y, ldy, n, c, alpha, (int)accumulate, skip);
+  HODLR_LAUNCH(axpy_kernel, grid2d(n, c), 256, 0, s, X, ldx, Y, ldy, n, c, alpha, (int)accumulate, skip);
   return cudaGetLastError();
 }
 
@@ -392,19 +384,14 @@ template <typename Td>
 __global__ void add_corr_kernel(const double *X, long long ldx, const Td *D, long long ldd, double *Y,
                                 long long ldy, long long n, int c, const int *skip) {
   if (skip && *skip) return;
-  const long long total = n * c;
-  for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < total;
-       e += (long long)gridDim.x * blockDim.x) {
-    const long long i = e % n, j = e / n;
-    Y[i + j * ldy] = X[i + j * ldx] + (double)D[i + j * ldd];
-  }
+  HODLR_FOR_2D(i, j, n, c) Y[i + j * ldy] = X[i + j * ldx] + (double)D[i + j * ldd];
 }
 
 template <typename Td>
 cudaError_t launch_add_correction(const double *X, long long ldx, const Td *D, long long ldd, double *Y,
                                   long long ldy, long long n, int c, const int *skip, cudaStream_t s) {
   if (n * c == 0) return cudaSuccess;
-  HODLR_LAUNCH(add_corr_kernel<Td>, grid_for(n * c), 256, 0, s, X, ldx, D, ldd, Y, ldy, n, c, skip);
+  HODLR_LAUNCH(add_corr_kernel<Td>, grid2d(n, c), 256, 0, s, X, ldx, D, ldd, Y, ldy, n, c, skip);
   return cudaGetLastError();
 }
 template cudaError_t launch_add_correction<float>(const double *, long long, const float *, long long, double *,
@@ -477,10 +464,7 @@ cudaError_t launch_refine_check(const double *rnorm, const double *bnorm, int c,
 }
 
 __global__ void check_finite_kernel(const double *X, long long ldx, long long n, int c, DevStatus *st) {
-  const long long total = n * c;
-  for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < total;
-       e += (long long)gridDim.x * blockDim.x) {
-    const long long i = e % n, j = e / n;
+  HODLR_FOR_2D(i, j, n, c) {
     if (!isfinite(X[i + j * ldx])) report_error(st, HODLR_ERR_NONFINITE_INPUT, i);
   }
 }
@@ -488,7 +472,7 @@ __global__ void check_finite_kernel(const double *X, long long ldx, long long n,
 cudaError_t launch_check_finite(const double *X, long long ldx, long long n, int c, DevStatus *st,
                                 cudaStream_t s) {
   if (n * c == 0) return cudaSuccess;
-  HODLR_LAUNCH(check_finite_kernel, grid_for(n * c), 256, 0, s, X, ldx, n, c, st);
+  HODLR_LAUNCH(check_finite_kernel, grid2d(n, c), 256, 0, s, X, ldx, n, c, st);
   return cudaGetLastError();
 }
 

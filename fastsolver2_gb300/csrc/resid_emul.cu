@@ -74,21 +74,13 @@ __device__ __forceinline__ float2 dw_sub(float2 c, float sh, float sl) {
 __global__ void split_kernel(const double *X, long long ldx, float2 *Y, long long ldy, long long n, int c,
                              const int *skip) {
   if (skip && *skip) return;
-  const long long total = n * c;
-  for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < total;
-       e += (long long)gridDim.x * blockDim.x) {
-    const long long i = e % n, j = e / n;
-    Y[i + j * ldy] = split_d(X[i + j * ldx]);
-  }
+  HODLR_FOR_2D(i, j, n, c) Y[i + j * ldy] = split_d(X[i + j * ldx]);
 }
 
 __global__ void merge_kernel(const float2 *Y, long long ldy, double *X, long long ldx, long long n, int c,
                              const int *skip) {
   if (skip && *skip) return;
-  const long long total = n * c;
-  for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < total;
-       e += (long long)gridDim.x * blockDim.x) {
-    const long long i = e % n, j = e / n;
+  HODLR_FOR_2D(i, j, n, c) {
     const float2 v = Y[i + j * ldy];
     X[i + j * ldx] = (double)v.x + (double)v.y;
   }
@@ -101,14 +93,14 @@ static int grid_for(long long total) {
 cudaError_t launch_split(const double *X, long long ldx, float2 *Y, long long ldy, long long n, int c,
                          const int *skip, cudaStream_t s) {
   if (n * c == 0) return cudaSuccess;
-  HODLR_LAUNCH(split_kernel, grid_for(n * c), 256, 0, s, X, ldx, Y, ldy, n, c, skip);
+  HODLR_LAUNCH(split_kernel, grid2d(n, c), 256, 0, s, X, ldx, Y, ldy, n, c, skip);
   return cudaGetLastError();
 }
 
 cudaError_t launch_merge(const float2 *Y, long long ldy, double *X, long long ldx, long long n, int c,
                          const int *skip, cudaStream_t s) {
   if (n * c == 0) return cudaSuccess;
-  HODLR_LAUNCH(merge_kernel, grid_for(n * c), 256, 0, s, Y, ldy, X, ldx, n, c, skip);
+  HODLR_LAUNCH(merge_kernel, grid2d(n, c), 256, 0, s, Y, ldy, X, ldx, n, c, skip);
   return cudaGetLastError();
 }
 
