@@ -198,24 +198,25 @@ __global__ void __launch_bounds__(256) cap_factor_kernel(CapFactorArgs a) {
   double *gS = a.cap_lu + (long long)node * n2 * n2;
   for (int e = threadIdx.x; e < n2 * n2; e += blockDim.x) gS[e] = S[e];
   for (int e = threadIdx.x; e < n2; e += blockDim.x) a.cap_ipiv[(long long)node * n2 + e] = piv[e];
+  // explicit inverse: Gauss-Jordan on a fresh copy of S
+  __syncthreads();
+  for (int e = threadIdx.x; e < n2 * n2; e += blockDim.x) {
+    const int i = e % n2, j = e / n2;
+    double v = (i == j) ? 1.0 : 0.0;
+    if (i >= r && j < r) v = (a.scale ? a.scale[i - r] : 1.0) * T0[(i - r) + (long long)(a.ucol + j) * r];
+    if (i < r && j >= r) v = (a.scale ? a.scale[i] : 1.0) * T1[i + (long long)(a.ucol + j - r) * r];
+    S[e] = v;
+  }
+  __syncthreads();
+  block_gj_inverse<double>(S, n2, n2, W, piv, &s_info);
   double *gI = a.sinv + (long long)node * n2 * n2;
   float2 *gI2 = a.sinv2 ? a.sinv2 + (long long)node * n2 * n2 : nullptr;
-  for (int c0 = 0; c0 < n2; c0 += 32) {
-    const int nc = min(32, n2 - c0);
-    for (int e = threadIdx.x; e < n2 * nc; e += blockDim.x) {
-      const int i = e % n2, j = e / n2;
-      W[e] = (i == c0 + j) ? 1.0 : 0.0;
+  for (int e = threadIdx.x; e < n2 * n2; e += blockDim.x) {
+    gI[e] = S[e];
+    if (gI2) {
+      const float h = __double2float_rn(S[e]);
+      gI2[e] = make_float2(h, __double2float_rn(S[e] - (double)h));
     }
-    __syncthreads();
-    block_getrs<double, false>(S, n2, piv, n2, W, n2, nc);
-    for (int e = threadIdx.x; e < n2 * nc; e += blockDim.x) {
-      gI[(long long)c0 * n2 + e] = W[e];
-      if (gI2) {
-        const float h = __double2float_rn(W[e]);
-        gI2[(long long)c0 * n2 + e] = make_float2(h, __double2float_rn(W[e] - (double)h));
-      }
-    }
-    __syncthreads();
   }
 }
 

@@ -90,6 +90,81 @@ __device__ void block_getrf(T *A, int lda, int m, int *piv, int *info) {
   __syncthreads();
 }
 
+// In-place inverse of the n x n matrix A by Gauss-Jordan elimination with
+// the partial-pivoting rule of block_getrf (first row of maximal |a|; the
+// rows searched are the Schur complement rows, so the pivot sequence is the
+// LU's).  Every step is a full 2-D rank-1 update over the block, so all
+// threads stay busy: n^3 multiply-adds at 4 block barriers per column.
+// fcol: n scratch entries, perm: n ints (shared memory).  Returns the first
+// zero pivot (k+1) or 0 in *info.
+template <typename T>
+__device__ void block_gj_inverse(T *A, int lda, int n, T *fcol, int *perm, int *info) {
+  const int tid = threadIdx.x, nt = blockDim.x;
+  const int lane = tid & 31, warp = tid >> 5;
+  const int ti = tid & 31, tj = tid >> 5, ntj = nt >> 5;
+  __shared__ int s_p, s_info;
+  if (tid == 0) s_info = 0;
+  for (int k = 0; k < n; ++k) {
+    if (warp == 0) {
+      T best = T(-1);
+      int bi = -1;
+      for (int i = k + lane; i < n; i += 32) {
+        const T v = dabs(A[i + (long long)k * lda]);
+        if (v > best) {
+          best = v;
+          bi = i;
+        }
+      }
+#pragma unroll
+      for (int off = 16; off; off >>= 1) {
+        const T ob = __shfl_down_sync(0xffffffffu, best, off);
+        const int oi = __shfl_down_sync(0xffffffffu, bi, off);
+        if (oi >= 0 && (bi < 0 || ob > best || (ob == best && oi < bi))) {
+          best = ob;
+          bi = oi;
+        }
+      }
+      if (lane == 0) {
+        const int p = bi < 0 ? k : bi;
+        s_p = p;
+        perm[k] = p;
+        if (A[p + (long long)k * lda] == T(0) && s_info == 0) s_info = k + 1;
+      }
+    }
+    __syncthreads();
+    const int p = s_p;
+    if (p != k)
+      for (int j = tid; j < n; j += nt) swap_vals(A[k + (long long)j * lda], A[p + (long long)j * lda]);
+    __syncthreads();
+    const T akk = A[k + (long long)k * lda];
+    const T d = akk != T(0) ? T(1) / akk : T(0);
+    // scale row k (its diagonal becomes d) and save column k
+    for (int j = tid; j < n; j += nt) {
+      T *x = A + k + (long long)j * lda;
+      *x = (j == k) ? d : *x * d;
+    }
+    for (int i = tid; i < n; i += nt) fcol[i] = A[i + (long long)k * lda];
+    __syncthreads();
+    for (int j = tj; j < n; j += ntj) {
+      const T akj = A[k + (long long)j * lda];
+      T *Aj = A + (long long)j * lda;
+      for (int i = ti; i < n; i += 32) {
+        if (i == k) continue;
+        Aj[i] = (j == k) ? -fcol[i] * akj : Aj[i] - fcol[i] * akj;
+      }
+    }
+    __syncthreads();
+  }
+  // the row interchanges become column interchanges of the inverse, in reverse
+  for (int i = tid; i < n; i += nt)
+    for (int k = n - 1; k >= 0; --k) {
+      const int p = perm[k];
+      if (p != k) swap_vals(A[i + (long long)k * lda], A[i + (long long)p * lda]);
+    }
+  if (tid == 0) *info = s_info;
+  __syncthreads();
+}
+
 // In-place inverse from the LU factors and pivots of block_getrf, in the
 // order of LAPACK DGETRI's unblocked path: inv(U) column by column (DTRTI2),
 // then inv(A) inv(L)... solved right to left, then the column interchanges

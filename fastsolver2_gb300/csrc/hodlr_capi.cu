@@ -1225,4 +1225,170 @@ int hodlr_hsolve(int nrow, int nrhs, int rank, int nPart, int LD, double *K, dou
   return hodlr_hsolve_ex(nrow, nrhs, rank, nPart, LD, K, U, V, HODLR_PREC_FP64, nullptr, nullptr);
 }
 
+// ------------------------------------------------- reference-structured init
+int hodlr_set_uvd(hodlr_handle h, const double *U, int64_t ldu, const double *V, int64_t ldv, const double *Dg) {
+  if (!h || !U || !V || !Dg) return set_err(HODLR_ERR_INVALID_ARG, "null argument");
+  if (ldu < h->n || ldv < h->n) return set_err(HODLR_ERR_INVALID_ARG, "ld < n");
+  const long long n = h->n;
+  const int m = h->m, L = h->L, r = h->r;
+  cudaStream_t s = h->st;
+  if (L == 0) return set_err(HODLR_ERR_INVALID_ARG, "hodlr_set_uvd needs levels >= 1");
+  // level 0 holds the device copy of U / V; the other levels repeat it
+  CK(cudaMemcpy2DAsync(h->Ulev(0), sizeof(double) * n, U, sizeof(double) * ldu, sizeof(double) * n, r,
+                       cudaMemcpyDefault, s));
+  CK(cudaMemcpy2DAsync(h->Vlev(0), sizeof(double) * n, V, sizeof(double) * ldv, sizeof(double) * n, r,
+                       cudaMemcpyDefault, s));
+  for (int l = 1; l < L; ++l) {
+    CK(cudaMemcpyAsync(h->Ulev(l), h->Ulev(0), sizeof(double) * n * r, cudaMemcpyDeviceToDevice, s));
+    CK(cudaMemcpyAsync(h->Vlev(l), h->Vlev(0), sizeof(double) * n * r, cudaMemcpyDeviceToDevice, s));
+  }
+  CK(launch_fill(h->s, (long long)L * r, 1.0, s));
+  // leaf blocks K_i = U_i V_i^T + diag(D_i) (DenseBlockTask)
+  double *dD = nullptr;
+  CK(cudaMallocAsync(&dD, sizeof(double) * n, s));
+  CK(cudaMemcpyAsync(dD, Dg, sizeof(double) * n, cudaMemcpyDefault, s));
+  CK(cudaMemsetAsync(h->D, 0, sizeof(double) * h->nleaf * m * m, s));
+  UpdateArgs ua{};
+  ua.A = h->Ulev(0);
+  ua.lda = n;
+  ua.a_bstride = m;
+  ua.B = h->Vlev(0);
+  ua.ldb = n;
+  ua.b_s1 = 2LL * m;
+  ua.b_s2 = m;
+  ua.b_trans = 1;
+  ua.C = h->D;
+  ua.ldc = m;
+  ua.c_bstride = (long long)m * m;
+  ua.M = m;
+  ua.N = m;
+  ua.K = r;
+  ua.nbatch = h->nleaf;
+  ua.alpha = 1.0;
+  CK(launch_update_nn<double>(ua, s));
+  CK(launch_add_leaf_diag(h->D, dD, m, h->nleaf, s));
+  CK(cudaFreeAsync(dD, s));
+  for (int l = 0; l < L; ++l) h->has_level[l] = 1;
+  h->has_D = true;
+  h->factored = false;
+  CK(cudaStreamSynchronize(s));
+  return HODLR_OK;
+}
+
+}  // extern "C"
+
+// ------------------------------------------------------ component entry points
+// Short-lived device scratch for the component calls below.
+struct Scratch {
+  std::vector<void *> p;
+  ~Scratch() {
+    for (void *q : p) cudaFree(q);
+  }
+  template <typename T> T *get(size_t count) {
+    void *q = nullptr;
+    if (cudaMalloc(&q, sizeof(T) * (count ? count : 1)) != cudaSuccess) return nullptr;
+    p.push_back(q);
+    return static_cast<T *>(q);
+  }
+};
+
+extern "C" {
+
+int hodlr_gemm_reduce(int nrow, int nPart, int ncolV, int ncolU, const double *V, int64_t ldv, const double *U,
+                      int64_t ldu, double *W, int64_t ldw) {
+  if (!V || !U || !W || nPart < 1 || nrow % nPart || ncolV < 1 || ncolV > 64 || ncolU < 1 || ldv < nrow ||
+      ldu < nrow || ldw < (int64_t)nPart * ncolV)
+    return set_err(HODLR_ERR_INVALID_ARG, "gemm_reduce: bad arguments");
+  const long long rows = nrow / nPart;
+  Scratch sc;
+  double *out = sc.get<double>((size_t)nPart * ncolV * ncolU);
+  double *work = sc.get<double>(reduce_workspace_doubles(rows, nPart, ncolV, ncolU, 8));
+  if (!out || !work) return set_err(HODLR_ERR_OUT_OF_MEMORY, "gemm_reduce: scratch");
+  CK(launch_reduce_tn<double>(V, ldv, U, ldu, rows, nPart, ncolV, ncolU, out, work, nullptr, 0));
+  for (int p = 0; p < nPart; ++p)  // block p (ncolV x ncolU, ld ncolV) -> rows p*ncolV of W
+    CK(cudaMemcpy2DAsync(W + (long long)p * ncolV, sizeof(double) * ldw, out + (long long)p * ncolV * ncolU,
+                         sizeof(double) * ncolV, sizeof(double) * ncolV, ncolU, cudaMemcpyDeviceToDevice, 0));
+  CK(cudaStreamSynchronize(0));
+  return HODLR_OK;
+}
+
+int hodlr_gemm_broadcast(int nrow, int nPart, int nBlock, int K, int N, double alpha, const double *U, int64_t ldu,
+                         const double *Vb, int64_t ldvb, double beta, double *W, int64_t ldw) {
+  if (!U || !Vb || !W || nPart < 1 || nBlock < 1 || nPart % nBlock || nrow % nPart || K < 1 || N < 1 ||
+      ldu < nrow || ldw < nrow || ldvb < (int64_t)nBlock * K)
+    return set_err(HODLR_ERR_INVALID_ARG, "gemm_broadcast: bad arguments");
+  const long long rows = nrow / nPart;
+  const int per = nPart / nBlock;  // row partitions sharing one block of Vb
+  if (beta != 1.0) CK(launch_axpy(W, ldw, W, ldw, nrow, N, beta, false, nullptr, 0));
+  for (int blk = 0; blk < nBlock; ++blk) {
+    UpdateArgs ua{};
+    ua.A = U + (long long)blk * per * rows;
+    ua.lda = ldu;
+    ua.a_bstride = rows;
+    ua.B = Vb + (long long)blk * K;
+    ua.ldb = ldvb;
+    ua.C = W + (long long)blk * per * rows;
+    ua.ldc = ldw;
+    ua.c_bstride = rows;
+    ua.M = (int)rows;
+    ua.N = N;
+    ua.K = K;
+    ua.nbatch = per;
+    ua.alpha = alpha;
+    CK(launch_update_nn<double>(ua, 0));
+  }
+  CK(cudaStreamSynchronize(0));
+  return HODLR_OK;
+}
+
+int hodlr_node_solve(int nnode, int r, int nrhs, const double *VTu, int64_t ldu, double *VTd, int64_t ldd) {
+  if (!VTu || !VTd || nnode < 1 || r < 1 || r > 64 || nrhs < 1 || ldu < 2LL * r * nnode || ldd < 2LL * r * nnode)
+    return set_err(HODLR_ERR_INVALID_ARG, "node_solve: bad arguments");
+  const int ct = nrhs + r;
+  Scratch sc;
+  double *Tb = sc.get<double>((size_t)2 * nnode * r * ct);
+  double *lu = sc.get<double>((size_t)nnode * 4 * r * r);
+  double *inv = sc.get<double>((size_t)nnode * 4 * r * r);
+  double *eta = sc.get<double>((size_t)nnode * 2 * r * nrhs);
+  int *piv = sc.get<int>((size_t)nnode * 2 * r);
+  DevStatus *st = sc.get<DevStatus>(1);
+  if (!Tb || !lu || !inv || !eta || !piv || !st) return set_err(HODLR_ERR_OUT_OF_MEMORY, "node_solve: scratch");
+  CK(cudaMemsetAsync(st, 0, sizeof(DevStatus), 0));
+  // child c = 2p + h: T_c = [VTd rows | VTu rows] of half h of node p
+  for (int c = 0; c < 2 * nnode; ++c) {
+    double *T = Tb + (long long)c * r * ct;
+    CK(cudaMemcpy2DAsync(T, sizeof(double) * r, VTd + (long long)c * r, sizeof(double) * ldd, sizeof(double) * r,
+                         nrhs, cudaMemcpyDeviceToDevice, 0));
+    CK(cudaMemcpy2DAsync(T + (long long)nrhs * r, sizeof(double) * r, VTu + (long long)c * r, sizeof(double) * ldu,
+                         sizeof(double) * r, r, cudaMemcpyDeviceToDevice, 0));
+  }
+  CapFactorArgs cf{};
+  cf.Tb = Tb;
+  cf.tb_stride = (long long)r * ct;
+  cf.ucol = nrhs;
+  cf.cap_lu = lu;
+  cf.cap_ipiv = piv;
+  cf.sinv = inv;
+  cf.r = r;
+  cf.nnode = nnode;
+  cf.st = st;
+  CK(launch_cap_factor(cf, 0));
+  CapApplyArgs ca{};
+  ca.Tb = Tb;
+  ca.tb_stride = (long long)r * ct;
+  ca.sinv = inv;
+  ca.eta = eta;
+  ca.r = r;
+  ca.C = nrhs;
+  ca.nnode = nnode;
+  CK(launch_cap_apply(ca, 0));
+  for (int p = 0; p < nnode; ++p)  // eta_p (2r x nrhs, ld 2r) -> rows [2r p, 2r (p+1)) of VTd
+    CK(cudaMemcpy2DAsync(VTd + (long long)p * 2 * r, sizeof(double) * ldd, eta + (long long)p * 2 * r * nrhs,
+                         sizeof(double) * 2 * r, sizeof(double) * 2 * r, nrhs, cudaMemcpyDeviceToDevice, 0));
+  DevStatus hs{};
+  CK(cudaMemcpy(&hs, st, sizeof(DevStatus), cudaMemcpyDeviceToHost));
+  if (hs.code) return set_err(hs.code, "node_solve: singular capacitance system");
+  return HODLR_OK;
+}
+
 }  // extern "C"

@@ -54,26 +54,6 @@ struct UpdateArgs {
 template <typename T>
 cudaError_t launch_update_nn(const UpdateArgs &a, cudaStream_t s);
 
-// K4: capacitance systems of the nodes at one depth.
-//   T-blocks: Tb + c*tb_stride is child c's r x Ct block (ld r), Ct >= C + (factor ? r : 0).
-//   forward (trans = false):  S = [I, s.T1u; s.T0u, I], RHS = [s.T1d; s.T0d]
-//   transposed:               S^T z = [T0d; T1d]
-//   factor = true: S is built from the T-blocks' last r columns (columns
-//   C..C+r), factorised and stored in cap_lu[node] (2r x 2r, ld 2r) /
-//   cap_ipiv[node]; otherwise the stored factors are used.  The solution
-//   (2r x C per node, ld 2r) is written to eta + node*2r*C.
-struct CapArgs {
-  const double *Tb; long long tb_stride;
-  const double *scale;   // r entries or NULL
-  double *cap_lu; int *cap_ipiv;
-  double *eta;
-  int r, C, nnode, node_base;  // node ids node_base + p
-  bool factor, trans;
-  DevStatus *st;
-  const int *skip;
-};
-cudaError_t launch_capacitance(const CapArgs &a, cudaStream_t s);
-
 // Explicit inverses of the leaf blocks from their LU factors ([nleaf][m][m]).
 template <typename T>
 cudaError_t launch_leaf_inverse(const T *LU, const int *ipiv, int m, int nleaf, T *Dinv, cudaStream_t s);
@@ -143,6 +123,8 @@ cudaError_t launch_refine_check(const double *rnorm, const double *bnorm, int c,
 cudaError_t launch_check_finite(const double *X, long long ldx, long long n, int c, DevStatus *st,
                                 cudaStream_t s);
 cudaError_t launch_fill(double *X, long long n, double v, cudaStream_t s);
+// D_i[j, j] += d[i*m + j] for the packed leaf blocks [nleaf][m][m].
+cudaError_t launch_add_leaf_diag(double *D, const double *d, int m, int nleaf, cudaStream_t s);
 
 // ds[j] = -sum_b sum_q W_b[j, q] * T_{b^1}[j, q] (blocks r x k, ld r), FP64.
 cudaError_t launch_scale_grad(const double *W, const double *T, int r, int k, int nbatch, double *ds,

@@ -42,8 +42,16 @@ leaf_getrf_kernel(const double *__restrict__ D, long long d_ld, long long d_stri
   if (s_info && threadIdx.x == 0) report_error(st, HODLR_ERR_SINGULAR_LEAF, leaf);
   if (SMEM) {
     for (int e = threadIdx.x; e < m * m; e += blockDim.x) LUg[e] = A[e];
-    if (Dinv) {  // explicit inverse from the factors still in shared memory
-      block_getri<T>(A, m, m, ipiv + (long long)leaf * m, A + (size_t)m * m);
+    if (Dinv) {  // explicit inverse: Gauss-Jordan on a fresh copy of the block
+      __syncthreads();
+      for (int e = threadIdx.x; e < m * m; e += blockDim.x) {
+        const int i = e % m, j = e / m;
+        A[e] = (T)Dg[i + (long long)j * d_ld];
+      }
+      __syncthreads();
+      T *fcol = A + (size_t)m * m;
+      int *perm = reinterpret_cast<int *>(fcol + m);
+      block_gj_inverse<T>(A, m, m, fcol, perm, &s_info);
       T *out = Dinv + (long long)leaf * m * m;
       for (int e = threadIdx.x; e < m * m; e += blockDim.x) out[e] = A[e];
     }
@@ -88,13 +96,13 @@ static cudaError_t set_smem(K kernel, size_t bytes) {
 }
 
 bool leaf_getrf_fused_inverse(int m, int elem_bytes) {
-  return (size_t)m * (m + 1) * elem_bytes <= kSmemCap;
+  return (size_t)m * (m + 1) * elem_bytes + (size_t)m * 4 <= kSmemCap;
 }
 
 template <typename T>
 cudaError_t launch_leaf_getrf(const double *D, long long d_ld, long long d_stride, T *LU, int *ipiv,
                               int m, int nleaf, DevStatus *st, T *Dinv, cudaStream_t s) {
-  const size_t bytes = (size_t)m * (m + 1) * sizeof(T);
+  const size_t bytes = (size_t)m * (m + 1) * sizeof(T) + (size_t)m * 4;
   if (bytes <= kSmemCap) {
     auto k = leaf_getrf_kernel<T, true>;
     cudaError_t e = set_smem(k, bytes);

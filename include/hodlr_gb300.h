@@ -142,6 +142,14 @@ HODLR_API int hodlr_set_leaf_blocks(hodlr_handle h, const double *D, int64_t ld,
 HODLR_API int hodlr_set_lowrank(hodlr_handle h, int level, const double *U, int64_t ldu,
                       const double *V, int64_t ldv, const double *s);
 
+/* The reference's HMatrix::init(U, V, D) (src/hmatrix.cc:22-47): A = U V^T +
+ * diag(D) in HODLR form -- every level gets the same U and V (N x r,
+ * leading dimensions ldu, ldv; VTree::level, src/tree.cc:189-197) and each
+ * leaf block is U_i V_i^T + diag(D_i) (DenseBlockTask,
+ * src/tasks/dense_block.cc:63-75).  D: N entries.  Host or device pointers. */
+HODLR_API int hodlr_set_uvd(hodlr_handle h, const double *U, int64_t ldu, const double *V, int64_t ldv,
+                            const double *D);
+
 /* Factorisation: leaf LUs, transformed bases Utilde^(l) = A_c^{-1} U^(l)_c and
  * the 2r x 2r capacitance LUs of every node -- the work hsolve redoes on
  * every call with U as extra right-hand sides (src/tasks/leaf_solve.cc:80-153,
@@ -176,6 +184,34 @@ HODLR_API int hodlr_adjoint(hodlr_handle h, const double *x, int64_t ldx,
  * position p is 2^l - 1 + p).  FP64 handles only. */
 HODLR_API int hodlr_get_factors(hodlr_handle h, double *leaf_lu, int32_t *leaf_ipiv,
                       double *utilde, double *cap_lu, int32_t *cap_ipiv);
+
+/* ------------------------------------------------- component entry points */
+/* LMatrix::gemmRed('t', 'n', 1.0, V, U, 0.0, W) over nPart row partitions
+ * (src/lmatrix.cc:713-761, GemmRedTask src/tasks/gemm_reduce.cc:33-83):
+ * W rows [p*ncolV, (p+1)*ncolV) = V_p^T U_p, V_p / U_p the rows
+ * [p*nrow/nPart, (p+1)*nrow/nPart) of V (nrow x ncolV) and U (nrow x ncolU).
+ * ncolV <= 64.  Device pointers, column-major. */
+HODLR_API int hodlr_gemm_reduce(int nrow, int nPart, int ncolV, int ncolU, const double *V, int64_t ldv,
+                                const double *U, int64_t ldu, double *W, int64_t ldw);
+
+/* LMatrix::gemmBro('n', 'n', alpha, U, Vb, beta, W) (src/lmatrix.cc:814-865,
+ * GemmBroTask src/tasks/gemm_broadcast.cc:33-83): the nrow rows of U and W
+ * split into nPart partitions, Vb into nBlock row blocks of K rows (nPart a
+ * multiple of nBlock); partition p uses block p / (nPart / nBlock):
+ * W_p = alpha U_p Vb_block + beta W_p.  Device pointers, column-major. */
+HODLR_API int hodlr_gemm_broadcast(int nrow, int nPart, int nBlock, int K, int N, double alpha, const double *U,
+                                   int64_t ldu, const double *Vb, int64_t ldvb, double beta, double *W,
+                                   int64_t ldw);
+
+/* LMatrix::node_solve / NodeSolveTask (src/lmatrix.cc:534-581,
+ * src/tasks/node_solve.cc:37-82) for nnode nodes: node p's rows
+ * [2r p, 2r (p+1)) of VTu hold [V0^T u0; V1^T u1] (2r x r) and of VTd
+ * [V0^T d0; V1^T d1] (2r x nrhs).  S = [I, V1^T u1; V0^T u0, I] is solved
+ * against the swapped right-hand side [V1^T d1; V0^T d0] and the solution
+ * (eta0; eta1) overwrites VTd.  FP64 LU with partial pivoting.  Device
+ * pointers, column-major. */
+HODLR_API int hodlr_node_solve(int nnode, int r, int nrhs, const double *VTu, int64_t ldu, double *VTd,
+                               int64_t ldd);
 
 /* Copy out the problem held by the handle (device or host destinations; any
  * may be NULL): leaf blocks in the layout of hodlr_set_leaf_blocks
