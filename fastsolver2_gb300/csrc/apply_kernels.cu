@@ -14,6 +14,7 @@
 
 #include "dense_ops.cuh"
 #include "kernels.cuh"
+#include "reg_factor.cuh"
 #include "resid_emul.cuh"
 
 namespace hodlr {
@@ -220,10 +221,54 @@ __global__ void __launch_bounds__(256) cap_factor_kernel(CapFactorArgs a) {
   }
 }
 
+// Same contract with the 2r x 2r system resident in registers (reg_factor.cuh)
+// for 2r in {32, 64, 128}.
+template <int N2>
+__global__ void __launch_bounds__(256, 1) cap_factor_reg_kernel(CapFactorArgs a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ int s_info;
+  double *buf = reinterpret_cast<double *>(smem_raw);
+  const int p = blockIdx.x, node = a.node_base + p;
+  constexpr int r = N2 / 2;
+  const double *T0 = a.Tb + (long long)(2 * p) * a.tb_stride;
+  const double *T1 = a.Tb + (long long)(2 * p + 1) * a.tb_stride;
+  auto load = [&](int i, int j) -> double {
+    double v = (i == j) ? 1.0 : 0.0;
+    if (i >= r && j < r) v = (a.scale ? a.scale[i - r] : 1.0) * T0[(i - r) + (long long)(a.ucol + j) * r];
+    if (i < r && j >= r) v = (a.scale ? a.scale[i] : 1.0) * T1[i + (long long)(a.ucol + j - r) * r];
+    return v;
+  };
+  double *gI = a.sinv + (long long)node * N2 * N2;
+  float2 *gI2 = a.sinv2 ? a.sinv2 + (long long)node * N2 * N2 : nullptr;
+  auto store = [&](int i, int j, double v) {
+    gI[i + j * N2] = v;
+    if (gI2) {
+      const float h = __double2float_rn(v);
+      gI2[i + j * N2] = make_float2(h, __double2float_rn(v - (double)h));
+    }
+  };
+  reg_factor<double, N2>(load, buf, a.cap_lu + (long long)node * N2 * N2, a.cap_ipiv + (long long)node * N2, store,
+                         true, &s_info);
+  if (s_info && threadIdx.x == 0) report_error(a.st, HODLR_ERR_SINGULAR_CAPACITANCE, node);
+}
+
+template <int N2>
+static cudaError_t launch_cap_reg(const CapFactorArgs &a, cudaStream_t s) {
+  const size_t bytes = (size_t)N2 * N2 * 8;
+  auto k = cap_factor_reg_kernel<N2>;
+  cudaError_t e = set_smem(k, bytes);
+  if (e != cudaSuccess) return e;
+  HODLR_LAUNCH(k, a.nnode, 256, bytes, s, a);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_cap_factor(const CapFactorArgs &a, cudaStream_t s) {
   if (a.nnode <= 0) return cudaSuccess;
   if (a.r < 1 || a.r > 64) return cudaErrorInvalidValue;
   const int n2 = 2 * a.r;
+  if (n2 == 32) return launch_cap_reg<32>(a, s);
+  if (n2 == 64) return launch_cap_reg<64>(a, s);
+  if (n2 == 128) return launch_cap_reg<128>(a, s);
   const size_t bytes = (size_t)n2 * n2 * 8 + (size_t)n2 * 32 * 8 + (size_t)n2 * 4 + 16;
   cudaError_t e = set_smem(cap_factor_kernel, bytes);
   if (e != cudaSuccess) return e;

@@ -14,8 +14,8 @@
 // summed by a deterministic second pass -- no atomics, so results are bitwise
 // reproducible run to run), across the four 64-thread groups of a CTA (summed
 // in shared memory in a fixed order), and along each thread's rows.  Each
-// thread keeps an (RT/8) x 8 register tile; operands are read from shared
-// memory as 16-byte vectors.
+// thread keeps an (RT/8) x 8 register tile; shared-memory rows are padded by
+// one element so the column-wise staging stores are bank-conflict free.
 #include <algorithm>
 
 #include "kernels.cuh"
@@ -36,8 +36,8 @@ reduce_tn_kernel(const T *__restrict__ A, long long lda, const T *__restrict__ X
   constexpr int RPT = RT / 8;           // ranks per thread (rows of the output)
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T *sA = reinterpret_cast<T *>(smem_raw);          // [kRedBK][RT]
-  T *sX = sA + kRedBK * RT;                         // [kRedBK][kRedBN]
-  T *sRed = sX + kRedBK * kRedBN;                   // [4][RT][kRedBN]
+  T *sX = sA + kRedBK * (RT + 1);                   // [kRedBK][kRedBN + 1]
+  T *sRed = sX + kRedBK * (kRedBN + 1);             // [4][RT][kRedBN]
   long long lin = blockIdx.x;
   const int ct = (int)(lin % nct);
   lin /= nct;
@@ -58,11 +58,11 @@ reduce_tn_kernel(const T *__restrict__ A, long long lda, const T *__restrict__ X
     const int ib = min(kRedBK, rows - i0);
     for (int e = tid; e < kRedBK * RT; e += 256) {
       const int i = e % kRedBK, q = e / kRedBK;
-      sA[i * RT + q] = (i < ib && q < r) ? Ab[i0 + i + (long long)q * lda] : T(0);
+      sA[i * (RT + 1) + q] = (i < ib && q < r) ? Ab[i0 + i + (long long)q * lda] : T(0);
     }
     for (int e = tid; e < kRedBK * kRedBN; e += 256) {
       const int i = e % kRedBK, j = e / kRedBK;
-      sX[i * kRedBN + j] = (i < ib && c0 + j < C) ? Xb[i0 + i + (long long)j * ldx] : T(0);
+      sX[i * (kRedBN + 1) + j] = (i < ib && c0 + j < C) ? Xb[i0 + i + (long long)j * ldx] : T(0);
     }
     __syncthreads();
 #pragma unroll 2
@@ -70,9 +70,9 @@ reduce_tn_kernel(const T *__restrict__ A, long long lda, const T *__restrict__ X
       const int i = ii * 4 + g;
       T av[RPT], xv[8];
 #pragma unroll
-      for (int a = 0; a < RPT; ++a) av[a] = sA[i * RT + tr * RPT + a];
+      for (int a = 0; a < RPT; ++a) av[a] = sA[i * (RT + 1) + tr * RPT + a];
 #pragma unroll
-      for (int c = 0; c < 8; ++c) xv[c] = sX[i * kRedBN + tc * 8 + c];
+      for (int c = 0; c < 8; ++c) xv[c] = sX[i * (kRedBN + 1) + tc * 8 + c];
 #pragma unroll
       for (int a = 0; a < RPT; ++a)
 #pragma unroll
@@ -84,7 +84,7 @@ reduce_tn_kernel(const T *__restrict__ A, long long lda, const T *__restrict__ X
 #pragma unroll
   for (int a = 0; a < RPT; ++a)
 #pragma unroll
-    for (int c = 0; c < 8; ++c) sRed[(g * RT + tr * RPT + a) * kRedBN + tc * 8 + c] = acc[a][c];
+    for (int c = 0; c < 8; ++c) sRed[(g * RT + tr * RPT + a) * (kRedBN + 1) + tc * 8 + c] = acc[a][c];
   __syncthreads();
   double *o = out + ((long long)b * nchunks + chunk) * r * C;
   for (int e = tid; e < RT * kRedBN; e += 256) {
@@ -92,7 +92,7 @@ reduce_tn_kernel(const T *__restrict__ A, long long lda, const T *__restrict__ X
     if (q >= r || c0 + j >= C) continue;
     double s = 0.0;
 #pragma unroll
-    for (int gg = 0; gg < 4; ++gg) s += (double)sRed[(gg * RT + q) * kRedBN + j];
+    for (int gg = 0; gg < 4; ++gg) s += (double)sRed[(gg * RT + q) * (kRedBN + 1) + j];
     o[q + (long long)(c0 + j) * r] = s;
   }
 }
@@ -130,7 +130,7 @@ template <typename T, int RT>
 static cudaError_t reduce_rt(const T *A, long long lda, const T *X, long long ldx, long long nrows, int nbatch,
                              int r, int C, int chunk_rows, int nchunks, int nct, double *dst, const int *skip,
                              cudaStream_t s) {
-  const size_t bytes = sizeof(T) * ((size_t)kRedBK * RT + (size_t)kRedBK * kRedBN + 4ull * RT * kRedBN);
+  const size_t bytes = sizeof(T) * ((size_t)kRedBK * (RT + 1) + (size_t)kRedBK * (kRedBN + 1) + 4ull * RT * (kRedBN + 1));
   auto k = reduce_tn_kernel<T, RT>;
   if (bytes > 48 * 1024) {
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
@@ -182,7 +182,7 @@ template <typename T>
 __global__ void __launch_bounds__(256) update_nn_kernel(UpdateArgs a, int nrt, int nct) {
   if (a.skip && *a.skip) return;
   __shared__ __align__(16) T sA[kUpdBK][kUpdBM];
-  __shared__ __align__(16) T sB[kUpdBK][kUpdBN];
+  __shared__ __align__(16) T sB[kUpdBK][kUpdBN + 1];  // +1: conflict-free column stores
   long long lin = blockIdx.x;
   const int rt = (int)(lin % nrt);
   lin /= nrt;

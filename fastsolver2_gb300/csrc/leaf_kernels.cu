@@ -9,6 +9,7 @@
 
 #include "dense_ops.cuh"
 #include "kernels.cuh"
+#include "reg_factor.cuh"
 
 namespace hodlr {
 
@@ -58,6 +59,36 @@ leaf_getrf_kernel(const double *__restrict__ D, long long d_ld, long long d_stri
   }
 }
 
+// Leaf LU (+ optional explicit inverse) with the block resident in registers
+// (reg_factor.cuh), for M in {32, 64, 128}.
+template <typename T, int M>
+__global__ void __launch_bounds__(256, 1)
+leaf_factor_reg_kernel(const double *__restrict__ D, long long d_ld, long long d_stride, T *LU, int *ipiv,
+                       DevStatus *st, T *Dinv) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ int s_bad, s_info;
+  T *buf = reinterpret_cast<T *>(smem_raw);
+  const int leaf = blockIdx.x;
+  const double *Dg = D + (long long)leaf * d_stride;
+  if (threadIdx.x == 0) s_bad = 0;
+  __syncthreads();
+  int bad = 0;
+  for (int e = threadIdx.x; e < M * M; e += blockDim.x)
+    if (!isfinite(Dg[(e % M) + (long long)(e / M) * d_ld])) bad = 1;
+  if (bad) atomicOr(&s_bad, 1);
+  __syncthreads();
+  if (s_bad) {
+    if (threadIdx.x == 0) report_error(st, HODLR_ERR_NONFINITE_INPUT, (long long)leaf * M);
+    return;
+  }
+  T *inv = Dinv ? Dinv + (long long)leaf * M * M : nullptr;
+  auto load = [&](int i, int j) -> T { return (T)Dg[i + (long long)j * d_ld]; };
+  auto store = [&](int i, int j, T v) { inv[i + j * M] = v; };
+  reg_factor<T, M>(load, buf, LU + (long long)leaf * M * M, ipiv + (long long)leaf * M, store, inv != nullptr,
+                   &s_info);
+  if (s_info && threadIdx.x == 0) report_error(st, HODLR_ERR_SINGULAR_LEAF, leaf);
+}
+
 template <typename T, bool TRANS, bool LU_SMEM>
 __global__ void __launch_bounds__(256)
 leaf_getrs_kernel(const T *__restrict__ LU, const int *__restrict__ ipiv, int m, T *X, long long ldx,
@@ -95,13 +126,29 @@ static cudaError_t set_smem(K kernel, size_t bytes) {
   return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
 }
 
+static bool reg_leaf(int m) { return m == 32 || m == 64 || m == 128; }
+
 bool leaf_getrf_fused_inverse(int m, int elem_bytes) {
-  return (size_t)m * (m + 1) * elem_bytes + (size_t)m * 4 <= kSmemCap;
+  return reg_leaf(m) || (size_t)m * (m + 1) * elem_bytes + (size_t)m * 4 <= kSmemCap;
+}
+
+template <typename T, int M>
+static cudaError_t launch_reg(const double *D, long long d_ld, long long d_stride, T *LU, int *ipiv, int nleaf,
+                              DevStatus *st, T *Dinv, cudaStream_t s) {
+  const size_t bytes = (size_t)M * M * sizeof(T);
+  auto k = leaf_factor_reg_kernel<T, M>;
+  cudaError_t e = set_smem(k, bytes);
+  if (e != cudaSuccess) return e;
+  HODLR_LAUNCH(k, nleaf, 256, bytes, s, D, d_ld, d_stride, LU, ipiv, st, Dinv);
+  return cudaGetLastError();
 }
 
 template <typename T>
 cudaError_t launch_leaf_getrf(const double *D, long long d_ld, long long d_stride, T *LU, int *ipiv,
                               int m, int nleaf, DevStatus *st, T *Dinv, cudaStream_t s) {
+  if (m == 32) return launch_reg<T, 32>(D, d_ld, d_stride, LU, ipiv, nleaf, st, Dinv, s);
+  if (m == 64) return launch_reg<T, 64>(D, d_ld, d_stride, LU, ipiv, nleaf, st, Dinv, s);
+  if (m == 128) return launch_reg<T, 128>(D, d_ld, d_stride, LU, ipiv, nleaf, st, Dinv, s);
   const size_t bytes = (size_t)m * (m + 1) * sizeof(T) + (size_t)m * 4;
   if (bytes <= kSmemCap) {
     auto k = leaf_getrf_kernel<T, true>;
