@@ -130,7 +130,13 @@ def colmajor(t):
 
 
 class Solver:
-    """Handle-based factor/solve API (hodlr_create ... hodlr_destroy)."""
+    """Handle-based factor/solve API (hodlr_create ... hodlr_destroy).
+
+    Without ``stream`` the library works on a non-blocking stream of its own:
+    tensors that torch kernels have just written must be finished
+    (``torch.cuda.synchronize()``) before they are passed in.  Every call that
+    returns results (factor, solve, matvec, adjoint, get_*) has finished its
+    device work when it returns."""
 
     def __init__(self, n, leaf, levels, rank, nrhs_max=1, precision=PREC_FP64, residual=RESID_FP64_EMULATED,
                  refine_tol=1e-12, refine_max_iter=10, stream=None):

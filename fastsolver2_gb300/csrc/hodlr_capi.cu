@@ -54,6 +54,10 @@ static int set_err(int code, const std::string &msg) {
   return code;
 }
 
+namespace hodlr {
+int set_last_error(int code, const char *msg) { return set_err(code, msg); }
+}  // namespace hodlr
+
 #define CK(expr)                                                                              \
   do {                                                                                        \
     cudaError_t e_ = (expr);                                                                  \
@@ -249,6 +253,7 @@ static void plan_sizes(hodlr_ctx *h) {
     red = std::max(red, reduce_workspace_doubles(rows, nb, r, (int)ct, 8));
     red = std::max(red, reduce_workspace_doubles(rows, nb, r, k, 8));
     red = std::max(red, reduce_workspace_doubles(rows, nb, r, r, 8));
+    red = std::max(red, dw_reduce_workspace_doubles(rows, nb, r, k));
   }
   h->tbuf_elems = tb;
   h->eta_elems = et;
@@ -633,6 +638,28 @@ static int mixed_solve(hodlr_ctx *h, double *B, long long ldb, int k, bool trans
   return HODLR_OK;
 }
 
+// Input-derived copies of the mixed path, made when the inputs are set (so a
+// factorisation only reads them): FP32 V for the sweeps and the double-word
+// splits of D, U, V for the emulated residual.
+static int prepare_leaves(hodlr_ctx *h) {
+  if (h->emulated) {
+    const long long dm = (long long)h->nleaf * h->m * h->m;
+    CK(launch_split(h->D, dm, h->D2, dm, dm, 1, nullptr, h->st));
+  }
+  return HODLR_OK;
+}
+
+static int prepare_level(hodlr_ctx *h, int l) {
+  if (!h->mixed) return HODLR_OK;
+  const long long n = h->n, off = (long long)l * n * h->r;
+  CK((launch_convert<double, float>(h->Vlev(l), n, h->V32 + off, n, n, h->r, h->st)));
+  if (h->emulated) {
+    CK(launch_split(h->Ulev(l), n, h->U2 + off, n, n, h->r, nullptr, h->st));
+    CK(launch_split(h->Vlev(l), n, h->V2 + off, n, n, h->r, nullptr, h->st));
+  }
+  return HODLR_OK;
+}
+
 // ----------------------------------------------------------------- C ABI
 extern "C" {
 
@@ -794,7 +821,7 @@ int hodlr_set_leaf_blocks(hodlr_handle h, const double *D, int64_t ld, int64_t l
   }
   h->has_D = true;
   h->factored = false;
-  return HODLR_OK;
+  return prepare_leaves(h);
 }
 
 int hodlr_set_lowrank(hodlr_handle h, int level, const double *U, int64_t ldu, const double *V, int64_t ldv,
@@ -813,7 +840,7 @@ int hodlr_set_lowrank(hodlr_handle h, int level, const double *U, int64_t ldu, c
     CK(launch_fill(h->slev(level), h->r, 1.0, h->st));
   h->has_level[level] = 1;
   h->factored = false;
-  return HODLR_OK;
+  return prepare_level(h, level);
 }
 
 int hodlr_factor(hodlr_handle h) {
@@ -825,20 +852,7 @@ int hodlr_factor(hodlr_handle h) {
   CKS(reset_status(h));
   CK(cudaEventRecord(h->ev[0], h->st));
   int rc = run_graphed(h, h->factor_graph, h->factor_runs, [&]() -> int {
-    if (h->mixed) {
-      const long long n = h->n, lr = (long long)h->L * h->r;
-      if (h->L > 0)
-        PHASE(h, HODLR_PHASE_MISC, (launch_convert<double, float>(h->V, n, h->V32, n, n, (int)lr, h->st)));
-      if (h->emulated) {
-        const long long dm = (long long)h->nleaf * h->m * h->m;
-        PHASE(h, HODLR_PHASE_MISC, launch_split(h->D, dm, h->D2, dm, dm, 1, nullptr, h->st));
-        if (h->L > 0) {
-          PHASE(h, HODLR_PHASE_MISC, launch_split(h->U, n, h->U2, n, n, (int)lr, nullptr, h->st));
-          PHASE(h, HODLR_PHASE_MISC, launch_split(h->V, n, h->V2, n, n, (int)lr, nullptr, h->st));
-        }
-      }
-      return factor_sweep<float>(h);
-    }
+    if (h->mixed) return factor_sweep<float>(h);
     return factor_sweep<double>(h);
   });
   CKS(rc);
@@ -1078,6 +1092,7 @@ int hodlr_generate(hodlr_handle h, uint64_t seed, double shift, int orthonormal,
   CKS(reset_status(h));
   CK(launch_gen_leaves(h->D, m, h->nleaf, seed, shift, s));
   h->has_D = true;
+  CKS(prepare_leaves(h));
   double *tmp = nullptr;
   if (orthonormal && L > 0) CK(cudaMallocAsync(&tmp, sizeof(double) * n * r, s));
   for (int l = 0; l < L; ++l) {
@@ -1118,6 +1133,7 @@ int hodlr_generate(hodlr_handle h, uint64_t seed, double shift, int orthonormal,
     CK(cudaMemcpyAsync(h->slev(l), sv.data(), sizeof(double) * r, cudaMemcpyHostToDevice, s));
     CK(cudaStreamSynchronize(s));  // sv is pageable host memory
     h->has_level[l] = 1;
+    CKS(prepare_level(h, l));
   }
   if (tmp) CK(cudaFreeAsync(tmp, s));
   if (B) CK(launch_gaussian(B, ldb, n, nrhs, seed, 0xBull, 1.0, s));
@@ -1268,8 +1284,12 @@ int hodlr_set_uvd(hodlr_handle h, const double *U, int64_t ldu, const double *V,
   CK(launch_update_nn<double>(ua, s));
   CK(launch_add_leaf_diag(h->D, dD, m, h->nleaf, s));
   CK(cudaFreeAsync(dD, s));
-  for (int l = 0; l < L; ++l) h->has_level[l] = 1;
+  for (int l = 0; l < L; ++l) {
+    h->has_level[l] = 1;
+    CKS(prepare_level(h, l));
+  }
   h->has_D = true;
+  CKS(prepare_leaves(h));
   h->factored = false;
   CK(cudaStreamSynchronize(s));
   return HODLR_OK;

@@ -5,6 +5,9 @@
 
 namespace hodlr {
 
+// Record the message returned by hodlr_last_error_string(); returns code.
+int set_last_error(int code, const char *msg);
+
 // ------------------------------------------------------------------ leaves
 // K1: LU with partial pivoting of every leaf block.  D: leaf i at
 // D + i*d_stride (FP64, column-major, ld d_ld).  LU: packed [nleaf][m][m]

@@ -215,21 +215,29 @@ cudaError_t launch_fill(double *X, long long n, double v, cudaStream_t s) {
   return cudaGetLastError();
 }
 
+// One CTA per rank index j; the batches are strided over the threads and the
+// partial sums combined in a fixed-order tree (deterministic).
 __global__ void scale_grad_kernel(const double *W, const double *T, int r, int k, int nbatch, double *ds) {
-  const int j = blockIdx.x * blockDim.x + threadIdx.x;
-  if (j >= r) return;
+  const int j = blockIdx.x;
   double acc = 0.0;
-  for (int b = 0; b < nbatch; ++b) {
+  for (int b = threadIdx.x; b < nbatch; b += blockDim.x) {
     const double *w = W + (long long)b * r * k;
     const double *t = T + (long long)(b ^ 1) * r * k;
     for (int q = 0; q < k; ++q) acc += w[j + (long long)q * r] * t[j + (long long)q * r];
   }
-  ds[j] = -acc;
+  __shared__ double red[256];
+  red[threadIdx.x] = acc;
+  __syncthreads();
+  for (int w = 128; w; w >>= 1) {
+    if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) ds[j] = -red[0];
 }
 
 cudaError_t launch_scale_grad(const double *W, const double *T, int r, int k, int nbatch, double *ds,
                               cudaStream_t s) {
-  HODLR_LAUNCH(scale_grad_kernel, ceil_div(r, 64), 64, 0, s, W, T, r, k, nbatch, ds);
+  HODLR_LAUNCH(scale_grad_kernel, r, 256, 0, s, W, T, r, k, nbatch, ds);
   return cudaGetLastError();
 }
 

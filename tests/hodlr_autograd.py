@@ -23,17 +23,20 @@ class HodlrSolve(torch.autograd.Function):
     def forward(ctx, b, D, U, V, s, leaf, precision=fs.PREC_FP64):
         L, N, r = U.shape
         k = b.shape[1]
-        torch.cuda.synchronize()  # the library works on its own stream
         solver = fs.Solver(N, leaf, L, r, nrhs_max=k, precision=precision)
         # leaf blocks: the library wants column-major m x m per leaf
         Dcm = D.transpose(1, 2).contiguous()          # memory = column-major blocks
-        solver.set_leaf_blocks(Dcm.reshape(-1), ld=leaf, leaf_stride=leaf * leaf)
         Ucm = [U[l].t().contiguous() for l in range(L)]   # (r, N) row-major = (N, r) column-major
         Vcm = [V[l].t().contiguous() for l in range(L)]
-        for l in range(L):
-            solver.set_lowrank(l, Ucm[l].t(), Vcm[l].t(), s[l].contiguous())
-        solver.factor()
         X = _colmajor_2d(b.detach().clone())
+        s = s.contiguous()
+        # the library works on its own non-blocking stream: the torch kernels
+        # that made its inputs must have finished before it reads them
+        torch.cuda.synchronize()
+        solver.set_leaf_blocks(Dcm.reshape(-1), ld=leaf, leaf_stride=leaf * leaf)
+        for l in range(L):
+            solver.set_lowrank(l, Ucm[l].t(), Vcm[l].t(), s[l])
+        solver.factor()
         solver.solve(X)
         ctx.solver = solver
         ctx.save_for_backward(X)
@@ -44,7 +47,6 @@ class HodlrSolve(torch.autograd.Function):
     def backward(ctx, gx):
         (X,) = ctx.saved_tensors
         L, N, r, leaf, k = ctx.shape
-        torch.cuda.synchronize()
         dev = X.device
         g = _colmajor_2d(gx.contiguous())
         db = torch.empty((k, N), dtype=torch.float64, device=dev).t()
@@ -52,6 +54,7 @@ class HodlrSolve(torch.autograd.Function):
         dU = torch.empty(L * N * r, dtype=torch.float64, device=dev)
         dV = torch.empty(L * N * r, dtype=torch.float64, device=dev)
         ds = torch.empty(L * r, dtype=torch.float64, device=dev)
+        torch.cuda.synchronize()   # g is made by torch kernels; the library reads it on its own stream
         ctx.solver.adjoint(X, g, db=db, dD=dD, dU=dU, dV=dV, ds=ds)
         nleaf = N // leaf
         dD = dD.reshape(nleaf, leaf, leaf).transpose(1, 2)   # back to D[i] row-major indexing

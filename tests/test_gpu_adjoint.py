@@ -50,16 +50,17 @@ def test_fd_and_cost_at_2_18(hodlr):
     m, L, r, k = 128, 11, 24, 1
     N = m << L
     b, D, U, V, s = _problem_tensors(N, m, L, r, k, seed=4)
-    params = [t.clone().requires_grad_() for t in (b, D, U, V, s)]
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    x = HodlrSolve.apply(*params, m)
-    torch.cuda.synchronize()
-    t1 = time.perf_counter()
-    loss = 0.5 * (x * x).sum()
-    loss.backward()
-    torch.cuda.synchronize()
-    t2 = time.perf_counter()
+    for _ in range(2):  # the second pass is timed (the first loads the kernels)
+        params = [t.clone().requires_grad_() for t in (b, D, U, V, s)]
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        x = HodlrSolve.apply(*params, m)
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        loss = 0.5 * (x * x).sum()
+        loss.backward()
+        torch.cuda.synchronize()
+        t2 = time.perf_counter()
     fwd, adj = t1 - t0, t2 - t1
     print("forward (factor+solve) %.1f ms, adjoint %.1f ms" % (1e3 * fwd, 1e3 * adj))
     assert adj <= 1.5 * fwd
