@@ -75,6 +75,7 @@ SIGNATURES = {
     "hodlr_get_inputs": (_I, [_VP, _VP, _I64, _I64, _VP, _VP, _VP]),
     "hodlr_set_uvd": (_I, [_VP, _VP, _I64, _VP, _I64, _VP]),
     "hodlr_gemm_reduce": (_I, [_I, _I, _I, _I, _VP, _I64, _VP, _I64, _VP, _I64]),
+    "hodlr_gemm_reduce_noalloc": (_I, [_I, _I, _I, _I, _VP, _I64, _VP, _I64, _VP, _I64]),
     "hodlr_gemm_broadcast": (_I, [_I, _I, _I, _I, _I, _D, _VP, _I64, _VP, _I64, _D, _VP, _I64]),
     "hodlr_node_solve": (_I, [_I, _I, _I, _VP, _I64, _VP, _I64]),
     "hodlr_generate": (_I, [_VP, ctypes.c_uint64, _D, _I, _D, _VP, _I64, _I]),

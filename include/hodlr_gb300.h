@@ -194,6 +194,20 @@ HODLR_API int hodlr_get_factors(hodlr_handle h, double *leaf_lu, int32_t *leaf_i
 HODLR_API int hodlr_gemm_reduce(int nrow, int nPart, int ncolV, int ncolU, const double *V, int64_t ldv,
                                 const double *U, int64_t ldu, double *W, int64_t ldw);
 
+/* hodlr_gemm_reduce for callers that may not allocate device memory (code
+ * running inside stream capture, frameworks that own the device through
+ * their own allocator, loops that cannot absorb cudaMalloc's
+ * synchronisation).  No counterpart in the reference.  Same arguments and
+ * result; its scratch is a fixed 16 MiB device array inside the library
+ * (2^21 doubles, held on every GPU that loads the library) instead of
+ * cudaMalloc.  nPart*ncolV*ncolU plus the split-K partial sums must fit that
+ * array, else HODLR_ERR_INVALID_ARG.  The first call on a device looks up the
+ * array's address (make it before any stream capture); calls that overlap
+ * on the GPU share the array and race.  Legacy default stream, returns when
+ * W is written. */
+HODLR_API int hodlr_gemm_reduce_noalloc(int nrow, int nPart, int ncolV, int ncolU, const double *V,
+                                        int64_t ldv, const double *U, int64_t ldu, double *W, int64_t ldw);
+
 /* LMatrix::gemmBro('n', 'n', alpha, U, Vb, beta, W) (src/lmatrix.cc:814-865,
  * GemmBroTask src/tasks/gemm_broadcast.cc:33-83): the nrow rows of U and W
  * split into nPart partitions, Vb into nBlock row blocks of K rows (nPart a
