@@ -56,6 +56,17 @@ class Grads(ctypes.Structure):
                 ("dU", ctypes.c_void_p), ("dV", ctypes.c_void_p), ("ds", ctypes.c_void_p)]
 
 
+class System(ctypes.Structure):
+    _fields_ = [("n", ctypes.c_int64), ("leaf", ctypes.c_int32), ("levels", ctypes.c_int32),
+                ("rank", ctypes.c_int32), ("nrhs", ctypes.c_int32)]
+
+
+class BatchDesc(ctypes.Structure):
+    _fields_ = [("systems", ctypes.POINTER(System)), ("count", ctypes.c_int32), ("precision", ctypes.c_int32),
+                ("residual", ctypes.c_int32), ("refine_tol", ctypes.c_double), ("refine_max_iter", ctypes.c_int32),
+                ("flags", ctypes.c_int32), ("stream", ctypes.c_void_p)]
+
+
 # name -> (restype, argtypes); the full exported surface of include/hodlr_gb300.h
 _VP, _I, _I64, _D = ctypes.c_void_p, ctypes.c_int, ctypes.c_int64, ctypes.c_double
 SIGNATURES = {
@@ -81,6 +92,14 @@ SIGNATURES = {
     "hodlr_generate": (_I, [_VP, ctypes.c_uint64, _D, _I, _D, _VP, _I64, _I]),
     "hodlr_profile": (_I, [_VP, _I, _VP, _VP, _I]),
     "hodlr_last_timings": (_I, [_VP, ctypes.POINTER(_D), ctypes.POINTER(_D)]),
+    "hodlr_batch_create": (_I, [ctypes.POINTER(BatchDesc), ctypes.POINTER(_VP)]),
+    "hodlr_batch_destroy": (_I, [_VP]),
+    "hodlr_batch_set_leaf_blocks": (_I, [_VP, _I, _VP, _I64, _I64]),
+    "hodlr_batch_set_lowrank": (_I, [_VP, _I, _I, _VP, _I64, _VP, _I64, _VP]),
+    "hodlr_batch_generate": (_I, [_VP, ctypes.c_uint64, _D, _VP, _VP]),
+    "hodlr_batch_factor": (_I, [_VP]),
+    "hodlr_batch_solve": (_I, [_VP, _VP, _VP, ctypes.POINTER(SolveInfo)]),
+    "hodlr_batch_stats": (_I, [_VP, ctypes.POINTER(_I), ctypes.POINTER(_D), ctypes.POINTER(_D)]),
     "hodlr_kernel_launches": (_I64, []),
     "hodlr_last_error_string": (ctypes.c_char_p, []),
 }
@@ -141,6 +160,7 @@ class Solver:
 
     def __init__(self, n, leaf, levels, rank, nrhs_max=1, precision=PREC_FP64, residual=RESID_FP64_EMULATED,
                  refine_tol=1e-12, refine_max_iter=10, stream=None):
+        self.h = None
         self.desc = Desc(n, leaf, levels, rank, nrhs_max, precision, residual, refine_tol, refine_max_iter, 0,
                          stream)
         h = ctypes.c_void_p()
@@ -210,6 +230,73 @@ class Solver:
         f, s = ctypes.c_double(), ctypes.c_double()
         check(lib().hodlr_last_timings(self.h, ctypes.byref(f), ctypes.byref(s)))
         return f.value, s.value
+
+
+class Batch:
+    """Ragged batch of independent systems (hodlr_batch_*).
+
+    systems: list of (n, leaf, levels, rank, nrhs).  Right-hand sides are
+    column-major float64 CUDA tensors, one per system.  As for Solver, torch
+    work that produced an input must be finished before it is passed in."""
+
+    def __init__(self, systems, precision=PREC_FP64, residual=RESID_FP64_EMULATED, refine_tol=1e-12,
+                 refine_max_iter=10, stream=None):
+        self.h = None
+        self.systems = [tuple(int(v) for v in s) for s in systems]
+        arr = (System * len(self.systems))(*[System(*s) for s in self.systems])
+        self._arr = arr
+        self.desc = BatchDesc(arr, len(self.systems), precision, residual, refine_tol, refine_max_iter, 0, stream)
+        h = ctypes.c_void_p()
+        check(lib().hodlr_batch_create(ctypes.byref(self.desc), ctypes.byref(h)))
+        self.h = h
+
+    def close(self):
+        if self.h:
+            lib().hodlr_batch_destroy(self.h)
+            self.h = None
+
+    __del__ = close
+
+    def __len__(self):
+        return len(self.systems)
+
+    @staticmethod
+    def _ptrs(Bs):
+        n = len(Bs)
+        ptrs = (ctypes.c_void_p * n)(*[b.data_ptr() if b is not None else None for b in Bs])
+        lds = (ctypes.c_int64 * n)(*[_ld(b) if b is not None else 0 for b in Bs])
+        return ptrs, lds
+
+    def set_leaf_blocks(self, i, D, ld=None, leaf_stride=None):
+        leaf = self.systems[i][1]
+        ld = _ld(D) if ld is None else ld
+        stride = leaf if leaf_stride is None else leaf_stride
+        check(lib().hodlr_batch_set_leaf_blocks(self.h, i, _ptr(D), ld, stride))
+
+    def set_lowrank(self, i, level, U, V, s=None):
+        check(lib().hodlr_batch_set_lowrank(self.h, i, level, _ptr(U), _ld(U), _ptr(V), _ld(V), _ptr(s)))
+
+    def generate(self, seed, shift=4.0, Bs=None):
+        if Bs is None:
+            check(lib().hodlr_batch_generate(self.h, seed, shift, None, None))
+        else:
+            ptrs, lds = self._ptrs(Bs)
+            check(lib().hodlr_batch_generate(self.h, seed, shift, ptrs, lds))
+
+    def factor(self):
+        check(lib().hodlr_batch_factor(self.h))
+
+    def solve(self, Bs):
+        """Solve in place; returns the per-system SolveInfo list."""
+        ptrs, lds = self._ptrs(Bs)
+        info = (SolveInfo * len(Bs))()
+        check(lib().hodlr_batch_solve(self.h, ptrs, lds, info))
+        return list(info)
+
+    def stats(self):
+        nf, f, s = ctypes.c_int(), ctypes.c_double(), ctypes.c_double()
+        check(lib().hodlr_batch_stats(self.h, ctypes.byref(nf), ctypes.byref(f), ctypes.byref(s)))
+        return nf.value, f.value, s.value
 
 
 def hsolve(nrow, nrhs, rank, nPart, LD, K, U, V, precision=PREC_FP64, stream=None):

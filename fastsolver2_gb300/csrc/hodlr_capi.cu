@@ -14,6 +14,7 @@
 // Level l's U/V/Ut block is the column range [l*r, (l+1)*r) of an n x L*r
 // matrix, i.e. the UTree column layout of the reference (src/tree.cc:61-73)
 // without the right-hand-side columns.
+#include <algorithm>
 #include <atomic>
 #include <cmath>
 #include <cstdio>
@@ -153,6 +154,27 @@ struct hodlr_ctx {
   double *Ulev(int l) const { return U + (long long)l * n * r; }
   double *Vlev(int l) const { return V + (long long)l * n * r; }
   double *slev(int l) const { return s + (long long)l * r; }
+
+  // Level geometry.  Level l = 0 .. L-1 counts from the root of the tallest
+  // tree.  One tree: 2^(l+1) child blocks of n / 2^(l+1) rows.  A forest (the
+  // systems of a ragged batch that share leaf size and rank, stacked in order
+  // of decreasing size) has, at level l, the child blocks of every tree tall
+  // enough to have that level: lev_nb[l] blocks of lev_rows[l] rows covering
+  // the first lev_nb[l] * lev_rows[l] rows; its nodes are numbered from
+  // lev_base[l].  Trees of different depth meet a level at the same height
+  // above the leaves, so their blocks there have the same size.
+  std::vector<int> lev_nb, lev_base;
+  std::vector<long long> lev_rows;
+  int nb(int l) const { return lev_nb[l]; }
+  long long rows(int l) const { return lev_rows[l]; }
+  int nodes(int l) const { return lev_nb[l] / 2; }
+  int node_base(int l) const { return lev_base[l]; }
+  // systems of a forest (one for a plain handle): leaf offsets, for the
+  // per-system residual norms of the refinement test
+  int nsys = 1;
+  int *seg_leaf = nullptr;  // device [nsys + 1]
+  bool forest = false;
+  double *sfold = nullptr;  // forest: device copy of one level's s, folded into V
 };
 
 static void clear_graphs(hodlr_ctx *h) {
@@ -237,19 +259,18 @@ static void free_ctx(hodlr_ctx *h) {
 
 // ----------------------------------------------------------------- sizes
 static void plan_sizes(hodlr_ctx *h) {
-  const long long n = h->n;
   const int L = h->L, r = h->r, k = h->kmax;
-  size_t tb = (size_t)1 << L;
-  tb = std::max(tb * r * std::max(k, r), (size_t)r * std::max(k, r));
-  size_t et = ((size_t)1 << L) * (size_t)r * r;
+  const size_t nbmax = L > 0 ? (size_t)h->nb(L - 1) : 1;
+  size_t tb = std::max(nbmax * r * std::max(k, r), (size_t)r * std::max(k, r));
+  size_t et = nbmax / 2 * 2 * (size_t)r * r;
   size_t red = 0;
   for (int l = 0; l < L; ++l) {
-    const int nb = 2 << l;
-    const long long rows = n >> (l + 1);
+    const int nb = h->nb(l);
+    const long long rows = h->rows(l);
     const size_t ct = (size_t)(l + 1) * r;
     tb = std::max(tb, (size_t)nb * r * ct);
-    et = std::max(et, ((size_t)1 << l) * 2 * r * (size_t)l * r);
-    et = std::max(et, ((size_t)1 << l) * 2 * r * (size_t)k);
+    et = std::max(et, (size_t)h->nodes(l) * 2 * r * (size_t)l * r);
+    et = std::max(et, (size_t)h->nodes(l) * 2 * r * (size_t)k);
     red = std::max(red, reduce_workspace_doubles(rows, nb, r, (int)ct, 8));
     red = std::max(red, reduce_workspace_doubles(rows, nb, r, k, 8));
     red = std::max(red, reduce_workspace_doubles(rows, nb, r, r, 8));
@@ -371,8 +392,8 @@ static int cap_apply(hodlr_ctx *h, int l, int C, long long tb_stride, bool trans
   ca.eta = h->eta;
   ca.r = h->r;
   ca.C = C;
-  ca.nnode = 1 << l;
-  ca.node_base = (1 << l) - 1;
+  ca.nnode = h->nodes(l);
+  ca.node_base = h->node_base(l);
   ca.trans = trans;
   ca.skip = skip;
   PHASE(h, HODLR_PHASE_CAPACITANCE, launch_cap_apply(ca, h->st));
@@ -402,8 +423,8 @@ template <typename T> static int factor_sweep(hodlr_ctx *h) {
           (launch_convert<double, float>(h->U, n, reinterpret_cast<float *>(Ut), n, n, L * r, s)));
   CKS(leaf_solve<T>(h, Ut, n, L * r, false, nullptr));
   for (int l = L - 1; l >= 0; --l) {
-    const int nb = 2 << l;
-    const long long rows = n >> (l + 1);
+    const int nb = h->nb(l);
+    const long long rows = h->rows(l);
     const int Cd = l * r, Ct = Cd + r;
     PHASE(h, HODLR_PHASE_REDUCE,
           launch_reduce_tn<T>(Vt + (long long)l * n * r, n, Ut, n, rows, nb, r, Ct, h->Tbuf, h->red, nullptr, s));
@@ -417,8 +438,8 @@ template <typename T> static int factor_sweep(hodlr_ctx *h) {
     cf.sinv = h->Sinv;
     cf.sinv2 = h->mixed ? h->Sinv2 : nullptr;
     cf.r = r;
-    cf.nnode = 1 << l;
-    cf.node_base = (1 << l) - 1;
+    cf.nnode = h->nodes(l);
+    cf.node_base = h->node_base(l);
     cf.st = h->dst;
     PHASE(h, HODLR_PHASE_CAPACITANCE, launch_cap_factor(cf, s));
     if (Cd > 0) {
@@ -456,8 +477,8 @@ static int solve_sweep(hodlr_ctx *h, T *X, long long ldx, int k, bool trans, con
   if (!trans) CKS(leaf_solve<T>(h, X, ldx, k, false, skip));
   for (int step = 0; step < L; ++step) {
     const int l = trans ? step : L - 1 - step;
-    const int nb = 2 << l;
-    const long long rows = n >> (l + 1);
+    const int nb = h->nb(l);
+    const long long rows = h->rows(l);
     const T *Ared = trans ? Ut + (long long)l * r * n : Vt + (long long)l * n * r;
     const T *Aupd = trans ? Vt + (long long)l * n * r : Ut + (long long)l * r * n;
     PHASE(h, HODLR_PHASE_REDUCE, launch_reduce_tn<T>(Ared, n, X, ldx, rows, nb, r, k, h->Tbuf, h->red, skip, s));
@@ -517,8 +538,8 @@ static int matvec_fp64(hodlr_ctx *h, bool trans, const double *X, long long ldx,
   la.skip = skip;
   PHASE(h, HODLR_PHASE_RESID_LEAF, launch_update_nn<double>(la, s));
   for (int l = 0; l < L; ++l) {
-    const int nb = 2 << l;
-    const long long rows = n >> (l + 1);
+    const int nb = h->nb(l);
+    const long long rows = h->rows(l);
     const double *Ared = trans ? h->Ulev(l) : h->Vlev(l);
     const double *Aupd = trans ? h->Vlev(l) : h->Ulev(l);
     PHASE(h, HODLR_PHASE_RESID_REDUCE, launch_reduce_tn<double>(Ared, n, X, ldx, rows, nb, r, k, h->Tbuf, h->red, skip, s));
@@ -574,8 +595,8 @@ static int residual_emulated(hodlr_ctx *h, bool trans, const double *X, long lon
   la.skip = skip;
   PHASE(h, HODLR_PHASE_RESID_LEAF, launch_dw_update(la, s));
   for (int l = 0; l < L; ++l) {
-    const int nb = 2 << l;
-    const long long rows = n >> (l + 1);
+    const int nb = h->nb(l);
+    const long long rows = h->rows(l);
     const float2 *U2l = h->U2 + (long long)l * n * r, *V2l = h->V2 + (long long)l * n * r;
     PHASE(h, HODLR_PHASE_RESID_REDUCE,
           launch_dw_reduce(trans ? U2l : V2l, n, h->X2, n, rows, nb, r, k, h->Tbuf, h->red, skip, s));
@@ -618,17 +639,22 @@ static int mixed_solve(hodlr_ctx *h, double *B, long long ldb, int k, bool trans
   const long long n = h->n;
   cudaStream_t s = h->st;
   const int *done = &h->dst->done;
-  double *bn = h->norms, *rn = h->norms + h->kmax;
+  double *bn = h->norms, *rn = h->norms + (size_t)h->kmax * h->nsys;
+  // column norms per system (a forest's refinement test is per system)
+  auto norms = [&](const double *X, double *out, const int *skip) {
+    if (!h->forest) return launch_colnorms(X, n, n, k, out, h->nwork, skip, s);
+    return launch_seg_colnorms(X, n, h->m, h->nleaf, k, h->seg_leaf, h->nsys, out, h->nwork, skip, s);
+  };
   CK(launch_axpy(B, ldb, h->B64, n, n, k, 1.0, false, nullptr, s));
-  CK(launch_colnorms(h->B64, n, n, k, bn, h->nwork, nullptr, s));
+  CK(norms(h->B64, bn, nullptr));
   CK((launch_convert<double, float>(h->B64, n, h->X32, n, n, k, s)));
   CKS(solve_sweep<float>(h, h->X32, n, k, trans, nullptr));
   CK((launch_convert<float, double>(h->X32, n, h->X64, n, n, k, s)));
   const int maxit = std::max(0, h->d.refine_max_iter);
   for (int it = 0; it <= maxit; ++it) {
     CKS(residual(h, trans, h->X64, n, h->B64, n, h->R64, n, k, done));
-    CK(launch_colnorms(h->R64, n, n, k, rn, h->nwork, done, s));
-    CK(launch_refine_check(rn, bn, k, h->d.refine_tol, h->dst, it < maxit ? 1 : 0, s));
+    CK(norms(h->R64, rn, done));
+    CK(launch_refine_check(rn, bn, k * h->nsys, h->d.refine_tol, h->dst, it < maxit ? 1 : 0, s));
     if (it == maxit) break;
     CK((launch_convert<double, float>(h->R64, n, h->X32, n, n, k, s)));
     CKS(solve_sweep<float>(h, h->X32, n, k, trans, done));
@@ -641,38 +667,52 @@ static int mixed_solve(hodlr_ctx *h, double *B, long long ldb, int k, bool trans
 // Input-derived copies of the mixed path, made when the inputs are set (so a
 // factorisation only reads them): FP32 V for the sweeps and the double-word
 // splits of D, U, V for the emulated residual.
-static int prepare_leaves(hodlr_ctx *h) {
-  if (h->emulated) {
-    const long long dm = (long long)h->nleaf * h->m * h->m;
-    CK(launch_split(h->D, dm, h->D2, dm, dm, 1, nullptr, h->st));
+static int prepare_leaves(hodlr_ctx *h, long long leaf0 = 0, long long count = -1) {
+  if (count < 0) count = h->nleaf;
+  if (h->emulated && count > 0) {
+    const long long mm = (long long)h->m * h->m, dm = count * mm;
+    CK(launch_split(h->D + leaf0 * mm, dm, h->D2 + leaf0 * mm, dm, dm, 1, nullptr, h->st));
   }
   return HODLR_OK;
 }
 
-static int prepare_level(hodlr_ctx *h, int l) {
+// Level l, rows [row0, row0 + count) (default: all rows).
+static int prepare_level(hodlr_ctx *h, int l, long long row0 = 0, long long count = -1) {
   if (!h->mixed) return HODLR_OK;
-  const long long n = h->n, off = (long long)l * n * h->r;
-  CK((launch_convert<double, float>(h->Vlev(l), n, h->V32 + off, n, n, h->r, h->st)));
+  const long long n = h->n, off = (long long)l * n * h->r + row0;
+  if (count < 0) count = n;
+  CK((launch_convert<double, float>(h->Vlev(l) + row0, n, h->V32 + off, n, count, h->r, h->st)));
   if (h->emulated) {
-    CK(launch_split(h->Ulev(l), n, h->U2 + off, n, n, h->r, nullptr, h->st));
-    CK(launch_split(h->Vlev(l), n, h->V2 + off, n, n, h->r, nullptr, h->st));
+    CK(launch_split(h->Ulev(l) + row0, n, h->U2 + off, n, count, h->r, nullptr, h->st));
+    CK(launch_split(h->Vlev(l) + row0, n, h->V2 + off, n, count, h->r, nullptr, h->st));
   }
   return HODLR_OK;
 }
 
-// ----------------------------------------------------------------- C ABI
-extern "C" {
+// Level geometry of one tree or of a forest (sys_levels: the trees' depths
+// in decreasing order, so that every tree starts on a row that is a multiple
+// of its own size and no block of a level straddles two trees).
+static void set_geometry(hodlr_ctx *h, const std::vector<int> &sys_levels) {
+  const int L = h->L;
+  h->lev_nb.assign(L, 0);
+  h->lev_rows.assign(L, 0);
+  h->lev_base.assign(L, 0);
+  int base = 0;
+  for (int l = 0; l < L; ++l) {
+    const int t = L - 1 - l;  // height above the leaves
+    const long long c = (long long)h->m << t;
+    long long covered = 0;
+    for (int Li : sys_levels)
+      if (Li > t) covered += (long long)h->m << Li;
+    h->lev_rows[l] = c;
+    h->lev_nb[l] = (int)(covered / c);
+    h->lev_base[l] = base;
+    base += h->lev_nb[l] / 2;
+  }
+  h->nnode = base;
+}
 
-const char *hodlr_last_error_string(void) { return g_err.c_str(); }
-
-int64_t hodlr_kernel_launches(void) { return (int64_t)g_launches.load(); }
-
-int hodlr_create(const hodlr_desc *desc, hodlr_handle *out) {
-  if (!desc || !out) return set_err(HODLR_ERR_INVALID_ARG, "null argument");
-  *out = nullptr;
-  const hodlr_desc &d = *desc;
-  if (d.leaf < 1 || d.levels < 0 || d.levels > 24 || d.n != ((int64_t)d.leaf << d.levels))
-    return set_err(HODLR_ERR_INVALID_ARG, "need n = leaf * 2^levels, leaf >= 1, 0 <= levels <= 24");
+static int check_common(const hodlr_desc &d) {
   if (d.levels > 0 && (d.rank < 1 || d.rank > 64))
     return set_err(HODLR_ERR_INVALID_ARG, "rank must be in [1, 64]");
   if (d.levels > 0 && (d.n >> d.levels) < 1) return set_err(HODLR_ERR_INVALID_ARG, "leaf too small");
@@ -682,17 +722,26 @@ int hodlr_create(const hodlr_desc *desc, hodlr_handle *out) {
   if (d.precision == HODLR_PREC_MIXED && !(d.refine_tol > 0.0))
     return set_err(HODLR_ERR_INVALID_ARG, "mixed mode needs refine_tol > 0");
   if ((long long)d.leaf * d.leaf * 8 > (1LL << 31)) return set_err(HODLR_ERR_INVALID_ARG, "leaf too large");
+  return HODLR_OK;
+}
+
+// Allocate a handle for one tree (sys_levels = {L}) or for a forest of
+// trees with the same leaf size and rank (sys_levels sorted in decreasing
+// order; d.n = sum of leaf * 2^L_i and d.levels = the largest L_i).
+static int create_ctx(const hodlr_desc &d, const std::vector<int> &sys_levels, hodlr_ctx **out) {
   hodlr_ctx *h = new hodlr_ctx();
   h->d = d;
   h->n = d.n;
   h->m = d.leaf;
   h->L = d.levels;
   h->r = d.levels > 0 ? d.rank : std::max(1, d.rank);
-  h->nleaf = 1 << d.levels;
-  h->nnode = (1 << d.levels) - 1;
+  h->nleaf = (int)(d.n / d.leaf);
   h->kmax = d.nrhs_max;
   h->mixed = d.precision == HODLR_PREC_MIXED;
   h->has_level.assign(h->L, 0);
+  h->nsys = (int)sys_levels.size();
+  h->forest = h->nsys > 1;
+  set_geometry(h, sys_levels);
   if (d.stream) {
     h->st = (cudaStream_t)d.stream;
   } else {
@@ -755,8 +804,12 @@ int hodlr_create(const hodlr_desc *desc, hodlr_handle *out) {
   ALLOC(h->Wbuf, double, h->tbuf_elems);
   ALLOC(h->eta, double, h->eta_elems);
   ALLOC(h->red, double, h->red_elems);
-  ALLOC(h->norms, double, 2 * (size_t)k);
-  ALLOC(h->nwork, double, (size_t)k * 64);
+  ALLOC(h->norms, double, 2 * (size_t)k * h->nsys);
+  ALLOC(h->nwork, double, (size_t)k * std::max(64, h->forest ? h->nleaf : 0));
+  if (h->forest) {
+    ALLOC(h->seg_leaf, int, (size_t)h->nsys + 1);
+    ALLOC(h->sfold, double, (size_t)r);
+  }
   ALLOC(h->dst, DevStatus, 1);
 #undef ALLOC
   if (cudaMallocHost(&h->hst, sizeof(DevStatus)) != cudaSuccess) {
@@ -775,6 +828,23 @@ int hodlr_create(const hodlr_desc *desc, hodlr_handle *out) {
       return set_err(HODLR_ERR_CUDA, cudaGetErrorString(fe));
     }
   }
+  if (h->forest) {
+    // rows of a level that a shorter tree does not have stay zero in U, V
+    // and their derived copies; per-system leaf offsets for the norms
+    std::vector<int> seg(1, 0);
+    for (int Li : sys_levels) seg.push_back(seg.back() + (1 << Li));
+    const size_t nlr = (size_t)n * L * r;
+    bool ok = cudaMemcpy(h->seg_leaf, seg.data(), sizeof(int) * seg.size(), cudaMemcpyHostToDevice) == cudaSuccess;
+    ok = ok && cudaMemsetAsync(h->U, 0, sizeof(double) * nlr, h->st) == cudaSuccess;
+    ok = ok && cudaMemsetAsync(h->V, 0, sizeof(double) * nlr, h->st) == cudaSuccess;
+    if (h->V32) ok = ok && cudaMemsetAsync(h->V32, 0, sizeof(float) * nlr, h->st) == cudaSuccess;
+    if (h->U2) ok = ok && cudaMemsetAsync(h->U2, 0, sizeof(float2) * nlr, h->st) == cudaSuccess;
+    if (h->V2) ok = ok && cudaMemsetAsync(h->V2, 0, sizeof(float2) * nlr, h->st) == cudaSuccess;
+    if (!ok) {
+      free_ctx(h);
+      return set_err(HODLR_ERR_CUDA, "forest initialisation");
+    }
+  }
   if (cudaMemsetAsync(h->dst, 0, sizeof(DevStatus), h->st) != cudaSuccess ||
       cudaStreamSynchronize(h->st) != cudaSuccess) {
     free_ctx(h);
@@ -782,6 +852,23 @@ int hodlr_create(const hodlr_desc *desc, hodlr_handle *out) {
   }
   *out = h;
   return HODLR_OK;
+}
+
+// ----------------------------------------------------------------- C ABI
+extern "C" {
+
+const char *hodlr_last_error_string(void) { return g_err.c_str(); }
+
+int64_t hodlr_kernel_launches(void) { return (int64_t)g_launches.load(); }
+
+int hodlr_create(const hodlr_desc *desc, hodlr_handle *out) {
+  if (!desc || !out) return set_err(HODLR_ERR_INVALID_ARG, "null argument");
+  *out = nullptr;
+  const hodlr_desc &d = *desc;
+  if (d.leaf < 1 || d.levels < 0 || d.levels > 24 || d.n != ((int64_t)d.leaf << d.levels))
+    return set_err(HODLR_ERR_INVALID_ARG, "need n = leaf * 2^levels, leaf >= 1, 0 <= levels <= 24");
+  CKS(check_common(d));
+  return create_ctx(d, std::vector<int>(1, d.levels), out);
 }
 
 int hodlr_destroy(hodlr_handle h) {
@@ -969,8 +1056,8 @@ int hodlr_adjoint(hodlr_handle h, const double *x, int64_t ldx, const double *g,
     CK(launch_update_nn<double>(ua, s));
   }
   for (int l = 0; l < L && (gr->dU || gr->dV || gr->ds); ++l) {
-    const int nb = 2 << l;
-    const long long rows = n >> (l + 1);
+    const int nb = h->nb(l);
+    const long long rows = h->rows(l);
     CK(launch_reduce_tn<double>(h->Vlev(l), n, x, ldx, rows, nb, r, k, h->Tbuf, h->red, nullptr, s));
     CK(launch_reduce_tn<double>(h->Ulev(l), n, lam, ldl, rows, nb, r, k, h->Wbuf, h->red, nullptr, s));
     for (int which = 0; which < 2; ++which) {
@@ -1096,8 +1183,8 @@ int hodlr_generate(hodlr_handle h, uint64_t seed, double shift, int orthonormal,
   double *tmp = nullptr;
   if (orthonormal && L > 0) CK(cudaMallocAsync(&tmp, sizeof(double) * n * r, s));
   for (int l = 0; l < L; ++l) {
-    const int nb = 2 << l;
-    const long long rows = n >> (l + 1);
+    const int nb = h->nb(l);
+    const long long rows = h->rows(l);
     for (int w = 0; w < 2; ++w) {
       double *X = w == 0 ? h->Ulev(l) : h->Vlev(l);
       const unsigned long long stream = 0x100ull + 2ull * l + w;
@@ -1408,6 +1495,447 @@ int hodlr_node_solve(int nnode, int r, int nrhs, const double *VTu, int64_t ldu,
   DevStatus hs{};
   CK(cudaMemcpy(&hs, st, sizeof(DevStatus), cudaMemcpyDeviceToHost));
   if (hs.code) return set_err(hs.code, "node_solve: singular capacitance system");
+  return HODLR_OK;
+}
+
+}  // extern "C"
+
+// =========================================================== ragged batches
+// Systems that share (leaf, rank) are stacked, largest first, into one
+// forest: a handle whose level l holds the blocks of every tree tall enough
+// to have it, so each sweep step is one launch over all of them.  Each forest
+// runs on its own stream; a batch factorisation or solve forks from the
+// batch stream into the forests' streams and joins back, and from the second
+// call on it is one CUDA graph launch.
+struct BatchMember {
+  int forest = 0;
+  long long row_off = 0;  // first row of the system in its forest
+  int slot0 = 0;          // forest level that holds the system's level 0
+  bool has_D = false;
+  std::vector<char> has_level;
+};
+
+struct BatchForest {
+  hodlr_ctx *h = nullptr;
+  std::vector<int> ids;          // member systems in stacking order
+  long long maxn = 0;
+  double *Bg = nullptr;          // stacked right-hand sides, n x kmax
+  RhsCopy *tab_host = nullptr;   // pinned; read by a graph memcpy node each solve
+  RhsCopy *tab_dev = nullptr;
+  cudaEvent_t join = nullptr;
+};
+
+struct hodlr_batch_ctx {
+  hodlr_batch_desc d{};
+  std::vector<hodlr_system> sys;
+  std::vector<BatchMember> mem;
+  std::vector<BatchForest> forests;
+  cudaStream_t st = nullptr;
+  bool own_stream = false;
+  cudaEvent_t fork = nullptr;
+  cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+  GraphEntry factor_graph, solve_graph;
+  int factor_runs = 0, solve_runs = 0;
+  bool factored = false;
+  float factor_ms = 0.f, solve_ms = 0.f;
+};
+
+static void free_batch(hodlr_batch_ctx *b) {
+  if (!b) return;
+  if (b->st) cudaStreamSynchronize(b->st);
+  for (GraphEntry *g : {&b->factor_graph, &b->solve_graph})
+    if (g->exec) cudaGraphExecDestroy(g->exec);
+  for (auto &f : b->forests) {
+    if (f.h) cudaStreamSynchronize(f.h->st);
+    if (f.tab_host) cudaFreeHost(f.tab_host);
+    if (f.join) cudaEventDestroy(f.join);
+    free_ctx(f.h);
+  }
+  if (b->fork) cudaEventDestroy(b->fork);
+  for (auto &e : b->ev)
+    if (e) cudaEventDestroy(e);
+  if (b->own_stream && b->st) cudaStreamDestroy(b->st);
+  delete b;
+}
+
+// Eager on the first call, then captured once into a graph and replayed.
+template <typename F>
+static int batch_graphed(hodlr_batch_ctx *b, GraphEntry &g, int &runs, F fn) {
+  if (runs == 0) {
+    ++runs;
+    return fn();
+  }
+  if (!g.exec) {
+    const long long before = g_launches.load();
+    CK(cudaStreamBeginCapture(b->st, cudaStreamCaptureModeThreadLocal));
+    int rc = fn();
+    cudaGraph_t graph = nullptr;
+    cudaError_t ce = cudaStreamEndCapture(b->st, &graph);
+    if (rc != HODLR_OK) {
+      if (graph) cudaGraphDestroy(graph);
+      return rc;
+    }
+    CK(ce);
+    cudaError_t ie = cudaGraphInstantiate(&g.exec, graph, 0);
+    cudaGraphDestroy(graph);
+    CK(ie);
+    g.kernels = g_launches.load() - before;
+    g_launches.fetch_sub(g.kernels);
+  }
+  g_launches.fetch_add(g.kernels);
+  CK(cudaGraphLaunch(g.exec, b->st));
+  ++runs;
+  return HODLR_OK;
+}
+
+// Run body(forest) on every forest's stream, forked from and joined back
+// into the batch stream.
+template <typename F>
+static int batch_forked(hodlr_batch_ctx *b, F body) {
+  CK(cudaEventRecord(b->fork, b->st));
+  for (auto &f : b->forests) {
+    CK(cudaStreamWaitEvent(f.h->st, b->fork, 0));
+    CKS(body(f));
+    CK(cudaEventRecord(f.join, f.h->st));
+    CK(cudaStreamWaitEvent(b->st, f.join, 0));
+  }
+  return HODLR_OK;
+}
+
+// The system that owns row `row` of forest f (or -1).
+static int batch_owner(const hodlr_batch_ctx *b, const BatchForest &f, long long row) {
+  for (int id : f.ids) {
+    const BatchMember &mb = b->mem[id];
+    if (row >= mb.row_off && row < mb.row_off + b->sys[id].n) return id;
+  }
+  return -1;
+}
+
+// Read every forest's device status; on an error name the system.
+static int batch_status(hodlr_batch_ctx *b, hodlr_solve_info *info) {
+  int first = HODLR_OK;
+  std::string msg;
+  for (auto &f : b->forests) {
+    hodlr_ctx *h = f.h;
+    CK(cudaMemcpy(h->hst, h->dst, sizeof(DevStatus), cudaMemcpyDeviceToHost));
+    const DevStatus s = *h->hst;
+    if (info)
+      for (int id : f.ids) {
+        info[id].status = s.code;
+        info[id].iterations = s.iters;
+        info[id].bad_index = -1;
+        info[id].rel_residual = -1.0;
+      }
+    if (s.code == HODLR_OK) continue;
+    long long row = s.index;  // a row for leaf / input errors, a node for capacitance errors
+    if (s.code == HODLR_ERR_SINGULAR_LEAF) row = s.index * h->m;
+    if (s.code == HODLR_ERR_SINGULAR_CAPACITANCE)
+      for (int l = h->L - 1; l >= 0; --l)
+        if (s.index >= h->node_base(l)) {
+          row = (s.index - h->node_base(l)) * 2 * h->rows(l);
+          break;
+        }
+    const int id = batch_owner(b, f, row);
+    if (info && id >= 0) info[id].bad_index = s.index;
+    if (first == HODLR_OK) {
+      first = s.code;
+      char buf[160];
+      snprintf(buf, sizeof buf, "system %d: error %d (forest index %lld)", id, s.code, s.index);
+      msg = buf;
+    }
+  }
+  if (first != HODLR_OK) return set_err(first, msg);
+  return HODLR_OK;
+}
+
+extern "C" {
+
+int hodlr_batch_create(const hodlr_batch_desc *desc, hodlr_batch *out) {
+  if (!desc || !out || !desc->systems || desc->count < 1)
+    return set_err(HODLR_ERR_INVALID_ARG, "batch: null argument or empty batch");
+  *out = nullptr;
+  const hodlr_batch_desc &d = *desc;
+  std::map<std::pair<int, int>, std::vector<int>> groups;
+  for (int i = 0; i < d.count; ++i) {
+    const hodlr_system &s = d.systems[i];
+    if (s.leaf < 1 || s.levels < 0 || s.levels > 24 || s.n != ((int64_t)s.leaf << s.levels) || s.nrhs < 1 ||
+        (s.levels > 0 && (s.rank < 1 || s.rank > 64))) {
+      char buf[128];
+      snprintf(buf, sizeof buf, "batch: system %d needs n = leaf * 2^levels, rank in [1, 64], nrhs >= 1", i);
+      return set_err(HODLR_ERR_INVALID_ARG, buf);
+    }
+    if (s.levels > 0) groups[{s.leaf, s.rank}].push_back(i);
+  }
+  // one-leaf systems (no levels) join a forest of their leaf size, if any
+  for (int i = 0; i < d.count; ++i) {
+    const hodlr_system &s = d.systems[i];
+    if (s.levels > 0) continue;
+    auto it = groups.lower_bound({s.leaf, 0});
+    if (it != groups.end() && it->first.first == s.leaf)
+      it->second.push_back(i);
+    else
+      groups[{s.leaf, 0}].push_back(i);
+  }
+  hodlr_batch_ctx *b = new hodlr_batch_ctx();
+  b->d = d;
+  b->sys.assign(d.systems, d.systems + d.count);
+  b->d.systems = nullptr;
+  b->mem.resize(d.count);
+  auto fail = [&](int code, const std::string &m) {
+    free_batch(b);
+    return set_err(code, m);
+  };
+  if (d.stream) {
+    b->st = (cudaStream_t)d.stream;
+  } else {
+    if (cudaStreamCreateWithFlags(&b->st, cudaStreamNonBlocking) != cudaSuccess)
+      return fail(HODLR_ERR_CUDA, "batch: stream");
+    b->own_stream = true;
+  }
+  if (cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming) != cudaSuccess)
+    return fail(HODLR_ERR_CUDA, "batch: event");
+  for (auto &e : b->ev)
+    if (cudaEventCreate(&e) != cudaSuccess) return fail(HODLR_ERR_CUDA, "batch: event");
+  for (auto &g : groups) {
+    std::vector<int> ids = g.second;
+    std::stable_sort(ids.begin(), ids.end(),
+                     [&](int a, int c) { return b->sys[a].levels > b->sys[c].levels; });
+    hodlr_desc fd{};
+    fd.leaf = g.first.first;
+    fd.rank = std::max(1, g.first.second);
+    fd.levels = b->sys[ids[0]].levels;
+    fd.n = 0;
+    fd.nrhs_max = 1;
+    std::vector<int> lv;
+    for (int id : ids) {
+      fd.n += b->sys[id].n;
+      fd.nrhs_max = std::max(fd.nrhs_max, b->sys[id].nrhs);
+      lv.push_back(b->sys[id].levels);
+    }
+    fd.precision = d.precision;
+    fd.residual = d.residual;
+    fd.refine_tol = d.refine_tol;
+    fd.refine_max_iter = d.refine_max_iter;
+    int rc = check_common(fd);
+    if (rc != HODLR_OK) return fail(rc, hodlr_last_error_string());
+    if (fd.n / fd.leaf > (1LL << 30)) return fail(HODLR_ERR_INVALID_ARG, "batch: too many leaves in one forest");
+    BatchForest f;
+    rc = create_ctx(fd, lv, &f.h);
+    if (rc != HODLR_OK) return fail(rc, hodlr_last_error_string());
+    b->forests.push_back(f);
+    BatchForest &F = b->forests.back();
+    F.ids = ids;
+    long long off = 0;
+    for (int id : ids) {
+      BatchMember &mb = b->mem[id];
+      mb.forest = (int)b->forests.size() - 1;
+      mb.row_off = off;
+      mb.slot0 = fd.levels - b->sys[id].levels;
+      mb.has_level.assign(b->sys[id].levels, 0);
+      off += b->sys[id].n;
+      F.maxn = std::max<long long>(F.maxn, b->sys[id].n);
+    }
+    cudaError_t e = cudaSuccess;
+    F.Bg = F.h->alloc<double>((size_t)fd.n * fd.nrhs_max, e);
+    if (e != cudaSuccess) return fail(HODLR_ERR_OUT_OF_MEMORY, "batch: right-hand-side buffer");
+    F.tab_dev = F.h->alloc<RhsCopy>(ids.size(), e);
+    if (e != cudaSuccess) return fail(HODLR_ERR_OUT_OF_MEMORY, "batch: copy table");
+    if (cudaMallocHost(&F.tab_host, sizeof(RhsCopy) * ids.size()) != cudaSuccess)
+      return fail(HODLR_ERR_OUT_OF_MEMORY, "batch: pinned copy table");
+    if (cudaEventCreateWithFlags(&F.join, cudaEventDisableTiming) != cudaSuccess)
+      return fail(HODLR_ERR_CUDA, "batch: event");
+  }
+  *out = b;
+  return HODLR_OK;
+}
+
+int hodlr_batch_destroy(hodlr_batch b) {
+  free_batch(b);
+  return HODLR_OK;
+}
+
+int hodlr_batch_set_leaf_blocks(hodlr_batch b, int i, const double *D, int64_t ld, int64_t leaf_stride) {
+  if (!b || !D || i < 0 || i >= (int)b->sys.size()) return set_err(HODLR_ERR_INVALID_ARG, "batch: bad argument");
+  const hodlr_system &sy = b->sys[i];
+  BatchMember &mb = b->mem[i];
+  hodlr_ctx *h = b->forests[mb.forest].h;
+  const int m = sy.leaf;
+  if (ld < m) return set_err(HODLR_ERR_INVALID_ARG, "batch: ld < leaf size");
+  const long long mm = (long long)m * m, leaf0 = mb.row_off / m, nl = sy.n / m;
+  double *dst = h->D + leaf0 * mm;
+  if (ld == m && leaf_stride == mm) {
+    CK(cudaMemcpyAsync(dst, D, sizeof(double) * mm * nl, cudaMemcpyDefault, h->st));
+  } else {
+    for (int j = 0; j < m; ++j)
+      CK(cudaMemcpy2DAsync(dst + (long long)j * m, sizeof(double) * mm, D + (long long)j * ld,
+                           sizeof(double) * leaf_stride, sizeof(double) * m, nl, cudaMemcpyDefault, h->st));
+  }
+  CKS(prepare_leaves(h, leaf0, nl));
+  mb.has_D = true;
+  b->factored = false;
+  CK(cudaStreamSynchronize(h->st));
+  return HODLR_OK;
+}
+
+int hodlr_batch_set_lowrank(hodlr_batch b, int i, int level, const double *U, int64_t ldu, const double *V,
+                            int64_t ldv, const double *s) {
+  if (!b || !U || !V || i < 0 || i >= (int)b->sys.size()) return set_err(HODLR_ERR_INVALID_ARG, "batch: bad argument");
+  const hodlr_system &sy = b->sys[i];
+  BatchMember &mb = b->mem[i];
+  hodlr_ctx *h = b->forests[mb.forest].h;
+  if (level < 0 || level >= sy.levels) return set_err(HODLR_ERR_INVALID_ARG, "batch: level out of range");
+  if (ldu < sy.n || ldv < sy.n) return set_err(HODLR_ERR_INVALID_ARG, "batch: ld < n");
+  const int slot = mb.slot0 + level, r = h->r;
+  double *Ud = h->Ulev(slot) + mb.row_off, *Vd = h->Vlev(slot) + mb.row_off;
+  CK(cudaMemcpy2DAsync(Ud, sizeof(double) * h->n, U, sizeof(double) * ldu, sizeof(double) * sy.n, r,
+                       cudaMemcpyDefault, h->st));
+  CK(cudaMemcpy2DAsync(Vd, sizeof(double) * h->n, V, sizeof(double) * ldv, sizeof(double) * sy.n, r,
+                       cudaMemcpyDefault, h->st));
+  if (s) {
+    CK(cudaMemcpyAsync(h->sfold, s, sizeof(double) * r, cudaMemcpyDefault, h->st));
+    CK(launch_scale_cols(Vd, h->n, sy.n, r, h->sfold, h->st));
+  }
+  CKS(prepare_level(h, slot, mb.row_off, sy.n));
+  mb.has_level[level] = 1;
+  b->factored = false;
+  CK(cudaStreamSynchronize(h->st));
+  return HODLR_OK;
+}
+
+int hodlr_batch_generate(hodlr_batch b, uint64_t seed, double shift, double *const *B, const int64_t *ldb) {
+  if (!b) return set_err(HODLR_ERR_INVALID_ARG, "batch: null handle");
+  for (int i = 0; i < (int)b->sys.size(); ++i) {
+    const hodlr_system &sy = b->sys[i];
+    BatchMember &mb = b->mem[i];
+    hodlr_ctx *h = b->forests[mb.forest].h;
+    const int m = sy.leaf, r = h->r;
+    const unsigned long long si = seed + (unsigned long long)i;
+    const long long leaf0 = mb.row_off / m, nl = sy.n / m;
+    CK(launch_gen_leaves(h->D + leaf0 * m * m, m, (int)nl, si, shift, h->st));
+    CKS(prepare_leaves(h, leaf0, nl));
+    mb.has_D = true;
+    for (int l = 0; l < sy.levels; ++l) {
+      const int slot = mb.slot0 + l;
+      const long long rows = sy.n >> (l + 1);
+      for (int w = 0; w < 2; ++w) {
+        double *X = (w == 0 ? h->Ulev(slot) : h->Vlev(slot)) + mb.row_off;
+        CK(launch_gaussian(X, h->n, sy.n, r, si, 0x100ull + 2ull * l + w, 1.0 / std::sqrt((double)rows), h->st));
+      }
+      CKS(prepare_level(h, slot, mb.row_off, sy.n));
+      mb.has_level[l] = 1;
+    }
+    if (B && B[i]) {
+      if (!ldb || ldb[i] < sy.n) return set_err(HODLR_ERR_INVALID_ARG, "batch: ldb < n");
+      CK(launch_gaussian(B[i], ldb[i], sy.n, sy.nrhs, si, 0xBull, 1.0, h->st));
+    }
+  }
+  for (auto &f : b->forests) CK(cudaStreamSynchronize(f.h->st));
+  b->factored = false;
+  return HODLR_OK;
+}
+
+int hodlr_batch_factor(hodlr_batch b) {
+  if (!b) return set_err(HODLR_ERR_INVALID_ARG, "batch: null handle");
+  for (int i = 0; i < (int)b->sys.size(); ++i) {
+    const BatchMember &mb = b->mem[i];
+    bool ok = mb.has_D;
+    for (char c : mb.has_level) ok = ok && c;
+    if (!ok) {
+      char buf[96];
+      snprintf(buf, sizeof buf, "batch: system %d has unset leaf blocks or levels", i);
+      return set_err(HODLR_ERR_NOT_FACTORED, buf);
+    }
+  }
+  b->factored = false;
+  CK(cudaEventRecord(b->ev[0], b->st));
+  int rc = batch_graphed(b, b->factor_graph, b->factor_runs, [&]() -> int {
+    return batch_forked(b, [&](BatchForest &f) -> int {
+      CKS(reset_status(f.h));
+      if (f.h->mixed) return factor_sweep<float>(f.h);
+      return factor_sweep<double>(f.h);
+    });
+  });
+  CKS(rc);
+  CK(cudaEventRecord(b->ev[1], b->st));
+  CK(cudaStreamSynchronize(b->st));
+  CKS(batch_status(b, nullptr));
+  cudaEventElapsedTime(&b->factor_ms, b->ev[0], b->ev[1]);
+  for (auto &f : b->forests) f.h->factored = true;
+  b->factored = true;
+  return HODLR_OK;
+}
+
+int hodlr_batch_solve(hodlr_batch b, double *const *B, const int64_t *ldb, hodlr_solve_info *info) {
+  if (!b || !B || !ldb) return set_err(HODLR_ERR_INVALID_ARG, "batch: null argument");
+  if (!b->factored) return set_err(HODLR_ERR_NOT_FACTORED, "batch: call hodlr_batch_factor first");
+  for (auto &f : b->forests)
+    for (size_t q = 0; q < f.ids.size(); ++q) {
+      const int id = f.ids[q];
+      const hodlr_system &sy = b->sys[id];
+      if (!B[id] || ldb[id] < sy.n) return set_err(HODLR_ERR_INVALID_ARG, "batch: null B[i] or ldb[i] < n_i");
+      RhsCopy t{};
+      t.ext = B[id];
+      t.ld = ldb[id];
+      t.row_off = b->mem[id].row_off;
+      t.n = sy.n;
+      t.k = sy.nrhs;
+      f.tab_host[q] = t;
+    }
+  CK(cudaEventRecord(b->ev[2], b->st));
+  int rc = batch_graphed(b, b->solve_graph, b->solve_runs, [&]() -> int {
+    return batch_forked(b, [&](BatchForest &f) -> int {
+      hodlr_ctx *h = f.h;
+      const int nid = (int)f.ids.size(), k = h->kmax;
+      CKS(reset_status(h));
+      CK(cudaMemcpyAsync(f.tab_dev, f.tab_host, sizeof(RhsCopy) * nid, cudaMemcpyHostToDevice, h->st));
+      CK(launch_gather_rhs(f.tab_dev, nid, f.maxn, f.Bg, h->n, k, h->st));
+      CK(launch_check_finite(f.Bg, h->n, h->n, k, h->dst, h->st));
+      if (h->mixed)
+        CKS(mixed_solve(h, f.Bg, h->n, k, false));
+      else
+        CKS(solve_sweep<double>(h, f.Bg, h->n, k, false, nullptr));
+      CK(launch_scatter_rhs(f.tab_dev, nid, f.maxn, f.Bg, h->n, k, h->st));
+      return HODLR_OK;
+    });
+  });
+  CKS(rc);
+  CK(cudaEventRecord(b->ev[3], b->st));
+  CK(cudaStreamSynchronize(b->st));
+  cudaEventElapsedTime(&b->solve_ms, b->ev[2], b->ev[3]);
+  int st = batch_status(b, info);
+  // per-system relative residuals of the refinement (mixed mode)
+  if (info && b->d.precision == HODLR_PREC_MIXED)
+    for (auto &f : b->forests) {
+      hodlr_ctx *h = f.h;
+      const size_t cnt = (size_t)h->nsys * h->kmax;
+      std::vector<double> nb(2 * cnt);
+      CK(cudaMemcpy(nb.data(), h->norms, sizeof(double) * 2 * cnt, cudaMemcpyDeviceToHost));
+      for (size_t q = 0; q < f.ids.size(); ++q) {
+        const int id = f.ids[q];
+        double rel = 0.0;
+        for (int j = 0; j < b->sys[id].nrhs; ++j) {
+          const double bn = nb[(size_t)j * h->nsys + q], rn = nb[cnt + (size_t)j * h->nsys + q];
+          rel = std::max(rel, rn / (bn > 0.0 ? bn : 1.0));
+        }
+        info[id].rel_residual = rel;
+      }
+    }
+  if (st != HODLR_OK) return st;
+  if (b->d.precision == HODLR_PREC_MIXED)
+    for (auto &f : b->forests)
+      if (!f.h->hst->done) {
+        if (info)
+          for (int id : f.ids) info[id].status = HODLR_ERR_NOT_CONVERGED;
+        return set_err(HODLR_ERR_NOT_CONVERGED, "batch: refinement did not reach the tolerance");
+      }
+  return HODLR_OK;
+}
+
+int hodlr_batch_stats(hodlr_batch b, int *nforests, double *factor_ms, double *solve_ms) {
+  if (!b) return set_err(HODLR_ERR_INVALID_ARG, "batch: null handle");
+  if (nforests) *nforests = (int)b->forests.size();
+  if (factor_ms) *factor_ms = b->factor_ms;
+  if (solve_ms) *solve_ms = b->solve_ms;
   return HODLR_OK;
 }
 

@@ -118,6 +118,27 @@ cudaError_t launch_add_correction(const double *X, long long ldx, const Td *D, l
 // Column norms ||X_j||_2 (FP64) into out[j]; deterministic.
 cudaError_t launch_colnorms(const double *X, long long ldx, long long n, int c, double *out,
                             double *work, const int *skip, cudaStream_t s);
+// Per-system column norms of a forest: out[j*nsys + i] = ||rows of system i
+// in column j||_2, system i = leaves [seg_leaf[i], seg_leaf[i+1]) of m rows.
+// work: nleaf*c doubles.  Deterministic.
+cudaError_t launch_seg_colnorms(const double *X, long long ldx, int m, int nleaf, int c, const int *seg_leaf,
+                                int nsys, double *out, double *work, const int *skip, cudaStream_t s);
+// X[:, j] *= sc[j] for the n x c tile X (FP64).
+cudaError_t launch_scale_cols(double *X, long long ldx, long long n, int c, const double *sc, cudaStream_t s);
+// Right-hand sides of the systems of a ragged batch and the stacked n x kmax
+// block of their forest: system i owns rows [row_off, row_off + n) and
+// columns [0, k) of its own buffer ext (ld).
+struct RhsCopy {
+  double *ext;
+  long long ld, row_off, n;
+  int k, pad;
+};
+// G[row_off + i, j] = ext[i, j] for j < k, 0 for k <= j < kmax (every system in tab).
+cudaError_t launch_gather_rhs(const RhsCopy *tab, int count, long long maxn, double *G, long long ldg, int kmax,
+                              cudaStream_t s);
+// ext[i, j] = G[row_off + i, j] for j < k.
+cudaError_t launch_scatter_rhs(const RhsCopy *tab, int count, long long maxn, const double *G, long long ldg,
+                               int kmax, cudaStream_t s);
 // Refinement control: rel = max_j rnorm[j]/bnorm[j]; st->resid = rel;
 // if rel <= tol set st->done = 1.  If advance, count an iteration when not done.
 cudaError_t launch_refine_check(const double *rnorm, const double *bnorm, int c, double tol,

@@ -154,6 +154,95 @@ cudaError_t launch_colnorms(const double *X, long long ldx, long long n, int c, 
   return cudaGetLastError();
 }
 
+// One warp per (leaf, column): the sum of squares of the leaf's m rows, in a
+// fixed butterfly order.
+__global__ void leaf_sumsq_kernel(const double *X, long long ldx, int m, int nleaf, int c, double *work,
+                                  const int *skip) {
+  if (skip && *skip) return;
+  const long long w = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (w >= (long long)nleaf * c) return;
+  const int leaf = (int)(w % nleaf), j = (int)(w / nleaf);
+  const double *x = X + (long long)leaf * m + (long long)j * ldx;
+  double acc = 0.0;
+  for (int i = lane; i < m; i += 32) acc += x[i] * x[i];
+  for (int o = 16; o; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+  if (lane == 0) work[(long long)j * nleaf + leaf] = acc;
+}
+
+__global__ void seg_norm_kernel(const double *work, int nleaf, int c, const int *seg, int nsys, double *out,
+                                const int *skip) {
+  if (skip && *skip) return;
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nsys * c) return;
+  const int i = t % nsys, j = t / nsys;
+  double acc = 0.0;
+  for (int q = seg[i]; q < seg[i + 1]; ++q) acc += work[(long long)j * nleaf + q];
+  out[(long long)j * nsys + i] = sqrt(acc);
+}
+
+cudaError_t launch_seg_colnorms(const double *X, long long ldx, int m, int nleaf, int c, const int *seg_leaf,
+                                int nsys, double *out, double *work, const int *skip, cudaStream_t s) {
+  if (c <= 0 || nleaf <= 0) return cudaSuccess;
+  const long long warps = (long long)nleaf * c;
+  HODLR_LAUNCH(leaf_sumsq_kernel, (int)ceil_div(warps * 32, 256), 256, 0, s, X, ldx, m, nleaf, c, work, skip);
+  HODLR_LAUNCH(seg_norm_kernel, ceil_div(nsys * c, 128), 128, 0, s, work, nleaf, c, seg_leaf, nsys, out, skip);
+  return cudaGetLastError();
+}
+
+__global__ void scale_cols_kernel(double *X, long long ldx, long long n, int c, const double *sc) {
+  HODLR_FOR_2D(i, j, n, c) X[i + j * ldx] *= sc[j];
+}
+
+cudaError_t launch_scale_cols(double *X, long long ldx, long long n, int c, const double *sc, cudaStream_t s) {
+  if (n * c == 0) return cudaSuccess;
+  HODLR_LAUNCH(scale_cols_kernel, grid2d(n, c), 256, 0, s, X, ldx, n, c, sc);
+  return cudaGetLastError();
+}
+
+// grid (row chunks, systems): each CTA strides over its system's n x kmax
+// elements (one column-major sweep per column).
+__global__ void gather_rhs_kernel(const RhsCopy *tab, double *G, long long ldg, int kmax) {
+  const RhsCopy t = tab[blockIdx.y];
+  const long long total = t.n * kmax;
+  for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < total;
+       e += (long long)gridDim.x * blockDim.x) {
+    const long long i = e % t.n;
+    const int j = (int)(e / t.n);
+    G[t.row_off + i + j * ldg] = j < t.k ? t.ext[i + j * t.ld] : 0.0;
+  }
+}
+
+__global__ void scatter_rhs_kernel(const RhsCopy *tab, const double *G, long long ldg) {
+  const RhsCopy t = tab[blockIdx.y];
+  const long long total = t.n * t.k;
+  for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < total;
+       e += (long long)gridDim.x * blockDim.x) {
+    const long long i = e % t.n;
+    const int j = (int)(e / t.n);
+    t.ext[i + j * t.ld] = G[t.row_off + i + j * ldg];
+  }
+}
+
+static dim3 rhs_grid(int count, long long maxn, int kmax) {
+  const long long chunks = std::max<long long>(1, std::min<long long>(ceil_div(maxn * kmax, 256), 64));
+  return dim3((unsigned)chunks, (unsigned)count);
+}
+
+cudaError_t launch_gather_rhs(const RhsCopy *tab, int count, long long maxn, double *G, long long ldg, int kmax,
+                              cudaStream_t s) {
+  if (count <= 0) return cudaSuccess;
+  HODLR_LAUNCH(gather_rhs_kernel, rhs_grid(count, maxn, kmax), 256, 0, s, tab, G, ldg, kmax);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_scatter_rhs(const RhsCopy *tab, int count, long long maxn, const double *G, long long ldg,
+                               int kmax, cudaStream_t s) {
+  if (count <= 0) return cudaSuccess;
+  HODLR_LAUNCH(scatter_rhs_kernel, rhs_grid(count, maxn, kmax), 256, 0, s, tab, G, ldg);
+  return cudaGetLastError();
+}
+
 __global__ void refine_check_kernel(const double *rnorm, const double *bnorm, int c, double tol,
                                     DevStatus *st, int advance) {
   if (threadIdx.x != 0) return;

@@ -267,6 +267,62 @@ HODLR_API int hodlr_profile(hodlr_handle h, int enable, double *phase_ms, int64_
  * (CUDA events on the handle's stream). */
 HODLR_API int hodlr_last_timings(hodlr_handle h, double *factor_ms, double *solve_ms);
 
+/* ------------------------------------------------------- ragged batches
+ * Many independent HODLR systems of different sizes, leaf sizes, ranks and
+ * right-hand-side counts, factored and solved together.  No counterpart in
+ * the reference, which builds one tree per HMatrix (include/hmatrix.hpp:
+ * 10-23) and runs its leaves and nodes as separate Legion tasks
+ * (src/lmatrix.cc:449-865); the per-system arithmetic is that of
+ * hodlr_factor / hodlr_solve.  Systems sharing (leaf, rank) are stacked into
+ * one forest whose levels are processed by single launches over all its
+ * trees; the forests run as concurrent branches of one CUDA graph, so after
+ * the first call a factorisation or a solve of the whole batch is one graph
+ * launch. */
+typedef struct hodlr_system {
+  int64_t n;       /* leaf * 2^levels */
+  int32_t leaf;    /* leaf block size m */
+  int32_t levels;  /* tree depth L (0: one dense block) */
+  int32_t rank;    /* rank of every off-diagonal block, 1..64 (ignored when levels = 0) */
+  int32_t nrhs;    /* right-hand sides solved per call, >= 1 */
+} hodlr_system;
+
+typedef struct hodlr_batch_desc {
+  const hodlr_system *systems;
+  int32_t count;
+  int32_t precision;       /* HODLR_PREC_FP64 or HODLR_PREC_MIXED (all systems) */
+  int32_t residual;        /* HODLR_RESID_* (mixed only) */
+  double refine_tol;       /* per system: max_j ||r_j|| / ||b_j|| */
+  int32_t refine_max_iter;
+  int32_t flags;           /* reserved, 0 */
+  void *stream;            /* cudaStream_t the batch is ordered on, or NULL (own stream) */
+} hodlr_batch_desc;
+
+typedef struct hodlr_batch_ctx *hodlr_batch;
+
+HODLR_API int hodlr_batch_create(const hodlr_batch_desc *desc, hodlr_batch *out);
+HODLR_API int hodlr_batch_destroy(hodlr_batch b);
+/* System i's leaf blocks and level-l factors, with the meaning and layouts
+ * of hodlr_set_leaf_blocks / hodlr_set_lowrank (host or device memory).
+ * s, when given, is folded into V at set time (V diag(s)). */
+HODLR_API int hodlr_batch_set_leaf_blocks(hodlr_batch b, int i, const double *D, int64_t ld,
+                                          int64_t leaf_stride);
+HODLR_API int hodlr_batch_set_lowrank(hodlr_batch b, int i, int level, const double *U, int64_t ldu,
+                                      const double *V, int64_t ldv, const double *s);
+/* Seeded random systems (system i seeded with seed + i): leaves
+ * G/sqrt(m) + shift I, U and V Gaussian scaled by 1/sqrt(block rows), and,
+ * if B is given, Gaussian right-hand sides B[i] (n_i x nrhs_i, ld ldb[i]). */
+HODLR_API int hodlr_batch_generate(hodlr_batch b, uint64_t seed, double shift, double *const *B,
+                                   const int64_t *ldb);
+HODLR_API int hodlr_batch_factor(hodlr_batch b);
+/* X_i = A_i^{-1} B_i for every system, in place: B[i] is a device pointer
+ * to n_i x nrhs_i column-major values with leading dimension ldb[i].  info
+ * (count entries, or NULL) receives each system's status, refinement
+ * iterations (of its forest) and, in mixed mode, its relative residual. */
+HODLR_API int hodlr_batch_solve(hodlr_batch b, double *const *B, const int64_t *ldb, hodlr_solve_info *info);
+/* Forests the batch was split into, and device milliseconds of the last
+ * hodlr_batch_factor / hodlr_batch_solve. */
+HODLR_API int hodlr_batch_stats(hodlr_batch b, int *nforests, double *factor_ms, double *solve_ms);
+
 /* Kernels launched by this library since load (for launch accounting). */
 HODLR_API int64_t hodlr_kernel_launches(void);
 
