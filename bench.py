@@ -51,6 +51,27 @@ def algo_bytes(n, m, L, r, k, w=8):
     return (2 * n * m + 3 * n * r * L) * w + caps, (n * m + 2 * n * r * L + 2 * n * k) * w + caps
 
 
+def ragged_systems(count=512, seed=SEED):
+    """Ragged batch: N log-uniform in [2^10, 2^16] rounded to a power of two,
+    leaf m in {64, 128, 256} with m <= N/2, rank r in {8, 16, 32, 64} with
+    r < m, 1..8 right-hand sides.  Returns [(n, leaf, levels, rank, nrhs)]."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(count):
+        e = int(round(rng.uniform(10.0, 16.0)))
+        n = 1 << e
+        m = int(rng.choice([x for x in (64, 128, 256) if x <= n // 2]))
+        r = int(rng.choice([x for x in (8, 16, 32, 64) if x < m]))
+        k = int(rng.integers(1, 9))
+        L = (n // m).bit_length() - 1
+        out.append((n, m, L, r, k))
+    return out
+
+
+def ragged_flops(systems):
+    return sum(sum(algo_flops(n, m, L, r, k)) for n, m, L, r, k in systems)
+
+
 def resid_flops(n, m, L, r, k):
     return 2 * n * m * k + 4 * n * r * k * L
 
@@ -195,6 +216,7 @@ def run_ours(args, wl):
         B0 = colmajor(n, k)
         mixed.generate(SEED + rank, shift=1.5, orthonormal=True, decay=6.0, B=B0)
         B = colmajor(n, k)
+        tuning = None if args.no_tune else mixed.autotune(nrhs=k)
 
         def step():
             B.copy_(B0)
@@ -303,6 +325,8 @@ def run_ours(args, wl):
             e2e = {"value": g0.elapsed_time(g1) / args.e2e_steps, "unit": "ms", "h2d_bytes_per_step": h2d,
                    "d2h_bytes_per_step": n * k * 8}
 
+        ragged = None if args.no_ragged else run_ragged(args, fs, torch, stream, colmajor)
+
     # ---- report (max over ranks)
     if world > 1:
         t = torch.tensor([ms], device=dev)
@@ -357,6 +381,7 @@ def run_ours(args, wl):
                    **wl, "parallelism": "replicas" if world > 1 else "single GPU",
                    "l2": "inputs larger than L2 (>14 GB resident per step)",
                    "residual": "fp64-emulated (double-FP32)" if args.resid == 1 else "native fp64"},
+        "tuning": tuning,
         "refine_iterations": float(np.mean(iters)), "rel_resid_device": final_resid_dev,
         "rel_resid_fp64_check": check,
         "fp64_ms": float(np.mean(fp64_ms)), "fp64_factor_ms": fp64_factor_ms, "fp64_solve_ms": fp64_solve_ms,
@@ -369,6 +394,8 @@ def run_ours(args, wl):
         "clocks": clk, "gpu_launches": launches, "wall_s": wall,
         "e2e": e2e,
     }
+    if ragged is not None:
+        line["ragged_batch"] = ragged
     if cpu is not None:
         line["cpu_baseline"] = {"value": cpu[0], "unit": "ms", "cores": cpu[1], "kind": "port", "sample": cpu[2]}
     if rank == 0:
@@ -376,6 +403,76 @@ def run_ours(args, wl):
     if world > 1:
         torch.distributed.destroy_process_group()
     return 0
+
+
+def run_ragged(args, fs, torch, stream, colmajor):
+    """The ragged batch of 512 systems: batched factor + solve (one graph
+    launch each), FP64 and mixed, and the same systems as 512 separate
+    handles (FP64) for comparison."""
+    systems = ragged_systems(512, SEED)
+    sp = stream.cuda_stream
+    total = sum(n * k for n, m, L, r, k in systems)
+    out = {"systems": len(systems), "workload": "512 systems, N log-uniform in [2^10, 2^16], leaf {64,128,256}, "
+           "rank {8,16,32,64} < leaf, 1-8 rhs; leaves G/sqrt(m)+4I, Gaussian U, V (seeded)",
+           "rows": int(sum(s[0] for s in systems)), "algorithmic_gflop": ragged_flops(systems) / 1e9}
+    big0 = torch.empty(total, dtype=torch.float64, device="cuda")
+    big = torch.empty_like(big0)
+
+    def views(buf):
+        vs, off = [], 0
+        for n, m, L, r, k in systems:
+            vs.append(buf[off:off + n * k].view(k, n).t())
+            off += n * k
+        return vs
+
+    V0, V = views(big0), views(big)
+    for prec, name in ((fs.PREC_FP64, "fp64"), (fs.PREC_MIXED, "mixed")):
+        b = fs.Batch(systems, precision=prec, refine_tol=1e-12, stream=sp)
+        b.generate(SEED, shift=4.0, Bs=V0)
+        # per-forest launch shapes (mixed only: an FP64 tuning pass would take a minute)
+        tunes = b.autotune() if (prec == fs.PREC_MIXED and not args.no_tune) else None
+        infos = []
+
+        def step():
+            big.copy_(big0)
+            b.factor()
+            infos[:] = b.solve(V)
+
+        nsteps = min(args.steps, 3)   # an FP64 step of this batch takes seconds
+        for _ in range(2):            # eager run, then graph capture
+            step()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(nsteps):
+            step()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / nsteps
+        nf, fms, sms = b.stats()
+        out[name] = {"ms_per_step": ms, "steps": nsteps, "factor_ms": fms, "solve_ms": sms, "forests": nf,
+                     "tuning": tunes,
+                     "max_rel_residual": max(i.rel_residual for i in infos) if prec == fs.PREC_MIXED else None,
+                     "max_iterations": max(i.iterations for i in infos)}
+        b.close()
+    # the same systems as separate handles, one after another (FP64)
+    handles = []
+    for i, (n, m, L, r, k) in enumerate(systems):
+        h = fs.Solver(n, m, L, r, nrhs_max=k, precision=fs.PREC_FP64, stream=sp)
+        h.generate(SEED + i, shift=4.0, B=None)
+        handles.append(h)
+    for rep in range(2):   # the first pass loads and captures, the second is timed
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for h, x in zip(handles, V):
+            h.factor()
+            h.solve(x)
+        torch.cuda.synchronize()
+        loop_ms = (time.perf_counter() - t0) * 1e3
+    out["fp64_separate_handles_ms"] = loop_ms
+    for h in handles:
+        h.close()
+    return out
 
 
 # Measured on this pool's GB300 (FFMA / DFMA issue-rate probe, profiles/fp_peaks.md).
@@ -398,6 +495,8 @@ def main():
     ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 comparator")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-ragged", action="store_true", help="skip the 512-system ragged batch")
+    ap.add_argument("--no-tune", action="store_true", help="default launch shapes (no autotuning pass)")
     ap.add_argument("--no-phase-timing", action="store_true",
                     help="no per-phase CUDA events in the timed graphs (for profiler runs)")
     args = ap.parse_args()

@@ -56,6 +56,13 @@ class Grads(ctypes.Structure):
                 ("dU", ctypes.c_void_p), ("dV", ctypes.c_void_p), ("ds", ctypes.c_void_p)]
 
 
+class Tuning(ctypes.Structure):
+    _fields_ = [("red_ctas_per_sm", ctypes.c_int32), ("update_tile_rows", ctypes.c_int32), ("ms", ctypes.c_double)]
+
+    def as_dict(self):
+        return {"red_ctas_per_sm": self.red_ctas_per_sm, "update_tile_rows": self.update_tile_rows, "ms": self.ms}
+
+
 class System(ctypes.Structure):
     _fields_ = [("n", ctypes.c_int64), ("leaf", ctypes.c_int32), ("levels", ctypes.c_int32),
                 ("rank", ctypes.c_int32), ("nrhs", ctypes.c_int32)]
@@ -100,6 +107,10 @@ SIGNATURES = {
     "hodlr_batch_factor": (_I, [_VP]),
     "hodlr_batch_solve": (_I, [_VP, _VP, _VP, ctypes.POINTER(SolveInfo)]),
     "hodlr_batch_stats": (_I, [_VP, ctypes.POINTER(_I), ctypes.POINTER(_D), ctypes.POINTER(_D)]),
+    "hodlr_autotune": (_I, [_VP, _I, ctypes.POINTER(Tuning)]),
+    "hodlr_set_tuning": (_I, [_VP, ctypes.POINTER(Tuning)]),
+    "hodlr_get_tuning": (_I, [_VP, ctypes.POINTER(Tuning)]),
+    "hodlr_batch_autotune": (_I, [_VP, ctypes.POINTER(Tuning), _I]),
     "hodlr_kernel_launches": (_I64, []),
     "hodlr_last_error_string": (ctypes.c_char_p, []),
 }
@@ -226,6 +237,20 @@ class Solver:
         check(lib().hodlr_profile(self.h, enable, ms, n, len(PHASES)))
         return {name: (ms[i], n[i]) for i, name in enumerate(PHASES)}
 
+    def autotune(self, nrhs=1):
+        """Pick the launch shapes by timing factor + solve; leaves the handle factored."""
+        t = Tuning()
+        check(lib().hodlr_autotune(self.h, nrhs, ctypes.byref(t)))
+        return t.as_dict()
+
+    def set_tuning(self, red_ctas_per_sm=4, update_tile_rows=0):
+        check(lib().hodlr_set_tuning(self.h, ctypes.byref(Tuning(red_ctas_per_sm, update_tile_rows, -1.0))))
+
+    def get_tuning(self):
+        t = Tuning()
+        check(lib().hodlr_get_tuning(self.h, ctypes.byref(t)))
+        return t.as_dict()
+
     def timings(self):
         f, s = ctypes.c_double(), ctypes.c_double()
         check(lib().hodlr_last_timings(self.h, ctypes.byref(f), ctypes.byref(s)))
@@ -292,6 +317,13 @@ class Batch:
         info = (SolveInfo * len(Bs))()
         check(lib().hodlr_batch_solve(self.h, ptrs, lds, info))
         return list(info)
+
+    def autotune(self):
+        """Per-forest launch shapes by timing; the batch must be factored again."""
+        nf = self.stats()[0]
+        arr = (Tuning * max(nf, 1))()
+        check(lib().hodlr_batch_autotune(self.h, arr, nf))
+        return [arr[i].as_dict() for i in range(nf)]
 
     def stats(self):
         nf, f, s = ctypes.c_int(), ctypes.c_double(), ctypes.c_double()

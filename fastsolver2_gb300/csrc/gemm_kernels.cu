@@ -19,14 +19,53 @@
 #include <algorithm>
 
 #include "kernels.cuh"
+#include "tma.cuh"
 
 namespace hodlr {
+
+// ------------------------------------------------------------ tensor maps
+typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                  const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+static EncodeTiledFn encode_fn() {
+  static EncodeTiledFn fn = [] {
+    void *p = nullptr;
+    cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) !=
+            cudaSuccess ||
+        q != cudaDriverEntryPointSuccess) {
+      (void)cudaGetLastError();
+      return (EncodeTiledFn) nullptr;
+    }
+    return reinterpret_cast<EncodeTiledFn>(p);
+  }();
+  return fn;
+}
+
+bool make_tensor_map_f32(CUtensorMap *map, const float *base, long long rows, long long cols, long long ld,
+                         int box_rows, int box_cols, bool swizzle128) {
+  EncodeTiledFn f = encode_fn();
+  if (!f || !base || rows < 1 || cols < 1) return false;
+  if ((reinterpret_cast<uintptr_t>(base) & 15) || (ld * 4) % 16 || ld < rows) return false;
+  cuuint64_t dims[2] = {(cuuint64_t)rows, (cuuint64_t)cols};
+  cuuint64_t strides[1] = {(cuuint64_t)ld * 4};
+  cuuint32_t box[2] = {(cuuint32_t)box_rows, (cuuint32_t)box_cols};
+  cuuint32_t es[2] = {1, 1};
+  return f(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float *>(base), dims, strides, box, es,
+           CU_TENSOR_MAP_INTERLEAVE_NONE, swizzle128 ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_NONE,
+           CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
 
 // ------------------------------------------------------------------ K3
 // output columns per CTA: 64, or 8 for narrow right-hand sides (C <= 8)
 static inline int red_bn(int C) { return C <= 8 ? 8 : 64; }
 static constexpr int kRedBK = 32;   // rows staged per step
-static constexpr int kRedTargetCTAs = 4 * 152;
+static thread_local const Tuning *g_tuning = nullptr;
+static const Tuning kDefaultTuning{};
+const Tuning &current_tuning() { return g_tuning ? *g_tuning : kDefaultTuning; }
+TuningScope::TuningScope(const Tuning *t) : prev(g_tuning) { g_tuning = t; }
+TuningScope::~TuningScope() { g_tuning = prev; }
 
 template <typename T, int RT, int BN>
 __global__ void __launch_bounds__(256)
@@ -99,6 +138,157 @@ reduce_tn_kernel(const T *__restrict__ A, long long lda, const T *__restrict__ X
   }
 }
 
+// K3, FP32 operands, TMA pipeline.  Each CTA owns one (column tile, row
+// chunk) of one child block and streams its rows in stages of 32: one thread
+// issues two 2-D TMA loads per stage (A: 32 rows x RT ranks, X: 32 rows x 64
+// columns, both landing K-major with the 128-byte swizzle) into a 4-deep ring
+// of shared-memory slots, completing on per-slot mbarriers.  The four 64-thread
+// groups each take 8 of a stage's 32 rows; a thread reads float4 runs of 4
+// rows for its RT/8 ranks (strided by 8: conflict-free under the swizzle) and
+// 8 columns (broadcast within a quarter warp) and accumulates RT/8 x 8
+// outputs.  The groups are summed in a fixed order at the end.
+// Preconditions (checked on the host): block rows and chunk rows multiples
+// of 32, 16-byte aligned bases and leading dimensions.
+static constexpr int kTmaStages = 4;
+
+template <int RT>
+__global__ void __launch_bounds__(256, RT <= 32 ? 2 : 1)
+reduce_tma_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapX,
+                  long long nrows, int r, int C, int chunk_rows, int nchunks, int nct, double *out,
+                  const int *skip, DevStatus *st) {
+  if (skip && *skip) return;
+  constexpr int BN = 64, BK = 32, RPT = RT / 8, CPT = BN / 8;
+  constexpr int A_BYTES = BK * RT * 4, X_BYTES = BK * BN * 4, STAGE = A_BYTES + X_BYTES;
+  extern __shared__ unsigned char smem_raw[];
+  unsigned char *base = reinterpret_cast<unsigned char *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) &
+                                                          ~static_cast<uintptr_t>(1023));
+  __shared__ __align__(8) uint64_t bars[kTmaStages];
+  long long lin = blockIdx.x;
+  const int ct = (int)(lin % nct);
+  lin /= nct;
+  const int chunk = (int)(lin % nchunks);
+  const int b = (int)(lin / nchunks);
+  const int c0 = ct * BN;
+  const long long row0 = (long long)b * nrows + (long long)chunk * chunk_rows;
+  const int rows = (int)min((long long)chunk_rows, nrows - (long long)chunk * chunk_rows);
+  const int nst = rows / BK;
+  const int tid = threadIdx.x, g = tid >> 6, t = tid & 63, tr = t & 7, tc = t >> 3;
+  if (tid == 0) {
+    prefetch_tensormap(&mapA);
+    prefetch_tensormap(&mapX);
+    for (int q = 0; q < kTmaStages; ++q) mbar_init(&bars[q], 1);
+    mbar_fence_init();
+  }
+  __syncthreads();
+  auto issue = [&](int s) {
+    const int slot = s % kTmaStages;
+    unsigned char *sa = base + slot * STAGE;
+    mbar_arrive_expect_tx(&bars[slot], STAGE);
+    tma_load_2d(sa, &mapA, &bars[slot], (int)(row0 + (long long)s * BK), 0);
+    tma_load_2d(sa + A_BYTES, &mapX, &bars[slot], (int)(row0 + (long long)s * BK), c0);
+  };
+  if (tid == 0)
+    for (int s = 0; s < min(kTmaStages, nst); ++s) issue(s);
+  float acc[RPT][CPT];
+#pragma unroll
+  for (int a = 0; a < RPT; ++a)
+#pragma unroll
+    for (int c = 0; c < CPT; ++c) acc[a][c] = 0.f;
+  for (int s = 0; s < nst; ++s) {
+    const int slot = s % kTmaStages;
+    const bool ok = mbar_wait_bounded(&bars[slot], (unsigned)((s / kTmaStages) & 1));
+    if (__syncthreads_or(!ok)) {  // every thread leaves together
+      if (tid == 0) {
+        report_error(st, HODLR_ERR_TIMEOUT, blockIdx.x);
+        for (int q = s; q < min(nst, s + kTmaStages); ++q)  // copies still in flight
+          (void)mbar_wait_bounded(&bars[q % kTmaStages], (unsigned)((q / kTmaStages) & 1));
+      }
+      return;
+    }
+    // every thread has finished stage s-1: its slot can be refilled
+    if (tid == 0 && s >= 1 && s - 1 + kTmaStages < nst) issue(s - 1 + kTmaStages);
+    const unsigned char *sa = base + slot * STAGE, *sx = sa + A_BYTES;
+#pragma unroll
+    for (int kc = 2 * g; kc < 2 * g + 2; ++kc) {
+      float4 av[RPT], xv[CPT];
+#pragma unroll
+      for (int a = 0; a < RPT; ++a) av[a] = *reinterpret_cast<const float4 *>(sa + swz128(tr + 8 * a, kc));
+#pragma unroll
+      for (int c = 0; c < CPT; ++c) xv[c] = *reinterpret_cast<const float4 *>(sx + swz128(tc + 8 * c, kc));
+#pragma unroll
+      for (int a = 0; a < RPT; ++a)
+#pragma unroll
+        for (int c = 0; c < CPT; ++c) {
+          float v = acc[a][c];
+          v = fmaf(av[a].x, xv[c].x, v);
+          v = fmaf(av[a].y, xv[c].y, v);
+          v = fmaf(av[a].z, xv[c].z, v);
+          v = fmaf(av[a].w, xv[c].w, v);
+          acc[a][c] = v;
+        }
+    }
+  }
+  __syncthreads();  // all stages consumed: the ring becomes the group-sum buffer
+  float *sRed = reinterpret_cast<float *>(base);  // [4][RT][BN + 1]
+#pragma unroll
+  for (int a = 0; a < RPT; ++a)
+#pragma unroll
+    for (int c = 0; c < CPT; ++c) sRed[(g * RT + tr + 8 * a) * (BN + 1) + tc + 8 * c] = acc[a][c];
+  __syncthreads();
+  double *o = out + ((long long)b * nchunks + chunk) * r * C;
+  for (int e = tid; e < RT * BN; e += 256) {
+    const int q = e % RT, j = e / RT;
+    if (q >= r || c0 + j >= C) continue;
+    double sum = 0.0;
+#pragma unroll
+    for (int gg = 0; gg < 4; ++gg) sum += (double)sRed[(gg * RT + q) * (BN + 1) + j];
+    o[q + (long long)(c0 + j) * r] = sum;
+  }
+}
+
+template <int RT>
+static size_t reduce_tma_smem() {
+  const size_t ring = (size_t)kTmaStages * 32 * (RT + 64) * 4, red = 4ull * RT * 65 * 4;
+  return std::max(ring, red) + 1024;
+}
+
+template <int RT>
+static cudaError_t reduce_tma_rt(const CUtensorMap &ma, const CUtensorMap &mx, long long nrows, int nbatch, int r,
+                                 int C, int chunk_rows, int nchunks, int nct, double *dst, const int *skip,
+                                 DevStatus *st, cudaStream_t s) {
+  const size_t bytes = reduce_tma_smem<RT>();
+  auto k = reduce_tma_kernel<RT>;
+  static bool attr = false;
+  if (!attr) {
+    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    if (e != cudaSuccess) return e;
+    attr = true;
+  }
+  const long long nblk = (long long)nct * nchunks * nbatch;
+  HODLR_LAUNCH(k, (unsigned)nblk, 256, bytes, s, ma, mx, nrows, r, C, chunk_rows, nchunks, nct, dst, skip, st);
+  return cudaGetLastError();
+}
+
+// The TMA path for FP32 operands, if its preconditions hold (else false).
+static bool reduce_tma_try(const float *A, long long lda, const float *X, long long ldx, long long nrows,
+                           int nbatch, int r, int C, int chunk_rows, int nchunks, double *dst, const int *skip,
+                           DevStatus *st, cudaStream_t s, cudaError_t &err) {
+  if (nrows % 32 || chunk_rows % 32 || C <= 8) return false;
+  const int RT = r <= 16 ? 16 : (r <= 32 ? 32 : 64);
+  const long long total = nrows * nbatch;
+  CUtensorMap ma, mx;
+  if (!make_tensor_map_f32(&ma, A, total, r, lda, 32, RT, true)) return false;
+  if (!make_tensor_map_f32(&mx, X, total, C, ldx, 32, 64, true)) return false;
+  const int nct = ceil_div(C, 64);
+  if (RT == 16)
+    err = reduce_tma_rt<16>(ma, mx, nrows, nbatch, r, C, chunk_rows, nchunks, nct, dst, skip, st, s);
+  else if (RT == 32)
+    err = reduce_tma_rt<32>(ma, mx, nrows, nbatch, r, C, chunk_rows, nchunks, nct, dst, skip, st, s);
+  else
+    err = reduce_tma_rt<64>(ma, mx, nrows, nbatch, r, C, chunk_rows, nchunks, nct, dst, skip, st, s);
+  return true;
+}
+
 __global__ void reduce_pass2_kernel(const double *__restrict__ partial, int nchunks, long long blk,
                                     double *out, const int *skip) {
   if (skip && *skip) return;
@@ -111,20 +301,22 @@ __global__ void reduce_pass2_kernel(const double *__restrict__ partial, int nchu
   out[(long long)b * blk + e] = s;
 }
 
-static void reduce_plan(long long nrows, int nbatch, int C, int &nchunks, int &chunk_rows) {
+// Row chunks per child so that about `target` CTAs run (at least 256 rows each).
+static void reduce_plan(long long nrows, int nbatch, int C, int target, int &nchunks, int &chunk_rows) {
   const int nct = ceil_div(C, red_bn(C));
   const long long base = (long long)nct * nbatch;
   nchunks = 1;
-  if (base < kRedTargetCTAs)
-    nchunks = (int)std::min<long long>(ceil_div(kRedTargetCTAs, base), ceil_div(nrows, 256));
+  if (base < target)
+    nchunks = (int)std::min<long long>(ceil_div(target, base), ceil_div(nrows, 256));
   nchunks = std::max(1, nchunks);
   chunk_rows = (int)std::min<long long>(nrows, (long long)ceil_div(ceil_div(nrows, nchunks), kRedBK) * kRedBK);
   nchunks = ceil_div(nrows, chunk_rows);
 }
 
+// Sized for the largest split-K target the tuner may choose.
 size_t reduce_workspace_doubles(long long nrows, int nbatch, int r, int C, int) {
   int nchunks, chunk_rows;
-  reduce_plan(nrows, nbatch, C, nchunks, chunk_rows);
+  reduce_plan(nrows, nbatch, C, kMaxRedCtasPerSm * kNumSMs, nchunks, chunk_rows);
   return nchunks > 1 ? (size_t)nbatch * nchunks * r * C : 0;
 }
 
@@ -146,15 +338,21 @@ static cudaError_t reduce_rt(const T *A, long long lda, const T *X, long long ld
 template <typename T>
 cudaError_t launch_reduce_tn(const T *A, long long lda, const T *X, long long ldx, long long nrows,
                              int nbatch, int r, int C, double *out, double *work, const int *skip,
-                             cudaStream_t s) {
+                             cudaStream_t s, DevStatus *st) {
   if (C <= 0 || nbatch <= 0) return cudaSuccess;
   if (r < 1 || r > 64) return cudaErrorInvalidValue;
   int nchunks, chunk_rows;
-  reduce_plan(nrows, nbatch, C, nchunks, chunk_rows);
+  reduce_plan(nrows, nbatch, C, current_tuning().red_ctas_per_sm * kNumSMs, nchunks, chunk_rows);
   const int bn = red_bn(C);
   const int nct = ceil_div(C, bn);
   double *dst = nchunks > 1 ? work : out;
-  cudaError_t e;
+  cudaError_t e = cudaSuccess;
+  bool done = false;
+  if constexpr (sizeof(T) == 4)
+    done = reduce_tma_try(A, lda, X, ldx, nrows, nbatch, r, C, chunk_rows, nchunks, dst, skip, st, s, e);
+  if (done) {
+    if (e != cudaSuccess) return e;
+  } else {
 #define HODLR_RED(RTV, BNV) \
   e = reduce_rt<T, RTV, BNV>(A, lda, X, ldx, nrows, nbatch, r, C, chunk_rows, nchunks, nct, dst, skip, s)
   if (bn == 8) {
@@ -168,6 +366,7 @@ cudaError_t launch_reduce_tn(const T *A, long long lda, const T *X, long long ld
   }
 #undef HODLR_RED
   if (e != cudaSuccess) return e;
+  }
   if (nchunks > 1) {
     const long long blk = (long long)r * C;
     dim3 grid(ceil_div(blk, 256), nbatch);
@@ -177,9 +376,10 @@ cudaError_t launch_reduce_tn(const T *A, long long lda, const T *X, long long ld
 }
 
 template cudaError_t launch_reduce_tn<double>(const double *, long long, const double *, long long, long long,
-                                              int, int, int, double *, double *, const int *, cudaStream_t);
+                                              int, int, int, double *, double *, const int *, cudaStream_t,
+                                              DevStatus *);
 template cudaError_t launch_reduce_tn<float>(const float *, long long, const float *, long long, long long, int,
-                                             int, int, double *, double *, const int *, cudaStream_t);
+                                             int, int, double *, double *, const int *, cudaStream_t, DevStatus *);
 
 // ------------------------------------------------------------------ K5
 // CTA tile 128 rows x 64 columns, K staged 32 at a time; each thread owns
@@ -257,9 +457,158 @@ __global__ void __launch_bounds__(256) update_nn_kernel(UpdateArgs a, int nrt, i
   }
 }
 
+// K5, FP32, TMA: one CTA per (BM-row x 64-column) tile of a block.  Thread 0
+// issues the A tile (BM rows x KMAX ranks) and the C tile (BM x 64) as 2-D
+// TMA loads on two mbarriers; meanwhile all threads stage op(B_b) (FP64 eta,
+// scaled, rounded to FP32) into shared memory.  Each thread owns float4 runs
+// of rows (4 tr + 64 g) and 4 columns; the product is added to the C tile in
+// shared memory, which thread 0 writes back with one TMA store (rows and
+// columns beyond the tensor are clipped by the copy engine).
+// Preconditions (host-checked): A not transposed, blocks of exactly M rows at
+// stride M in A and C, M a multiple of BM, K <= KMAX, 16-byte alignment.
+template <int BM, int KMAX>
+__global__ void __launch_bounds__(256)
+update_tma_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapC, UpdateArgs a,
+                  int nrt, int nct, DevStatus *st) {
+  if (a.skip && *a.skip) return;
+  constexpr int BN = 64, RG = BM / 64;
+  extern __shared__ unsigned char smem_raw[];
+  float *base = reinterpret_cast<float *>((reinterpret_cast<uintptr_t>(smem_raw) + 127) &
+                                          ~static_cast<uintptr_t>(127));
+  float *sC = base;                 // [BN][BM]
+  float *sA = sC + BN * BM;         // [KMAX][BM]
+  float *sB = sA + KMAX * BM;       // [KMAX][BN]
+  __shared__ __align__(8) uint64_t bars[2];
+  long long lin = blockIdx.x;
+  const int rt = (int)(lin % nrt);
+  lin /= nrt;
+  const int ct = (int)(lin % nct);
+  const int b = (int)(lin / nct);
+  const int i0 = rt * BM, j0 = ct * BN;
+  const long long rowA = (long long)b * a.a_bstride + i0, rowC = (long long)b * a.c_bstride + i0;
+  const int tid = threadIdx.x, tr = tid & 15, tc = tid >> 4;
+  if (tid == 0) {
+    prefetch_tensormap(&mapA);
+    prefetch_tensormap(&mapC);
+    mbar_init(&bars[0], 1);
+    mbar_init(&bars[1], 1);
+    mbar_fence_init();
+  }
+  __syncthreads();
+  if (tid == 0) {
+    mbar_arrive_expect_tx(&bars[0], KMAX * BM * 4);
+    tma_load_2d(sA, &mapA, &bars[0], (int)rowA, 0);
+    mbar_arrive_expect_tx(&bars[1], BN * BM * 4);
+    tma_load_2d(sC, &mapC, &bars[1], (int)rowC, j0);
+  }
+  const double *B = a.B + (long long)(b >> 1) * a.b_s1 + (long long)((b & 1) ^ a.b_flip) * a.b_s2;
+  for (int e = tid; e < KMAX * BN; e += 256) {
+    const int q = e / BN, j = e % BN;
+    float v = 0.f;
+    if (q < a.K && j0 + j < a.N) {
+      double x = a.b_trans ? B[(j0 + j) + (long long)q * a.ldb] : B[q + (long long)(j0 + j) * a.ldb];
+      if (a.scale) x *= a.scale_cols ? a.scale[j0 + j] : a.scale[q];
+      v = (float)x;
+    }
+    sB[e] = v;
+  }
+  bool ok = mbar_wait_bounded(&bars[0], 0);
+  if (__syncthreads_or(!ok)) {
+    if (tid == 0) {
+      report_error(st, HODLR_ERR_TIMEOUT, blockIdx.x);
+      (void)mbar_wait_bounded(&bars[1], 0);
+    }
+    return;
+  }
+  float acc[RG * 4][4];
+#pragma unroll
+  for (int u = 0; u < RG * 4; ++u)
+#pragma unroll
+    for (int v = 0; v < 4; ++v) acc[u][v] = 0.f;
+#pragma unroll 4
+  for (int q = 0; q < a.K; ++q) {
+    const float4 bv = *reinterpret_cast<const float4 *>(sB + q * BN + 4 * tc);
+#pragma unroll
+    for (int g = 0; g < RG; ++g) {
+      const float4 av = *reinterpret_cast<const float4 *>(sA + q * BM + 64 * g + 4 * tr);
+      const float ar[4] = {av.x, av.y, av.z, av.w}, br[4] = {bv.x, bv.y, bv.z, bv.w};
+#pragma unroll
+      for (int ii = 0; ii < 4; ++ii)
+#pragma unroll
+        for (int jj = 0; jj < 4; ++jj) acc[g * 4 + ii][jj] = fmaf(ar[ii], br[jj], acc[g * 4 + ii][jj]);
+    }
+  }
+  ok = mbar_wait_bounded(&bars[1], 0);
+  if (__syncthreads_or(!ok)) {
+    if (tid == 0) report_error(st, HODLR_ERR_TIMEOUT, blockIdx.x);
+    return;
+  }
+  const float alpha = (float)a.alpha;
+#pragma unroll
+  for (int jj = 0; jj < 4; ++jj)
+#pragma unroll
+    for (int g = 0; g < RG; ++g) {
+      float4 *c = reinterpret_cast<float4 *>(sC + (4 * tc + jj) * BM + 64 * g + 4 * tr);
+      float4 v = *c;
+      v.x = fmaf(alpha, acc[g * 4 + 0][jj], v.x);
+      v.y = fmaf(alpha, acc[g * 4 + 1][jj], v.y);
+      v.z = fmaf(alpha, acc[g * 4 + 2][jj], v.z);
+      v.w = fmaf(alpha, acc[g * 4 + 3][jj], v.w);
+      *c = v;
+    }
+  fence_proxy_async_smem();
+  __syncthreads();
+  if (tid == 0) {
+    tma_store_2d(&mapC, sC, (int)rowC, j0);
+    tma_store_commit();
+    tma_store_wait_all();
+  }
+}
+
+template <int BM, int KMAX>
+static cudaError_t update_tma_launch(const CUtensorMap &ma, const CUtensorMap &mc, const UpdateArgs &a, int nrt,
+                                     int nct, DevStatus *st, cudaStream_t s) {
+  const size_t bytes = sizeof(float) * ((size_t)64 * BM + (size_t)KMAX * BM + (size_t)KMAX * 64) + 128;
+  auto k = update_tma_kernel<BM, KMAX>;
+  static bool attr = false;
+  if (!attr) {
+    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    if (e != cudaSuccess) return e;
+    attr = true;
+  }
+  const long long nblk = (long long)nrt * nct * a.nbatch;
+  HODLR_LAUNCH(k, (unsigned)nblk, 256, bytes, s, ma, mc, a, nrt, nct, st);
+  return cudaGetLastError();
+}
+
+static bool update_tma_try(const UpdateArgs &a, DevStatus *st, cudaStream_t s, cudaError_t &err) {
+  if (a.a_trans || a.K < 1 || a.K > 64 || a.a_bstride != a.M || a.c_bstride != a.M) return false;
+  const int want = current_tuning().upd_bm;
+  int BM = a.M % 128 == 0 ? 128 : (a.M % 64 == 0 ? 64 : 0);
+  if (want == 64 && a.M % 64 == 0) BM = 64;
+  if (!BM) return false;
+  const int KMAX = a.K <= 32 ? 32 : 64;
+  const long long rows = (long long)a.M * a.nbatch;
+  CUtensorMap ma, mc;
+  if (!make_tensor_map_f32(&ma, static_cast<const float *>(a.A), rows, a.K, a.lda, BM, KMAX, false)) return false;
+  if (!make_tensor_map_f32(&mc, static_cast<const float *>(a.C), rows, a.N, a.ldc, BM, 64, false)) return false;
+  const int nrt = a.M / BM, nct = ceil_div(a.N, 64);
+  if (BM == 128)
+    err = KMAX == 32 ? update_tma_launch<128, 32>(ma, mc, a, nrt, nct, st, s)
+                     : update_tma_launch<128, 64>(ma, mc, a, nrt, nct, st, s);
+  else
+    err = KMAX == 32 ? update_tma_launch<64, 32>(ma, mc, a, nrt, nct, st, s)
+                     : update_tma_launch<64, 64>(ma, mc, a, nrt, nct, st, s);
+  return true;
+}
+
 template <typename T>
-cudaError_t launch_update_nn(const UpdateArgs &a, cudaStream_t s) {
+cudaError_t launch_update_nn(const UpdateArgs &a, cudaStream_t s, DevStatus *st) {
   if (a.M <= 0 || a.N <= 0 || a.nbatch <= 0) return cudaSuccess;
+  if constexpr (sizeof(T) == 4) {
+    cudaError_t e = cudaSuccess;
+    if (update_tma_try(a, st, s, e)) return e;
+  }
   const int nrt = ceil_div(a.M, kUpdBM), nct = ceil_div(a.N, kUpdBN);
   const long long nblk = (long long)nrt * nct * a.nbatch;
   if (a.K <= 8)
@@ -268,7 +617,7 @@ cudaError_t launch_update_nn(const UpdateArgs &a, cudaStream_t s) {
     HODLR_LAUNCH((update_nn_kernel<T, 32>), (unsigned)nblk, 256, 0, s, a, nrt, nct);
   return cudaGetLastError();
 }
-template cudaError_t launch_update_nn<double>(const UpdateArgs &, cudaStream_t);
-template cudaError_t launch_update_nn<float>(const UpdateArgs &, cudaStream_t);
+template cudaError_t launch_update_nn<double>(const UpdateArgs &, cudaStream_t, DevStatus *);
+template cudaError_t launch_update_nn<float>(const UpdateArgs &, cudaStream_t, DevStatus *);
 
 }  // namespace hodlr

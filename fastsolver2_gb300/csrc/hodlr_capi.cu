@@ -175,6 +175,7 @@ struct hodlr_ctx {
   int *seg_leaf = nullptr;  // device [nsys + 1]
   bool forest = false;
   double *sfold = nullptr;  // forest: device copy of one level's s, folded into V
+  Tuning tune;              // launch shapes of the tunable kernels (hodlr_autotune)
 };
 
 static void clear_graphs(hodlr_ctx *h) {
@@ -427,7 +428,7 @@ template <typename T> static int factor_sweep(hodlr_ctx *h) {
     const long long rows = h->rows(l);
     const int Cd = l * r, Ct = Cd + r;
     PHASE(h, HODLR_PHASE_REDUCE,
-          launch_reduce_tn<T>(Vt + (long long)l * n * r, n, Ut, n, rows, nb, r, Ct, h->Tbuf, h->red, nullptr, s));
+          launch_reduce_tn<T>(Vt + (long long)l * n * r, n, Ut, n, rows, nb, r, Ct, h->Tbuf, h->red, nullptr, s, h->dst));
     CapFactorArgs cf{};
     cf.Tb = h->Tbuf;
     cf.tb_stride = (long long)r * Ct;
@@ -460,7 +461,7 @@ template <typename T> static int factor_sweep(hodlr_ctx *h) {
       ua.K = r;
       ua.nbatch = nb;
       ua.alpha = -1.0;
-      PHASE(h, HODLR_PHASE_UPDATE, launch_update_nn<T>(ua, s));
+      PHASE(h, HODLR_PHASE_UPDATE, launch_update_nn<T>(ua, s, h->dst));
     }
   }
   return HODLR_OK;
@@ -481,7 +482,7 @@ static int solve_sweep(hodlr_ctx *h, T *X, long long ldx, int k, bool trans, con
     const long long rows = h->rows(l);
     const T *Ared = trans ? Ut + (long long)l * r * n : Vt + (long long)l * n * r;
     const T *Aupd = trans ? Vt + (long long)l * n * r : Ut + (long long)l * r * n;
-    PHASE(h, HODLR_PHASE_REDUCE, launch_reduce_tn<T>(Ared, n, X, ldx, rows, nb, r, k, h->Tbuf, h->red, skip, s));
+    PHASE(h, HODLR_PHASE_REDUCE, launch_reduce_tn<T>(Ared, n, X, ldx, rows, nb, r, k, h->Tbuf, h->red, skip, s, h->dst));
     CKS(cap_apply(h, l, k, (long long)r * k, trans, skip));
     UpdateArgs ua{};
     ua.A = Aupd;
@@ -502,7 +503,7 @@ static int solve_sweep(hodlr_ctx *h, T *X, long long ldx, int k, bool trans, con
     ua.nbatch = nb;
     ua.alpha = -1.0;
     ua.skip = skip;
-    PHASE(h, HODLR_PHASE_UPDATE, launch_update_nn<T>(ua, s));
+    PHASE(h, HODLR_PHASE_UPDATE, launch_update_nn<T>(ua, s, h->dst));
   }
   if (trans) CKS(leaf_solve<T>(h, X, ldx, k, true, skip));
   return HODLR_OK;
@@ -932,6 +933,7 @@ int hodlr_set_lowrank(hodlr_handle h, int level, const double *U, int64_t ldu, c
 
 int hodlr_factor(hodlr_handle h) {
   if (!h) return set_err(HODLR_ERR_INVALID_ARG, "null handle");
+  TuningScope tscope(&h->tune);
   if (!h->has_D) return set_err(HODLR_ERR_NOT_FACTORED, "leaf blocks not set");
   for (int l = 0; l < h->L; ++l)
     if (!h->has_level[l]) return set_err(HODLR_ERR_NOT_FACTORED, "low-rank level not set");
@@ -954,6 +956,7 @@ int hodlr_factor(hodlr_handle h) {
 
 static int solve_impl(hodlr_handle h, double *B, int64_t ldb, int nrhs, hodlr_solve_info *info, bool trans) {
   if (!h || !B) return set_err(HODLR_ERR_INVALID_ARG, "null argument");
+  TuningScope tscope(&h->tune);
   if (!h->factored) return set_err(HODLR_ERR_NOT_FACTORED, "call hodlr_factor first");
   if (nrhs < 1 || nrhs > h->kmax) return set_err(HODLR_ERR_INVALID_ARG, "nrhs out of range");
   if (ldb < h->n) return set_err(HODLR_ERR_INVALID_ARG, "ldb < n");
@@ -1002,6 +1005,7 @@ int hodlr_solve_transpose(hodlr_handle h, double *B, int64_t ldb, int nrhs, hodl
 
 int hodlr_matvec(hodlr_handle h, int transpose, const double *X, int64_t ldx, double *Y, int64_t ldy, int nrhs) {
   if (!h || !X || !Y) return set_err(HODLR_ERR_INVALID_ARG, "null argument");
+  TuningScope tscope(&h->tune);
   if (nrhs < 1 || nrhs > h->kmax) return set_err(HODLR_ERR_INVALID_ARG, "nrhs out of range");
   if (ldx < h->n || ldy < h->n) return set_err(HODLR_ERR_INVALID_ARG, "ld < n");
   CKS(reset_status(h));
@@ -1012,6 +1016,7 @@ int hodlr_matvec(hodlr_handle h, int transpose, const double *X, int64_t ldx, do
 int hodlr_adjoint(hodlr_handle h, const double *x, int64_t ldx, const double *g, int64_t ldg, int nrhs,
                   hodlr_grads *gr) {
   if (!h || !x || !g || !gr) return set_err(HODLR_ERR_INVALID_ARG, "null argument");
+  TuningScope tscope(&h->tune);
   if (!h->factored) return set_err(HODLR_ERR_NOT_FACTORED, "call hodlr_factor first");
   if (nrhs < 1 || nrhs > h->kmax) return set_err(HODLR_ERR_INVALID_ARG, "nrhs out of range");
   const long long n = h->n;
@@ -1173,6 +1178,7 @@ int hodlr_last_timings(hodlr_handle h, double *factor_ms, double *solve_ms) {
 int hodlr_generate(hodlr_handle h, uint64_t seed, double shift, int orthonormal, double decay, double *B,
                    int64_t ldb, int nrhs) {
   if (!h) return set_err(HODLR_ERR_INVALID_ARG, "null handle");
+  TuningScope tscope(&h->tune);
   const long long n = h->n;
   const int m = h->m, L = h->L, r = h->r;
   cudaStream_t s = h->st;
@@ -1595,7 +1601,10 @@ static int batch_forked(hodlr_batch_ctx *b, F body) {
   CK(cudaEventRecord(b->fork, b->st));
   for (auto &f : b->forests) {
     CK(cudaStreamWaitEvent(f.h->st, b->fork, 0));
-    CKS(body(f));
+    {
+      TuningScope tscope(&f.h->tune);
+      CKS(body(f));
+    }
     CK(cudaEventRecord(f.join, f.h->st));
     CK(cudaStreamWaitEvent(b->st, f.join, 0));
   }
@@ -1937,6 +1946,151 @@ int hodlr_batch_stats(hodlr_batch b, int *nforests, double *factor_ms, double *s
   if (factor_ms) *factor_ms = b->factor_ms;
   if (solve_ms) *solve_ms = b->solve_ms;
   return HODLR_OK;
+}
+
+}  // extern "C"
+
+// ================================================================ autotuner
+// Coordinate search over the tunable launch shapes (split-K target of the
+// row reductions, FP32 update tile rows), timing complete factor + solve
+// sweeps on the handle's own inputs with a seeded scratch right-hand side.
+static const int kRedCands[] = {2, 4, 8};
+static const int kUpdCands[] = {0, 64};
+
+template <typename Measure>
+static int tune_search(Tuning &cur, double &cur_ms, Measure measure) {
+  CKS(measure(cur, cur_ms));
+  for (int red : kRedCands) {
+    if (red == cur.red_ctas_per_sm) continue;
+    Tuning t = cur;
+    t.red_ctas_per_sm = red;
+    double ms = 0.0;
+    CKS(measure(t, ms));
+    if (ms < cur_ms) cur = t, cur_ms = ms;
+  }
+  for (int bm : kUpdCands) {
+    if (bm == cur.upd_bm) continue;
+    Tuning t = cur;
+    t.upd_bm = bm;
+    double ms = 0.0;
+    CKS(measure(t, ms));
+    if (ms < cur_ms) cur = t, cur_ms = ms;
+  }
+  return HODLR_OK;
+}
+
+static bool valid_tuning(const hodlr_tuning &t) {
+  return (t.red_ctas_per_sm == 2 || t.red_ctas_per_sm == 4 || t.red_ctas_per_sm == 8) &&
+         (t.update_tile_rows == 0 || t.update_tile_rows == 64 || t.update_tile_rows == 128);
+}
+
+extern "C" {
+
+int hodlr_set_tuning(hodlr_handle h, const hodlr_tuning *t) {
+  if (!h || !t || !valid_tuning(*t)) return set_err(HODLR_ERR_INVALID_ARG, "bad tuning");
+  h->tune.red_ctas_per_sm = t->red_ctas_per_sm;
+  h->tune.upd_bm = t->update_tile_rows == 128 ? 0 : t->update_tile_rows;
+  clear_graphs(h);
+  h->factored = false;
+  return HODLR_OK;
+}
+
+int hodlr_get_tuning(hodlr_handle h, hodlr_tuning *t) {
+  if (!h || !t) return set_err(HODLR_ERR_INVALID_ARG, "null argument");
+  t->red_ctas_per_sm = h->tune.red_ctas_per_sm;
+  t->update_tile_rows = h->tune.upd_bm;
+  t->ms = -1.0;
+  return HODLR_OK;
+}
+
+int hodlr_autotune(hodlr_handle h, int nrhs, hodlr_tuning *best) {
+  if (!h) return set_err(HODLR_ERR_INVALID_ARG, "null handle");
+  if (nrhs < 1 || nrhs > h->kmax) return set_err(HODLR_ERR_INVALID_ARG, "nrhs out of range");
+  if (!h->has_D) return set_err(HODLR_ERR_NOT_FACTORED, "leaf blocks not set");
+  for (int l = 0; l < h->L; ++l)
+    if (!h->has_level[l]) return set_err(HODLR_ERR_NOT_FACTORED, "low-rank level not set");
+  const long long n = h->n;
+  double *B = nullptr;
+  CK(cudaMalloc(&B, sizeof(double) * n * nrhs));
+  auto measure = [&](const Tuning &t, double &ms) -> int {
+    h->tune = t;
+    clear_graphs(h);
+    for (int rep = 0; rep < 3; ++rep) {  // eager, captured, replayed: the last is timed
+      CK(launch_gaussian(B, n, n, nrhs, 0x5eedull, 0x7ull, 1.0, h->st));
+      CKS(hodlr_factor(h));
+      hodlr_solve_info info;
+      const int rc = solve_impl(h, B, n, nrhs, &info, false);
+      if (rc != HODLR_OK && rc != HODLR_ERR_NOT_CONVERGED) return rc;
+    }
+    ms = (double)h->factor_ms + (double)h->solve_ms;
+    return HODLR_OK;
+  };
+  Tuning cur = h->tune;
+  double cur_ms = 0.0;
+  int rc = tune_search(cur, cur_ms, measure);
+  cudaFree(B);
+  CKS(rc);
+  h->tune = cur;
+  clear_graphs(h);
+  h->factored = false;
+  CKS(hodlr_factor(h));  // leave the handle factored with the chosen shapes
+  if (best) {
+    best->red_ctas_per_sm = cur.red_ctas_per_sm;
+    best->update_tile_rows = cur.upd_bm;
+    best->ms = cur_ms;
+  }
+  return HODLR_OK;
+}
+
+int hodlr_batch_autotune(hodlr_batch b, hodlr_tuning *per_forest, int capacity) {
+  if (!b) return set_err(HODLR_ERR_INVALID_ARG, "batch: null handle");
+  for (int i = 0; i < (int)b->sys.size(); ++i) {
+    bool ok = b->mem[i].has_D;
+    for (char c : b->mem[i].has_level) ok = ok && c;
+    if (!ok) return set_err(HODLR_ERR_NOT_FACTORED, "batch: inputs not set");
+  }
+  for (size_t fi = 0; fi < b->forests.size(); ++fi) {
+    hodlr_ctx *h = b->forests[fi].h;
+    const long long n = h->n;
+    const int k = h->kmax;
+    double *B = nullptr;
+    CK(cudaMalloc(&B, sizeof(double) * n * k));
+    auto measure = [&](const Tuning &t, double &ms) -> int {
+      h->tune = t;
+      TuningScope tscope(&h->tune);
+      for (int rep = 0; rep < 2; ++rep) {  // the second run is timed
+        CK(launch_gaussian(B, n, n, k, 0x5eedull, 0x7ull, 1.0, h->st));
+        CK(cudaEventRecord(b->ev[0], h->st));
+        CKS(reset_status(h));
+        CKS(h->mixed ? factor_sweep<float>(h) : factor_sweep<double>(h));
+        CKS(h->mixed ? mixed_solve(h, B, n, k, false) : solve_sweep<double>(h, B, n, k, false, nullptr));
+        CK(cudaEventRecord(b->ev[1], h->st));
+        CK(cudaStreamSynchronize(h->st));
+      }
+      float f = 0.f;
+      CK(cudaEventElapsedTime(&f, b->ev[0], b->ev[1]));
+      ms = f;
+      return HODLR_OK;
+    };
+    Tuning cur = h->tune;
+    double cur_ms = 0.0;
+    int rc = tune_search(cur, cur_ms, measure);
+    cudaFree(B);
+    CKS(rc);
+    h->tune = cur;
+    if (per_forest && (int)fi < capacity) {
+      per_forest[fi].red_ctas_per_sm = cur.red_ctas_per_sm;
+      per_forest[fi].update_tile_rows = cur.upd_bm;
+      per_forest[fi].ms = cur_ms;
+    }
+  }
+  for (GraphEntry *g : {&b->factor_graph, &b->solve_graph}) {
+    if (g->exec) cudaGraphExecDestroy(g->exec);
+    *g = GraphEntry();
+  }
+  b->factor_runs = b->solve_runs = 0;
+  b->factored = false;
+  return (int)b->forests.size() > 0 ? HODLR_OK : HODLR_OK;
 }
 
 }  // extern "C"

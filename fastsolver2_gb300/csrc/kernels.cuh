@@ -8,6 +8,23 @@ namespace hodlr {
 // Record the message returned by hodlr_last_error_string(); returns code.
 int set_last_error(int code, const char *msg);
 
+// Launch-shape choices of the tunable kernels, chosen per handle (per forest
+// of a batch) by the autotuner.  Launches made by a host thread use the
+// choices of the innermost live TuningScope on that thread (defaults
+// otherwise).
+struct Tuning {
+  int red_ctas_per_sm = 4;  // split-K target of the row reductions, CTAs per SM (2, 4 or 8)
+  int upd_bm = 0;           // FP32 update tile rows: 0 = 128 when the block allows, else 64
+};
+constexpr int kMaxRedCtasPerSm = 8;
+constexpr int kNumSMs = 152;
+const Tuning &current_tuning();
+struct TuningScope {
+  const Tuning *prev;
+  explicit TuningScope(const Tuning *t);
+  ~TuningScope();
+};
+
 // ------------------------------------------------------------------ leaves
 // K1: LU with partial pivoting of every leaf block.  D: leaf i at
 // D + i*d_stride (FP64, column-major, ld d_ld).  LU: packed [nleaf][m][m]
@@ -37,7 +54,7 @@ size_t reduce_workspace_doubles(long long nrows, int nbatch, int r, int C, int e
 template <typename T>
 cudaError_t launch_reduce_tn(const T *A, long long lda, const T *X, long long ldx, long long nrows,
                              int nbatch, int r, int C, double *out, double *work, const int *skip,
-                             cudaStream_t s);
+                             cudaStream_t s, DevStatus *st = nullptr);
 
 // K5: C_b += alpha * A_b * diag(scale) * op(B_b) for b in [0, nbatch):
 //   A_b = A + b*a_bstride (M x K, lda), C_b = C + b*c_bstride (M x N, ldc),
@@ -55,7 +72,7 @@ struct UpdateArgs {
   const int *skip;
 };
 template <typename T>
-cudaError_t launch_update_nn(const UpdateArgs &a, cudaStream_t s);
+cudaError_t launch_update_nn(const UpdateArgs &a, cudaStream_t s, DevStatus *st = nullptr);
 
 // Explicit inverses of the leaf blocks from their LU factors ([nleaf][m][m]).
 template <typename T>

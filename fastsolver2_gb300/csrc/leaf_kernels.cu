@@ -62,7 +62,7 @@ leaf_getrf_kernel(const double *__restrict__ D, long long d_ld, long long d_stri
 // Leaf LU (+ optional explicit inverse) with the block resident in registers
 // (reg_factor.cuh), for M in {32, 64, 128}.
 template <typename T, int M>
-__global__ void __launch_bounds__(256, 1)
+__global__ void __launch_bounds__(256, (sizeof(T) == 4 && M == 128) ? 2 : 1)
 leaf_factor_reg_kernel(const double *__restrict__ D, long long d_ld, long long d_stride, T *LU, int *ipiv,
                        DevStatus *st, T *Dinv) {
   extern __shared__ __align__(16) unsigned char smem_raw[];

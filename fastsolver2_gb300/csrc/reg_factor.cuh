@@ -8,12 +8,16 @@
 // memory accesses per FMA in a shared-memory-resident elimination.
 //
 // Pivoting follows LAPACK (first row of maximal |a| in the column, rows
-// >= k; netlib_blas/idamax.f:52, dgetf2 semantics): the LU factors and the
-// 1-based pivots are written in the DGETRF layout, then the block is
-// reloaded and inverted by Gauss-Jordan elimination with the same pivot rule
-// (its pivot search covers the LU's Schur-complement rows, so the pivot
-// sequence is the same), and the inverse is written with the column
-// interchanges undone.
+// >= k; netlib_blas/idamax.f:52, dgetf2 semantics).  When the inverse is
+// wanted, one Gauss-Jordan sweep produces both: at step k the multipliers
+// l_i = a_ik / a_kk (scaled as dgetf2 scales, by the reciprocal unless the
+// pivot is tiny) eliminate column k from every other row with the unscaled
+// pivot row, so rows >= k see exactly the operations of a right-looking LU
+// and the LU factors (row k of U, column k of L) are captured as they appear
+// into shared memory, where later row interchanges are applied to the L
+// columns already captured (DGETRF's layout); the rows above k carry the
+// inverse.  Without the inverse a plain right-looking LU runs.  The inverse
+// is written with the column interchanges undone.
 #pragma once
 #include "dense_ops.cuh"
 
@@ -111,7 +115,7 @@ __device__ void reg_factor(Load load, T *buf, T *lu_out, int *ipiv_out, StoreInv
   };
 
   // ------------------------------------------------------------- LU
-  if (lu_out || ipiv_out) {
+  if (!want_inv && (lu_out || ipiv_out)) {
     fill();
     for (int kb = 0; kb < 16; ++kb) {
 #pragma unroll
@@ -159,7 +163,8 @@ __device__ void reg_factor(Load load, T *buf, T *lu_out, int *ipiv_out, StoreInv
   }
   // ------------------------------------------------------------- Gauss-Jordan
   if (want_inv) {
-    fill();
+    const bool capture = lu_out != nullptr;
+    fill();  // buf is free from here on: it collects the LU factors
     for (int kb = 0; kb < 16; ++kb) {
 #pragma unroll
       for (int kk = 0; kk < TB; ++kk) {
@@ -170,23 +175,39 @@ __device__ void reg_factor(Load load, T *buf, T *lu_out, int *ipiv_out, StoreInv
         __syncthreads();
         pivot(k);
         const int p = s_p;
-        if (tid == 0) perm[k] = p;
+        if (tid == 0) {
+          perm[k] = p;
+          if (ipiv_out) ipiv_out[k] = p + 1;
+          if (colbuf[p] == T(0) && s_info == 0) s_info = k + 1;
+        }
         swap_rows(kb, kk, p);
-        // column k after the swap, then eliminate it from every other row
+        // the interchange also applies to the L columns captured so far
+        if (capture && p != k)
+          for (int j = tid; j < k; j += 256) {
+            const T t = buf[k + j * M];
+            buf[k + j * M] = buf[p + j * M];
+            buf[p + j * M] = t;
+          }
+        const T pv = rowb[k];
+        // multipliers of column k (dgetf2 scaling), captured below the diagonal
         if (tx == kb)
 #pragma unroll
-          for (int i = 0; i < TB; ++i) colbuf[ty * TB + i] = a[i][kk];
+          for (int i = 0; i < TB; ++i) {
+            const int gi = ty * TB + i;
+            T l = a[i][kk];
+            if (gi != k && pv != T(0)) l = dabs(pv) >= safe_min<T>() ? l * (T(1) / pv) : l / pv;
+            colbuf[gi] = l;
+            if (capture && gi > k) buf[gi + k * M] = l;
+          }
+        if (capture)
+          for (int j = k + tid; j < M; j += 256) buf[k + j * M] = rowb[j];  // row k of U
         __syncthreads();
-        const T piv = rowb[k];
-        const T d = piv != T(0) ? T(1) / piv : T(0);
-        T cv[TB], rs[TB];
+        const T d = pv != T(0) ? T(1) / pv : T(0);
+        T cv[TB], rv[TB];
 #pragma unroll
         for (int i = 0; i < TB; ++i) cv[i] = colbuf[ty * TB + i];
 #pragma unroll
-        for (int j = 0; j < TB; ++j) {
-          const int gj = tx * TB + j;
-          rs[j] = (gj == k) ? d : rowb[gj] * d;
-        }
+        for (int j = 0; j < TB; ++j) rv[j] = rowb[tx * TB + j];
 #pragma unroll
         for (int i = 0; i < TB; ++i) {
           const int gi = ty * TB + i;
@@ -194,13 +215,17 @@ __device__ void reg_factor(Load load, T *buf, T *lu_out, int *ipiv_out, StoreInv
           for (int j = 0; j < TB; ++j) {
             const int gj = tx * TB + j;
             if (gi == k)
-              a[i][j] = rs[j];
+              a[i][j] = (gj == k) ? d : rv[j] * d;
             else
-              a[i][j] = (gj == k) ? -cv[i] * d : a[i][j] - cv[i] * rs[j];
+              a[i][j] = (gj == k) ? -cv[i] : a[i][j] - cv[i] * rv[j];
           }
         }
         __syncthreads();
       }
+    }
+    if (capture) {
+      for (int e = tid; e < M * M; e += 256) lu_out[e] = buf[e];
+      __syncthreads();
     }
     stage();
     // the row interchanges become column interchanges of the inverse

@@ -123,7 +123,7 @@ cudaError_t launch_scale_split(const double *T, const double *scale, int r, long
 }
 
 // ------------------------------------------------------------------ reduce
-static constexpr int kCT = 32, kBK = 32, kTarget = 4 * 152;
+static constexpr int kCT = 32, kBK = 32;
 
 template <int RT>
 __global__ void __launch_bounds__(256)
@@ -201,11 +201,11 @@ __global__ void dw_pass2_kernel(const double *__restrict__ partial, int nchunks,
   out[(long long)b * blk + e] = s;
 }
 
-static void plan(long long nrows, int nbatch, int C, int &nchunks, int &chunk_rows) {
+static void plan(long long nrows, int nbatch, int C, int target, int &nchunks, int &chunk_rows) {
   const int nct = ceil_div(C, kCT);
   const long long base = (long long)nct * nbatch;
   nchunks = 1;
-  if (base < kTarget) nchunks = (int)std::min<long long>(ceil_div(kTarget, base), ceil_div(nrows, 256));
+  if (base < target) nchunks = (int)std::min<long long>(ceil_div(target, base), ceil_div(nrows, 256));
   nchunks = std::max(1, nchunks);
   chunk_rows = (int)std::min<long long>(nrows, (long long)ceil_div(ceil_div(nrows, nchunks), kBK) * kBK);
   nchunks = ceil_div(nrows, chunk_rows);
@@ -213,7 +213,7 @@ static void plan(long long nrows, int nbatch, int C, int &nchunks, int &chunk_ro
 
 size_t dw_reduce_workspace_doubles(long long nrows, int nbatch, int r, int C) {
   int nchunks, chunk_rows;
-  plan(nrows, nbatch, C, nchunks, chunk_rows);
+  plan(nrows, nbatch, C, kMaxRedCtasPerSm * kNumSMs, nchunks, chunk_rows);
   return nchunks > 1 ? (size_t)nbatch * nchunks * r * C : 0;
 }
 
@@ -223,7 +223,7 @@ cudaError_t launch_dw_reduce(const float2 *A, long long lda, const float2 *X, lo
   if (C <= 0 || nbatch <= 0) return cudaSuccess;
   if (r < 1 || r > 64) return cudaErrorInvalidValue;
   int nchunks, chunk_rows;
-  plan(nrows, nbatch, C, nchunks, chunk_rows);
+  plan(nrows, nbatch, C, current_tuning().red_ctas_per_sm * kNumSMs, nchunks, chunk_rows);
   const int nct = ceil_div(C, kCT);
   double *dst = nchunks > 1 ? work : out;
   const long long nblk = (long long)nct * nchunks * nbatch;

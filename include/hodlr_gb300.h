@@ -323,6 +323,29 @@ HODLR_API int hodlr_batch_solve(hodlr_batch b, double *const *B, const int64_t *
  * hodlr_batch_factor / hodlr_batch_solve. */
 HODLR_API int hodlr_batch_stats(hodlr_batch b, int *nforests, double *factor_ms, double *solve_ms);
 
+/* ------------------------------------------------------------ autotuner
+ * Launch shapes of the tunable kernels: the split-K target of the row
+ * reductions (CTAs per SM) and the row tile of the FP32 low-rank update.
+ * No counterpart in the reference (its BLAS calls have no launch shapes).
+ * hodlr_autotune times complete factor + solve sweeps of the handle's own
+ * inputs (a seeded scratch right-hand side of nrhs columns) for a coordinate
+ * search over the candidates, keeps the fastest and leaves the handle
+ * factored with it; choices change only rounding, not the algorithm.  Its
+ * result can be cached by the caller and restored with hodlr_set_tuning
+ * (which invalidates the factorisation).  hodlr_batch_autotune does the same
+ * per forest (systems sharing leaf size and rank); the batch must be
+ * factored again afterwards. */
+typedef struct hodlr_tuning {
+  int32_t red_ctas_per_sm;   /* 2, 4 or 8 */
+  int32_t update_tile_rows;  /* 0 (128 where the blocks allow it, else 64) or 64 */
+  double ms;                 /* autotune: factor + solve milliseconds with these shapes */
+} hodlr_tuning;
+
+HODLR_API int hodlr_autotune(hodlr_handle h, int nrhs, hodlr_tuning *best);
+HODLR_API int hodlr_set_tuning(hodlr_handle h, const hodlr_tuning *t);
+HODLR_API int hodlr_get_tuning(hodlr_handle h, hodlr_tuning *t);
+HODLR_API int hodlr_batch_autotune(hodlr_batch b, hodlr_tuning *per_forest, int capacity);
+
 /* Kernels launched by this library since load (for launch accounting). */
 HODLR_API int64_t hodlr_kernel_launches(void);
 

@@ -140,3 +140,18 @@ def test_batch_rejects_bad_systems(hodlr):
     b = hodlr.Batch([(64, 16, 2, 4, 1)])
     with pytest.raises(hodlr.HodlrError):
         b.factor()                                 # inputs not set
+
+
+def test_batch_autotune_then_solve(hodlr):
+    probs = _problems(RAGGED[:6], seed0=700)
+    b = _load(hodlr, probs, hodlr.PREC_MIXED)
+    tunes = b.autotune()
+    assert len(tunes) == b.stats()[0]
+    for t in tunes:
+        assert t["red_ctas_per_sm"] in (2, 4, 8) and t["update_tile_rows"] in (0, 64) and t["ms"] > 0
+    b.factor()
+    Bs = [to_dev(p.B) for p in probs]
+    torch.cuda.synchronize()
+    b.solve(Bs)
+    for i, p in enumerate(probs):
+        assert P.rel_residual(p, to_host(Bs[i])) <= 1.5e-12

@@ -264,3 +264,24 @@ def test_nonfinite_rhs_reports_status(hodlr):
     with pytest.raises(hodlr.HodlrError) as e:
         s.solve(Bd)
     assert e.value.code == hodlr.HODLR_ERR_NONFINITE_INPUT
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_autotune_picks_valid_shapes_and_keeps_results(hodlr, precision):
+    pr = P.gaussian_problem(128, 6, 32, nrhs=4, seed=11, decay=2.0)
+    s = make_solver(hodlr, pr, precision=precision)
+    t = s.autotune(nrhs=4)
+    assert t["red_ctas_per_sm"] in (2, 4, 8) and t["update_tile_rows"] in (0, 64) and t["ms"] > 0
+    assert s.get_tuning()["red_ctas_per_sm"] == t["red_ctas_per_sm"]
+    B = to_dev(pr.B)
+    s.solve(B)   # autotune left the handle factored
+    Xo, _, _ = O.hsolve_general(pr, pr.B)
+    assert rel(to_host(B), Xo) < (1e-12 if precision == 0 else 1e-10)
+    # every candidate shape gives the same solution up to rounding
+    for red in (2, 8):
+        for bm in (0, 64):
+            s.set_tuning(red, bm)
+            s.factor()
+            B2 = to_dev(pr.B)
+            s.solve(B2)
+            assert rel(to_host(B2), Xo) < (1e-12 if precision == 0 else 1e-10)
