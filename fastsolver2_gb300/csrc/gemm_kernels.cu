@@ -151,8 +151,20 @@ reduce_tn_kernel(const T *__restrict__ A, long long lda, const T *__restrict__ X
 // of 32, 16-byte aligned bases and leading dimensions.
 static constexpr int kTmaStages = 4;
 
+// Stage s of a reduce CTA: rows [row0 + 32 s, +32) of A (all ranks) and of
+// the X column tile at c0, into ring slot s % kTmaStages.
+template <int A_BYTES, int STAGE>
+__device__ __forceinline__ void reduce_tma_issue(unsigned char *base, uint64_t *bars, const CUtensorMap *mapA,
+                                                 const CUtensorMap *mapX, int s, int row0, int c0) {
+  const int slot = s % kTmaStages;
+  unsigned char *sa = base + slot * STAGE;
+  mbar_arrive_expect_tx(&bars[slot], STAGE);
+  tma_load_2d(sa, mapA, &bars[slot], row0 + s * 32, 0);
+  tma_load_2d(sa + A_BYTES, mapX, &bars[slot], row0 + s * 32, c0);
+}
+
 template <int RT>
-__global__ void __launch_bounds__(256, RT <= 32 ? 2 : 1)
+__global__ void __launch_bounds__(256, RT <= 32 ? 3 : 1)
 reduce_tma_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapX,
                   long long nrows, int r, int C, int chunk_rows, int nchunks, int nct, double *out,
                   const int *skip, DevStatus *st) {
@@ -180,15 +192,10 @@ reduce_tma_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constan
     mbar_fence_init();
   }
   __syncthreads();
-  auto issue = [&](int s) {
-    const int slot = s % kTmaStages;
-    unsigned char *sa = base + slot * STAGE;
-    mbar_arrive_expect_tx(&bars[slot], STAGE);
-    tma_load_2d(sa, &mapA, &bars[slot], (int)(row0 + (long long)s * BK), 0);
-    tma_load_2d(sa + A_BYTES, &mapX, &bars[slot], (int)(row0 + (long long)s * BK), c0);
-  };
+  const int row0i = (int)row0;  // tensor coordinates are 32-bit
   if (tid == 0)
-    for (int s = 0; s < min(kTmaStages, nst); ++s) issue(s);
+    for (int s = 0; s < min(kTmaStages, nst); ++s)
+      reduce_tma_issue<A_BYTES, STAGE>(base, bars, &mapA, &mapX, s, row0i, c0);
   float acc[RPT][CPT];
 #pragma unroll
   for (int a = 0; a < RPT; ++a)
@@ -206,26 +213,27 @@ reduce_tma_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constan
       return;
     }
     // every thread has finished stage s-1: its slot can be refilled
-    if (tid == 0 && s >= 1 && s - 1 + kTmaStages < nst) issue(s - 1 + kTmaStages);
+    if (tid == 0 && s >= 1 && s - 1 + kTmaStages < nst)
+      reduce_tma_issue<A_BYTES, STAGE>(base, bars, &mapA, &mapX, s - 1 + kTmaStages, row0i, c0);
     const unsigned char *sa = base + slot * STAGE, *sx = sa + A_BYTES;
 #pragma unroll
     for (int kc = 2 * g; kc < 2 * g + 2; ++kc) {
-      float4 av[RPT], xv[CPT];
+      float4 av[RPT];
 #pragma unroll
       for (int a = 0; a < RPT; ++a) av[a] = *reinterpret_cast<const float4 *>(sa + swz128(tr + 8 * a, kc));
 #pragma unroll
-      for (int c = 0; c < CPT; ++c) xv[c] = *reinterpret_cast<const float4 *>(sx + swz128(tc + 8 * c, kc));
+      for (int c = 0; c < CPT; ++c) {  // one column at a time keeps the live set small
+        const float4 xv = *reinterpret_cast<const float4 *>(sx + swz128(tc + 8 * c, kc));
 #pragma unroll
-      for (int a = 0; a < RPT; ++a)
-#pragma unroll
-        for (int c = 0; c < CPT; ++c) {
+        for (int a = 0; a < RPT; ++a) {
           float v = acc[a][c];
-          v = fmaf(av[a].x, xv[c].x, v);
-          v = fmaf(av[a].y, xv[c].y, v);
-          v = fmaf(av[a].z, xv[c].z, v);
-          v = fmaf(av[a].w, xv[c].w, v);
+          v = fmaf(av[a].x, xv.x, v);
+          v = fmaf(av[a].y, xv.y, v);
+          v = fmaf(av[a].z, xv.z, v);
+          v = fmaf(av[a].w, xv.w, v);
           acc[a][c] = v;
         }
+      }
     }
   }
   __syncthreads();  // all stages consumed: the ring becomes the group-sum buffer
@@ -502,15 +510,19 @@ update_tma_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constan
     tma_load_2d(sC, &mapC, &bars[1], (int)rowC, j0);
   }
   const double *B = a.B + (long long)(b >> 1) * a.b_s1 + (long long)((b & 1) ^ a.b_flip) * a.b_s2;
-  for (int e = tid; e < KMAX * BN; e += 256) {
-    const int q = e / BN, j = e % BN;
-    float v = 0.f;
-    if (q < a.K && j0 + j < a.N) {
-      double x = a.b_trans ? B[(j0 + j) + (long long)q * a.ldb] : B[q + (long long)(j0 + j) * a.ldb];
-      if (a.scale) x *= a.scale_cols ? a.scale[j0 + j] : a.scale[q];
-      v = (float)x;
+  {
+    // all of this thread's eta loads in flight at once, then convert and store
+    constexpr int PER = KMAX * BN / 256;
+    double x[PER], sc[PER];
+#pragma unroll
+    for (int u = 0; u < PER; ++u) {
+      const int e = tid + 256 * u, q = e / BN, j = e % BN;
+      const bool in = q < a.K && j0 + j < a.N;
+      x[u] = in ? (a.b_trans ? B[(j0 + j) + (long long)q * a.ldb] : B[q + (long long)(j0 + j) * a.ldb]) : 0.0;
+      sc[u] = (in && a.scale) ? (a.scale_cols ? a.scale[j0 + j] : a.scale[q]) : 1.0;
     }
-    sB[e] = v;
+#pragma unroll
+    for (int u = 0; u < PER; ++u) sB[tid + 256 * u] = (float)(x[u] * sc[u]);
   }
   bool ok = mbar_wait_bounded(&bars[0], 0);
   if (__syncthreads_or(!ok)) {

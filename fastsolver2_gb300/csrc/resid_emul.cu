@@ -148,17 +148,37 @@ dw_reduce_kernel(const float2 *__restrict__ A, long long lda, const float2 *__re
   const float2 *Ab = A + row_begin;
   const float2 *Xb = X + row_begin + (long long)c0 * ldx;
   const float2 z = make_float2(0.f, 0.f);
-  for (int i0 = 0; i0 < rows; i0 += kBK) {
+  // register double buffering: the next row block's loads are in flight
+  // while the current one is multiplied
+  constexpr int NA = kBK * RT / 256, NX = kBK * kCT / 256;
+  float2 ra[NA], rx[NX];
+  auto fetch = [&](int i0) {
     const int ib = min(kBK, rows - i0);
-    for (int e = tid; e < kBK * RT; e += 256) {
-      const int i = e % kBK, q = e / kBK;
-      sA[i][q] = (i < ib && q < r) ? Ab[i0 + i + (long long)q * lda] : z;
+#pragma unroll
+    for (int u = 0; u < NA; ++u) {
+      const int e = tid + 256 * u, i = e % kBK, q = e / kBK;
+      ra[u] = (i < ib && q < r) ? Ab[i0 + i + (long long)q * lda] : z;
     }
-    for (int e = tid; e < kBK * kCT; e += 256) {
-      const int i = e % kBK, j = e / kBK;
-      sX[i][j] = (i < ib && c0 + j < C) ? Xb[i0 + i + (long long)j * ldx] : z;
+#pragma unroll
+    for (int u = 0; u < NX; ++u) {
+      const int e = tid + 256 * u, i = e % kBK, j = e / kBK;
+      rx[u] = (i < ib && c0 + j < C) ? Xb[i0 + i + (long long)j * ldx] : z;
+    }
+  };
+  fetch(0);
+  for (int i0 = 0; i0 < rows; i0 += kBK) {
+#pragma unroll
+    for (int u = 0; u < NA; ++u) {
+      const int e = tid + 256 * u;
+      sA[e % kBK][e / kBK] = ra[u];
+    }
+#pragma unroll
+    for (int u = 0; u < NX; ++u) {
+      const int e = tid + 256 * u;
+      sX[e % kBK][e / kBK] = rx[u];
     }
     __syncthreads();
+    if (i0 + kBK < rows) fetch(i0 + kBK);
 #pragma unroll 4
     for (int i = 0; i < kBK; ++i) {
       const float2 x0 = sX[i][tc], x1 = sX[i][tc + 16];
