@@ -111,6 +111,7 @@ SIGNATURES = {
     "hodlr_set_tuning": (_I, [_VP, ctypes.POINTER(Tuning)]),
     "hodlr_get_tuning": (_I, [_VP, ctypes.POINTER(Tuning)]),
     "hodlr_batch_autotune": (_I, [_VP, ctypes.POINTER(Tuning), _I]),
+    "hodlr_probe_fp_peaks": (_I, [ctypes.POINTER(_D), ctypes.POINTER(_D)]),
     "hodlr_kernel_launches": (_I64, []),
     "hodlr_last_error_string": (ctypes.c_char_p, []),
 }
@@ -346,6 +347,13 @@ def hsolve(nrow, nrhs, rank, nPart, LD, K, U, V, precision=PREC_FP64, stream=Non
     check(lib().hodlr_hsolve_ex(nrow, nrhs, rank, nPart, LD, p(K), p(U), p(V), precision, stream,
                                 ctypes.byref(info)))
     return info
+
+
+def probe_fp_peaks():
+    """Measured (FFMA, DFMA) TFLOP/s of the current GPU."""
+    f, d = _D(), _D()
+    check(lib().hodlr_probe_fp_peaks(ctypes.byref(f), ctypes.byref(d)))
+    return f.value, d.value
 
 
 def kernel_launches():

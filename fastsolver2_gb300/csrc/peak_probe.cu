@@ -1,0 +1,72 @@
+// Throughput probe: the FP32 and FP64 FMA issue rates of the current GPU,
+// the denominators of the roofline fractions of the CUDA-core kernels (the
+// FP32 GEMMs and double-word residual on the FMA pipe, the FP64 capacitance
+// factorisation on the FP64 pipe).  Each thread runs eight independent FMA
+// chains; every index is the thread's own output slot.
+#include <cuda_runtime.h>
+
+#include "kernels.cuh"
+
+namespace hodlr {
+
+template <typename T>
+__global__ void __launch_bounds__(256) fma_chain_kernel(T *out, int iters, T a, T b) {
+  T x0 = (T)threadIdx.x, x1 = x0 + 1, x2 = x0 + 2, x3 = x0 + 3, x4 = x0 + 4, x5 = x0 + 5, x6 = x0 + 6,
+    x7 = x0 + 7;
+  for (int i = 0; i < iters; ++i) {
+    x0 = fma(x0, a, b);
+    x1 = fma(x1, a, b);
+    x2 = fma(x2, a, b);
+    x3 = fma(x3, a, b);
+    x4 = fma(x4, a, b);
+    x5 = fma(x5, a, b);
+    x6 = fma(x6, a, b);
+    x7 = fma(x7, a, b);
+  }
+  out[(long long)blockIdx.x * blockDim.x + threadIdx.x] = x0 + x1 + x2 + x3 + x4 + x5 + x6 + x7;
+}
+
+template <typename T>
+static cudaError_t time_chain(int iters, double *tflops) {
+  int dev = 0, sms = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if (e != cudaSuccess) return e;
+  const int threads = 256, blocks = sms * 8;
+  T *out = nullptr;
+  e = cudaMalloc(&out, sizeof(T) * threads * blocks);
+  if (e != cudaSuccess) return e;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  float best = 0.f;
+  for (int rep = 0; rep < 3; ++rep) {  // the first run loads the module
+    cudaEventRecord(e0, 0);
+    HODLR_LAUNCH(fma_chain_kernel<T>, blocks, threads, 0, 0, out, iters, (T)0.999999, (T)1e-7);
+    cudaEventRecord(e1, 0);
+    e = cudaEventSynchronize(e1);
+    if (e == cudaSuccess) e = cudaGetLastError();
+    if (e != cudaSuccess) break;
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    if (rep > 0 && (best == 0.f || ms < best)) best = ms;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(out);
+  if (e != cudaSuccess) return e;
+  *tflops = 2.0 * 8.0 * iters * (double)threads * blocks / (best * 1e-3) / 1e12;
+  return cudaSuccess;
+}
+
+}  // namespace hodlr
+
+using namespace hodlr;
+
+extern "C" int hodlr_probe_fp_peaks(double *ffma_tflops, double *dfma_tflops) {
+  if (!ffma_tflops || !dfma_tflops) return set_last_error(HODLR_ERR_INVALID_ARG, "probe: null argument");
+  cudaError_t e = time_chain<float>(65536, ffma_tflops);
+  if (e == cudaSuccess) e = time_chain<double>(4096, dfma_tflops);
+  if (e != cudaSuccess) return set_last_error(HODLR_ERR_CUDA, cudaGetErrorString(e));
+  return HODLR_OK;
+}

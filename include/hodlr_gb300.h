@@ -346,6 +346,12 @@ HODLR_API int hodlr_set_tuning(hodlr_handle h, const hodlr_tuning *t);
 HODLR_API int hodlr_get_tuning(hodlr_handle h, hodlr_tuning *t);
 HODLR_API int hodlr_batch_autotune(hodlr_batch b, hodlr_tuning *per_forest, int capacity);
 
+/* Measured FP32 and FP64 FMA throughput of the current GPU (TFLOP/s, eight
+ * independent FMA chains per thread, best of two timed runs) -- the
+ * denominators of the roofline fractions of the CUDA-core kernels.  No
+ * counterpart in the reference.  Legacy default stream; synchronous. */
+HODLR_API int hodlr_probe_fp_peaks(double *ffma_tflops, double *dfma_tflops);
+
 /* Kernels launched by this library since load (for launch accounting). */
 HODLR_API int64_t hodlr_kernel_launches(void);
 
