@@ -302,10 +302,12 @@ __global__ void __launch_bounds__(256) cap_apply_kernel(CapApplyArgs a) {
   constexpr int NP = MT * 32;  // padded rows
   E *sS = reinterpret_cast<E *>(smem_raw);   // [q][i], NP x NP (op(Sinv)(i, q) at sS[q*NP + i])
   E *sR = sS + NP * NP;                      // [q][j], NP x 32
-  const int p = blockIdx.y, c0 = blockIdx.x * 32, nc = min(32, a.C - c0);
+  const int p = blockIdx.y;
   const int node = a.node_base + p;
   const double *Sg = a.sinv + (long long)node * n2 * n2;
   const float2 *Sg2 = a.sinv2 ? a.sinv2 + (long long)node * n2 * n2 : nullptr;
+  // op(Sinv) is staged once per CTA; the CTA then walks its column tiles
+  // (blockIdx.x, + gridDim.x, ...)
   for (int e = threadIdx.x; e < NP * NP; e += blockDim.x) {
     const int i = e % NP, q = e / NP;
     E v;
@@ -320,6 +322,9 @@ __global__ void __launch_bounds__(256) cap_apply_kernel(CapApplyArgs a) {
   }
   const double *T0 = a.Tb + (long long)(2 * p) * a.tb_stride;
   const double *T1 = a.Tb + (long long)(2 * p + 1) * a.tb_stride;
+  for (int c0 = blockIdx.x * 32; c0 < a.C; c0 += gridDim.x * 32) {
+  const int nc = min(32, a.C - c0);
+  __syncthreads();  // the previous tile's reads of sR are done
   for (int e = threadIdx.x; e < NP * 32; e += blockDim.x) {
     const int q = e % NP, j = e / NP;
     double v = 0.0;
@@ -374,7 +379,13 @@ __global__ void __launch_bounds__(256) cap_apply_kernel(CapApplyArgs a) {
 #pragma unroll
       for (int v = 0; v < 4; ++v) {
         const int j = tj + 8 * v;
-        if (j < nc) eta[i + (long long)(c0 + j) * n2] = (double)sh[u][v] + (double)sl[u][v];
+        if (j >= nc) continue;
+        const double val = (double)sh[u][v] + (double)sl[u][v];
+        if (a.eta32)
+          a.eta32[(long long)p * n2 * a.C + i + (long long)(c0 + j) * n2] =
+              (float)(a.out_scale ? val * a.out_scale[i % r] : val);
+        else
+          eta[i + (long long)(c0 + j) * n2] = val;
       }
     }
   } else {
@@ -401,10 +412,16 @@ __global__ void __launch_bounds__(256) cap_apply_kernel(CapApplyArgs a) {
 #pragma unroll
       for (int v = 0; v < 4; ++v) {
         const int j = tj + 8 * v;
-        if (j < nc) eta[i + (long long)(c0 + j) * n2] = acc[u][v];
+        if (j >= nc) continue;
+        if (a.eta32)
+          a.eta32[(long long)p * n2 * a.C + i + (long long)(c0 + j) * n2] =
+              (float)(a.out_scale ? acc[u][v] * a.out_scale[i % r] : acc[u][v]);
+        else
+          eta[i + (long long)(c0 + j) * n2] = acc[u][v];
       }
     }
   }
+  }  // column tiles
 }
 
 cudaError_t launch_cap_apply(const CapApplyArgs &a, cudaStream_t s) {
@@ -416,7 +433,10 @@ cudaError_t launch_cap_apply(const CapApplyArgs &a, cudaStream_t s) {
   const bool dw = a.sinv2 != nullptr;
   const size_t es = dw ? sizeof(float2) : sizeof(double);
   const size_t bytes = (size_t)NP * NP * es + (size_t)NP * 32 * es;
-  dim3 grid(ceil_div(a.C, 32), a.nnode);
+  // enough CTAs to fill the GPU, each covering several column tiles of its node
+  const int tiles = ceil_div(a.C, 32);
+  const int groups = std::max(1, std::min(tiles, ceil_div(4 * 152, a.nnode)));
+  dim3 grid(groups, a.nnode);
 #define HODLR_CAPA(MTV, DWV)                                   \
   {                                                            \
     auto k = cap_apply_kernel<MTV, DWV>;                       \

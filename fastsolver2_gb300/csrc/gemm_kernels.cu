@@ -247,10 +247,10 @@ reduce_tma_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constan
   for (int e = tid; e < RT * BN; e += 256) {
     const int q = e % RT, j = e / RT;
     if (q >= r || c0 + j >= C) continue;
-    double sum = 0.0;
+    float sum = 0.f;  // fixed-order FP32 sum of the groups; one conversion
 #pragma unroll
-    for (int gg = 0; gg < 4; ++gg) sum += (double)sRed[(gg * RT + q) * (BN + 1) + j];
-    o[q + (long long)(c0 + j) * r] = sum;
+    for (int gg = 0; gg < 4; ++gg) sum += sRed[(gg * RT + q) * (BN + 1) + j];
+    o[q + (long long)(c0 + j) * r] = (double)sum;
   }
 }
 
@@ -429,8 +429,13 @@ __global__ void __launch_bounds__(256) update_nn_kernel(UpdateArgs a, int nrt, i
       const int q = e % BK, j = e / BK;
       double v = 0.0;
       if (q0 + q < a.K && j0 + j < a.N) {
-        v = a.b_trans ? B[(j0 + j) + (long long)(q0 + q) * a.ldb] : B[(q0 + q) + (long long)(j0 + j) * a.ldb];
-        if (a.scale) v *= a.scale_cols ? a.scale[j0 + j] : a.scale[q0 + q];
+        if (sizeof(T) == 4 && a.B32) {
+          const float *B32 = a.B32 + (long long)(b >> 1) * a.b_s1 + (long long)((b & 1) ^ a.b_flip) * a.b_s2;
+          v = a.b_trans ? B32[(j0 + j) + (long long)(q0 + q) * a.ldb] : B32[(q0 + q) + (long long)(j0 + j) * a.ldb];
+        } else {
+          v = a.b_trans ? B[(j0 + j) + (long long)(q0 + q) * a.ldb] : B[(q0 + q) + (long long)(j0 + j) * a.ldb];
+          if (a.scale) v *= a.scale_cols ? a.scale[j0 + j] : a.scale[q0 + q];
+        }
       }
       sB[q][j] = (T)v;
     }
@@ -509,8 +514,22 @@ update_tma_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constan
     mbar_arrive_expect_tx(&bars[1], BN * BM * 4);
     tma_load_2d(sC, &mapC, &bars[1], (int)rowC, j0);
   }
-  const double *B = a.B + (long long)(b >> 1) * a.b_s1 + (long long)((b & 1) ^ a.b_flip) * a.b_s2;
-  {
+  const long long boff = (long long)(b >> 1) * a.b_s1 + (long long)((b & 1) ^ a.b_flip) * a.b_s2;
+  if (a.B32) {
+    const float *B = a.B32 + boff;
+    constexpr int PER = KMAX * BN / 256;
+    float x[PER];
+#pragma unroll
+    for (int u = 0; u < PER; ++u) {
+      const int e = tid + 256 * u, q = e / BN, j = e % BN;
+      x[u] = (q < a.K && j0 + j < a.N)
+                 ? (a.b_trans ? B[(j0 + j) + (long long)q * a.ldb] : B[q + (long long)(j0 + j) * a.ldb])
+                 : 0.f;
+    }
+#pragma unroll
+    for (int u = 0; u < PER; ++u) sB[tid + 256 * u] = x[u];
+  } else {
+    const double *B = a.B + boff;
     // all of this thread's eta loads in flight at once, then convert and store
     constexpr int PER = KMAX * BN / 256;
     double x[PER], sc[PER];

@@ -118,6 +118,7 @@ struct hodlr_ctx {
   bool factored = false;
   // workspaces
   double *Tbuf = nullptr, *Wbuf = nullptr, *eta = nullptr, *red = nullptr;
+  float *eta32 = nullptr;   // mixed: capacitance solutions rounded for the FP32 updates
   double *X64 = nullptr, *R64 = nullptr, *B64 = nullptr, *norms = nullptr, *nwork = nullptr;
   float *X32 = nullptr;
   // double-word (hi, lo) copies for the emulated FP64 residual (mixed mode)
@@ -391,6 +392,10 @@ static int cap_apply(hodlr_ctx *h, int l, int C, long long tb_stride, bool trans
   ca.sinv = h->Sinv;
   ca.sinv2 = h->mixed ? h->Sinv2 : nullptr;
   ca.eta = h->eta;
+  if (h->mixed) {  // the consumers are FP32 updates: write FP32, with the solve's row scaling applied
+    ca.eta32 = h->eta32;
+    ca.out_scale = trans ? h->slev(l) : nullptr;
+  }
   ca.r = h->r;
   ca.C = C;
   ca.nnode = h->nodes(l);
@@ -450,6 +455,7 @@ template <typename T> static int factor_sweep(hodlr_ctx *h) {
       ua.lda = n;
       ua.a_bstride = rows;
       ua.B = h->eta;
+      if (sizeof(T) == 4) ua.B32 = h->eta32;
       ua.ldb = 2 * r;
       ua.b_s1 = 2LL * r * Cd;
       ua.b_s2 = r;
@@ -494,6 +500,10 @@ static int solve_sweep(hodlr_ctx *h, T *X, long long ldx, int k, bool trans, con
     ua.b_s2 = r;
     ua.b_flip = trans ? 1 : 0;
     ua.scale = trans ? h->slev(l) : nullptr;
+    if (sizeof(T) == 4) {  // FP32 eta, scaled by the capacitance kernel
+      ua.B32 = h->eta32;
+      ua.scale = nullptr;
+    }
     ua.C = X;
     ua.ldc = ldx;
     ua.c_bstride = rows;
@@ -804,6 +814,7 @@ static int create_ctx(const hodlr_desc &d, const std::vector<int> &sys_levels, h
   ALLOC(h->Tbuf, double, h->tbuf_elems);
   ALLOC(h->Wbuf, double, h->tbuf_elems);
   ALLOC(h->eta, double, h->eta_elems);
+  if (h->mixed) ALLOC(h->eta32, float, h->eta_elems);
   ALLOC(h->red, double, h->red_elems);
   ALLOC(h->norms, double, 2 * (size_t)k * h->nsys);
   ALLOC(h->nwork, double, (size_t)k * std::max(64, h->forest ? h->nleaf : 0));

@@ -65,6 +65,7 @@ cudaError_t launch_reduce_tn(const T *A, long long lda, const T *X, long long ld
 struct UpdateArgs {
   const void *A; long long lda; long long a_bstride; int a_trans;  // a_trans: A_b(i,q) at A_b[q + i*lda]
   const double *B; long long ldb; long long b_s1, b_s2; int b_flip; int b_trans;
+  const float *B32;  // FP32 kernels: if set, B is read from here (same layout, scale already applied)
   const double *scale; int scale_cols;
   void *C; long long ldc; long long c_bstride;
   int M, N, K, nbatch;
@@ -105,6 +106,8 @@ struct CapApplyArgs {
   const double *scale;
   const double *sinv; const float2 *sinv2;
   double *eta;
+  float *eta32;              // if set: FP32 output instead, rows scaled by out_scale[i % r]
+  const double *out_scale;   // (for FP32 consumers; may be null)
   int r, C, nnode, node_base;
   bool trans;
   const int *skip;
