@@ -211,6 +211,7 @@ def run_ours(args, wl):
 
     launches0 = fs.kernel_launches()
     ffma_tf, dfma_tf = fs.probe_fp_peaks()   # live FMA-pipe rates of this GPU
+    mma_tf = fs.probe_mma_bf16()              # live warp-level bf16 MMA rate
     with torch.cuda.stream(stream):
         mixed = fs.Solver(n, m, L, r, nrhs_max=k, precision=fs.PREC_MIXED, residual=args.resid,
                           refine_tol=1e-12, refine_max_iter=10, stream=sp)
@@ -398,9 +399,9 @@ def run_ours(args, wl):
     dw_tf = ffma_tf / 12.0   # a double-word FMA is 12 FP32 instructions
     peak_of = {"leaf_lu": ffma_tf, "leaf_solve": ffma_tf, "reduce": ffma_tf,
                "update": ffma_tf, "capacitance": dw_tf,
-               "resid_leaf": dw_tf if args.resid == 1 else dfma_tf,
-               "resid_reduce": dw_tf if args.resid == 1 else dfma_tf,
-               "resid_update": dw_tf if args.resid == 1 else dfma_tf}
+               "resid_leaf": dw_tf if args.resid == 1 else (mma_tf / OZ_PAIRS if args.resid == 2 else dfma_tf),
+               "resid_reduce": dw_tf if args.resid == 1 else (mma_tf / OZ_PAIRS if args.resid == 2 else dfma_tf),
+               "resid_update": dw_tf if args.resid == 1 else (mma_tf / OZ_PAIRS if args.resid == 2 else dfma_tf)}
     phase_report = {}
     for name, (pms, pn) in phases.items():
         per_step = pms / args.steps
@@ -409,33 +410,49 @@ def run_ours(args, wl):
             ach = work[name] / (per_step * 1e-3) / 1e12
             ent.update(tflops=ach, peak=peak_of[name], frac=ach / peak_of[name])
         phase_report[name] = ent
-    # kernels: the phases they run in, and their DRAM traffic per launch from
-    # the ncu captures in profiles/ (N = 2^17 launches scaled by 8 to N = 2^20)
-    kernels = {
-        "dw_update_kernel": (("resid_leaf", "resid_update"), 8 * (100.77e6 + 16.15e6)),
-        "dw_reduce_kernel": (("resid_reduce",), 8 * (100.69e6 + 3.11e6)),
-        "reduce_tma_kernel": (("reduce",), None),
-        "update_tma_kernel": (("update",), None),
-    }
+    # the kernels of the dominant phases: (phases, bound, peak, native work
+    # factor, DRAM bytes per launch from the ncu captures in profiles/, N=2^17 x 8)
+    bf16_peak = _measured_peak("bf16_tflops")
+    if args.resid == 2:
+        resid_kernels = {
+            "oz_update_kernel": (("resid_update",), "tensor", bf16_peak, OZ_PAIRS, None),
+            "oz_reduce_kernel": (("resid_reduce",), "tensor", bf16_peak, OZ_PAIRS, None),
+            "oz_leaf_kernel": (("resid_leaf",), "tensor", bf16_peak, OZ_PAIRS, None),
+        }
+    else:
+        resid_kernels = {
+            "dw_update_kernel": (("resid_leaf", "resid_update"), "fp32_fma_pipe", dw_tf, 1.0,
+                                 8 * (100.77e6 + 16.15e6)),
+            "dw_reduce_kernel": (("resid_reduce",), "fp32_fma_pipe", dw_tf, 1.0, 8 * (100.69e6 + 3.11e6)),
+        }
+    kernels = dict(resid_kernels)
+    kernels["reduce_tma_kernel"] = (("reduce",), "fp32_fma_pipe", ffma_tf, 1.0, None)
+    kernels["update_tma_kernel"] = (("update",), "fp32_fma_pipe", ffma_tf, 1.0, None)
     roof = None
     best = None
-    for kname, (phs, traffic) in kernels.items():
-        kms = sum(phase_report.get(ph, {}).get("ms_per_step", 0.0) for ph in phs)
+    for kname, spec in kernels.items():
+        kms = sum(phase_report.get(ph, {}).get("ms_per_step", 0.0) for ph in spec[0])
         if best is None or kms > best[1]:
-            best = (kname, kms, phs, traffic)
+            best = (kname, kms, spec)
     if best and best[1] > 0:
-        kname, kms, phs, traffic = best
-        kwork = sum(work[ph] for ph in phs)
+        kname, kms, (phs, bound, pk, factor, traffic) = best
+        kwork = factor * sum(work[ph] for ph in phs)
         nl = sum(phase_report[ph]["launches_per_step"] for ph in phs)
         ach = kwork / (kms * 1e-3) / 1e12
-        pk = peak_of[phs[0]]
-        roof = {"kernel": kname, "bound": "fp32_fma_pipe", "achieved": ach, "peak": pk, "unit": "TFLOP/s",
-                "frac": ach / pk, "traffic": traffic,
-                "avg_launch_ms": kms / max(nl, 1), "launches_per_step": nl,
-                "note": "FP64-equivalent algorithmic flops of the kernel's phases / their CUDA-event time in the "
-                        "timed graphs; peak = this GPU's FFMA rate measured live (hodlr_probe_fp_peaks), /12 for "
-                        "double-word arithmetic (neither the HBM copy nor the bf16 GEMM peak bounds this "
-                        "FP32-pipe kernel); traffic = ncu DRAM bytes per launch of the N=2^17 capture x 8"}
+        roof = {"kernel": kname, "bound": bound, "achieved": ach, "peak": pk, "unit": "TFLOP/s",
+                "frac": ach / pk if pk else None, "traffic": traffic,
+                "avg_launch_ms": kms / max(nl, 1), "launches_per_step": nl}
+        if bound == "tensor":
+            roof["note"] = ("bf16 digit-product flops (%d digit pairs per FP64 product) of the kernel's phases / "
+                            "their CUDA-event time in the timed graphs; peak = the driver-measured dense bf16 "
+                            "GEMM rate (MEASURED_PEAKS.json); frac_of_mma_sync = against the warp-level bf16 MMA "
+                            "rate measured live (hodlr_probe_mma_bf16)" % OZ_PAIRS)
+            roof["frac_of_mma_sync"] = ach / mma_tf
+        else:
+            roof["note"] = ("FP64-equivalent algorithmic flops of the kernel's phases / their CUDA-event time in "
+                            "the timed graphs; peak = this GPU's FFMA rate measured live (hodlr_probe_fp_peaks), "
+                            "/12 for double-word arithmetic; traffic = ncu DRAM bytes per launch of the N=2^17 "
+                            "capture x 8")
     line = {
         "metric": METRIC, "value": ms, "unit": "ms", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": ms, "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
@@ -444,10 +461,12 @@ def run_ours(args, wl):
                                "orthonormal factors s_i=10^(-6i/32), leaf shift 1.5",
                    **wl, "parallelism": "replicas" if world > 1 else "single GPU",
                    "l2": "inputs larger than L2 (>14 GB resident per step)",
-                   "residual": "fp64-emulated (double-FP32)" if args.resid == 1 else "native fp64"},
+                   "residual": {0: "native fp64", 1: "fp64-accurate double-word (FP32 pipes)",
+                                2: "fp64-accurate bf16 digit products (tensor cores, mma.sync)"}[args.resid]},
         "ms_per_step_without_phase_events": ms_no_events,
-        "fp_peaks_measured_tflops": {"ffma": ffma_tf, "dfma": dfma_tf,
-                                     "hbm_gbs_measured_peaks_json": _hbm_peak()},
+        "fp_peaks_measured_tflops": {"ffma": ffma_tf, "dfma": dfma_tf, "mma_sync_bf16": mma_tf,
+                                     "hbm_gbs_measured_peaks_json": _measured_peak("hbm_gbs"),
+                                     "bf16_gemm_measured_peaks_json": _measured_peak("bf16_tflops")},
         "tuning": tuning,
         "refine_iterations": float(np.mean(iters)), "rel_resid_device": final_resid_dev,
         "rel_resid_fp64_check": check,
@@ -590,10 +609,13 @@ def run_ragged(args, fs, torch, stream, colmajor):
     return out
 
 
-def _hbm_peak():
+OZ_PAIRS = 28   # digit pairs (s + t <= 6 of 7 x 7) per FP64 product in the tensor-core residual
+
+
+def _measured_peak(key):
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
-            return json.load(f).get("hbm_gbs")
+            return json.load(f).get(key)
     except (OSError, ValueError):
         return None
 
@@ -604,7 +626,8 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--resid", type=int, default=1, help="0 native FP64 residual, 1 FP64-emulated")
+    ap.add_argument("--resid", type=int, default=2,
+                    help="0 native FP64 residual, 1 double-word FP32 pipes, 2 tensor-core digit products")
     ap.add_argument("--fp64-steps", type=int, default=3)
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--small", action="store_true", help="N=2^14 smoke-sized workload")

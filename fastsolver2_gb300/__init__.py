@@ -26,6 +26,7 @@ PREC_FP64 = 0
 PREC_MIXED = 1
 RESID_FP64 = 0
 RESID_FP64_EMULATED = 1
+RESID_FP64_TENSOR = 2
 
 LIB_PATH = _build.LIB
 
@@ -112,6 +113,7 @@ SIGNATURES = {
     "hodlr_get_tuning": (_I, [_VP, ctypes.POINTER(Tuning)]),
     "hodlr_batch_autotune": (_I, [_VP, ctypes.POINTER(Tuning), _I]),
     "hodlr_probe_fp_peaks": (_I, [ctypes.POINTER(_D), ctypes.POINTER(_D)]),
+    "hodlr_probe_mma_bf16": (_I, [ctypes.POINTER(_D)]),
     "hodlr_kernel_launches": (_I64, []),
     "hodlr_last_error_string": (ctypes.c_char_p, []),
 }
@@ -354,6 +356,13 @@ def probe_fp_peaks():
     f, d = _D(), _D()
     check(lib().hodlr_probe_fp_peaks(ctypes.byref(f), ctypes.byref(d)))
     return f.value, d.value
+
+
+def probe_mma_bf16():
+    """Measured warp-level bf16 MMA TFLOP/s of the current GPU."""
+    t = _D()
+    check(lib().hodlr_probe_mma_bf16(ctypes.byref(t)))
+    return t.value
 
 
 def kernel_launches():

@@ -184,15 +184,18 @@ __global__ void __launch_bounds__(256) cap_factor_kernel(CapFactorArgs a) {
   double *S = reinterpret_cast<double *>(smem_raw);
   double *W = S + n2 * n2;  // n2 x 32 identity tile
   int *piv = reinterpret_cast<int *>(W + n2 * 32);
-  const double *T0 = a.Tb + (long long)(2 * p) * a.tb_stride;
-  const double *T1 = a.Tb + (long long)(2 * p + 1) * a.tb_stride;
-  for (int e = threadIdx.x; e < n2 * n2; e += blockDim.x) {
-    const int i = e % n2, j = e / n2;
-    double v = (i == j) ? 1.0 : 0.0;
-    if (i >= r && j < r) v = (a.scale ? a.scale[i - r] : 1.0) * T0[(i - r) + (long long)(a.ucol + j) * r];
-    if (i < r && j >= r) v = (a.scale ? a.scale[i] : 1.0) * T1[i + (long long)(a.ucol + j - r) * r];
-    S[e] = v;
-  }
+  const long long o0 = (long long)(2 * p) * a.tb_stride, o1 = (long long)(2 * p + 1) * a.tb_stride;
+  auto T = [&](long long off) -> double { return a.Tb32 ? (double)a.Tb32[off] : a.Tb[off]; };
+  auto fill_S = [&]() {
+    for (int e = threadIdx.x; e < n2 * n2; e += blockDim.x) {
+      const int i = e % n2, j = e / n2;
+      double v = (i == j) ? 1.0 : 0.0;
+      if (i >= r && j < r) v = (a.scale ? a.scale[i - r] : 1.0) * T(o0 + (i - r) + (long long)(a.ucol + j) * r);
+      if (i < r && j >= r) v = (a.scale ? a.scale[i] : 1.0) * T(o1 + i + (long long)(a.ucol + j - r) * r);
+      S[e] = v;
+    }
+  };
+  fill_S();
   __syncthreads();
   block_getrf<double>(S, n2, n2, piv, &s_info);
   if (s_info && threadIdx.x == 0) report_error(a.st, HODLR_ERR_SINGULAR_CAPACITANCE, node);
@@ -201,19 +204,15 @@ __global__ void __launch_bounds__(256) cap_factor_kernel(CapFactorArgs a) {
   for (int e = threadIdx.x; e < n2; e += blockDim.x) a.cap_ipiv[(long long)node * n2 + e] = piv[e];
   // explicit inverse: Gauss-Jordan on a fresh copy of S
   __syncthreads();
-  for (int e = threadIdx.x; e < n2 * n2; e += blockDim.x) {
-    const int i = e % n2, j = e / n2;
-    double v = (i == j) ? 1.0 : 0.0;
-    if (i >= r && j < r) v = (a.scale ? a.scale[i - r] : 1.0) * T0[(i - r) + (long long)(a.ucol + j) * r];
-    if (i < r && j >= r) v = (a.scale ? a.scale[i] : 1.0) * T1[i + (long long)(a.ucol + j - r) * r];
-    S[e] = v;
-  }
+  fill_S();
   __syncthreads();
   block_gj_inverse<double>(S, n2, n2, W, piv, &s_info);
-  double *gI = a.sinv + (long long)node * n2 * n2;
+  double *gI = a.sinv ? a.sinv + (long long)node * n2 * n2 : nullptr;
   float2 *gI2 = a.sinv2 ? a.sinv2 + (long long)node * n2 * n2 : nullptr;
+  float *gI32 = a.sinv32 ? a.sinv32 + (long long)node * n2 * n2 : nullptr;
   for (int e = threadIdx.x; e < n2 * n2; e += blockDim.x) {
-    gI[e] = S[e];
+    if (gI) gI[e] = S[e];
+    if (gI32) gI32[e] = (float)S[e];
     if (gI2) {
       const float h = __double2float_rn(S[e]);
       gI2[e] = make_float2(h, __double2float_rn(S[e] - (double)h));
@@ -230,14 +229,30 @@ __global__ void __launch_bounds__(256, 1) cap_factor_reg_kernel(CapFactorArgs a)
   double *buf = reinterpret_cast<double *>(smem_raw);
   const int p = blockIdx.x, node = a.node_base + p;
   constexpr int r = N2 / 2;
-  const double *T0 = a.Tb + (long long)(2 * p) * a.tb_stride;
-  const double *T1 = a.Tb + (long long)(2 * p + 1) * a.tb_stride;
+  const long long o0 = (long long)(2 * p) * a.tb_stride, o1 = (long long)(2 * p + 1) * a.tb_stride;
+  auto T = [&](long long off) -> double { return a.Tb32 ? (double)a.Tb32[off] : a.Tb[off]; };
   auto load = [&](int i, int j) -> double {
     double v = (i == j) ? 1.0 : 0.0;
-    if (i >= r && j < r) v = (a.scale ? a.scale[i - r] : 1.0) * T0[(i - r) + (long long)(a.ucol + j) * r];
-    if (i < r && j >= r) v = (a.scale ? a.scale[i] : 1.0) * T1[i + (long long)(a.ucol + j - r) * r];
+    if (i >= r && j < r) v = (a.scale ? a.scale[i - r] : 1.0) * T(o0 + (i - r) + (long long)(a.ucol + j) * r);
+    if (i < r && j >= r) v = (a.scale ? a.scale[i] : 1.0) * T(o1 + i + (long long)(a.ucol + j - r) * r);
     return v;
   };
+  if (a.sinv32) {
+    // mixed path: the LU (and pivots) in FP64, then the inverse the FP32 sweeps
+    // apply, by an FP32 Gauss-Jordan sweep on S rounded to FP32
+    auto nostore = [](int, int, double) {};
+    reg_factor<double, N2>(load, buf, a.cap_lu + (long long)node * N2 * N2, a.cap_ipiv + (long long)node * N2,
+                           nostore, false, &s_info);
+    if (s_info && threadIdx.x == 0) report_error(a.st, HODLR_ERR_SINGULAR_CAPACITANCE, node);
+    __syncthreads();
+    float *g32 = a.sinv32 + (long long)node * N2 * N2;
+    auto load32 = [&](int i, int j) -> float { return (float)load(i, j); };
+    auto store32 = [&](int i, int j, float v) { g32[i + j * N2] = v; };
+    int info32 = 0;
+    reg_factor<float, N2>(load32, reinterpret_cast<float *>(buf), (float *)nullptr, (int *)nullptr, store32, true,
+                          &info32);
+    return;
+  }
   double *gI = a.sinv + (long long)node * N2 * N2;
   float2 *gI2 = a.sinv2 ? a.sinv2 + (long long)node * N2 * N2 : nullptr;
   auto store = [&](int i, int j, double v) {
@@ -424,7 +439,97 @@ __global__ void __launch_bounds__(256) cap_apply_kernel(CapApplyArgs a) {
   }  // column tiles
 }
 
+// Mixed path: eta = op(Sinv) RHS in FP32 (the FP32 inverse against the FP32
+// T blocks), written as FP32 for the FP32 updates (eta32, rows scaled by
+// out_scale).  Same tiling as above.
+template <int MT>
+__global__ void __launch_bounds__(256) cap_apply_f32_kernel(CapApplyArgs a) {
+  if (a.skip && *a.skip) return;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int r = a.r, n2 = 2 * r;
+  constexpr int NP = MT * 32;
+  float *sS = reinterpret_cast<float *>(smem_raw);  // [q][i]
+  float *sR = sS + NP * (NP + 1);                    // [j][q], padded
+  const int p = blockIdx.y;
+  const int node = a.node_base + p;
+  const float *Sg = a.sinv32 + (long long)node * n2 * n2;
+  for (int e = threadIdx.x; e < NP * NP; e += blockDim.x) {
+    const int i = e % NP, q = e / NP;
+    float v = 0.f;
+    if (i < n2 && q < n2) v = a.trans ? Sg[q + (long long)i * n2] : Sg[i + (long long)q * n2];
+    sS[q * (NP + 1) + i] = v;
+  }
+  const float *T0 = a.Tb32 + (long long)(2 * p) * a.tb_stride;
+  const float *T1 = a.Tb32 + (long long)(2 * p + 1) * a.tb_stride;
+  const int ti = threadIdx.x & 31, tj = threadIdx.x >> 5;
+  for (int c0 = blockIdx.x * 32; c0 < a.C; c0 += gridDim.x * 32) {
+    const int nc = min(32, a.C - c0);
+    __syncthreads();
+    for (int e = threadIdx.x; e < NP * 32; e += blockDim.x) {
+      const int q = e % NP, j = e / NP;
+      float v = 0.f;
+      if (q < n2 && j < nc) {
+        if (!a.trans)
+          v = (q < r) ? (a.scale ? (float)a.scale[q] : 1.f) * T1[q + (long long)(c0 + j) * r]
+                      : (a.scale ? (float)a.scale[q - r] : 1.f) * T0[(q - r) + (long long)(c0 + j) * r];
+        else
+          v = (q < r) ? T0[q + (long long)(c0 + j) * r] : T1[(q - r) + (long long)(c0 + j) * r];
+      }
+      sR[j * (NP + 1) + q] = v;
+    }
+    __syncthreads();
+    float acc[MT][4];
+#pragma unroll
+    for (int u = 0; u < MT; ++u)
+#pragma unroll
+      for (int v = 0; v < 4; ++v) acc[u][v] = 0.f;
+    for (int q = 0; q < n2; ++q) {
+      float sv[MT];
+#pragma unroll
+      for (int u = 0; u < MT; ++u) sv[u] = sS[q * (NP + 1) + ti + 32 * u];
+#pragma unroll
+      for (int v = 0; v < 4; ++v) {
+        const float rv = sR[(tj + 8 * v) * (NP + 1) + q];
+#pragma unroll
+        for (int u = 0; u < MT; ++u) acc[u][v] = fmaf(sv[u], rv, acc[u][v]);
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < MT; ++u) {
+      const int i = ti + 32 * u;
+      if (i >= n2) continue;
+      const float sc = a.out_scale ? (float)a.out_scale[i % r] : 1.f;
+#pragma unroll
+      for (int v = 0; v < 4; ++v) {
+        const int j = tj + 8 * v;
+        if (j < nc) a.eta32[(long long)p * n2 * a.C + i + (long long)(c0 + j) * n2] = acc[u][v] * sc;
+      }
+    }
+  }
+}
+
 cudaError_t launch_cap_apply(const CapApplyArgs &a, cudaStream_t s) {
+  if (a.Tb32 && a.sinv32 && a.eta32) {
+    if (a.nnode <= 0 || a.C <= 0) return cudaSuccess;
+    if (a.r < 1 || a.r > 64) return cudaErrorInvalidValue;
+    const int n2 = 2 * a.r;
+    const int MT = n2 <= 32 ? 1 : (n2 <= 64 ? 2 : 4);
+    const int NP = MT * 32;
+    const size_t bytes = sizeof(float) * ((size_t)NP * (NP + 1) + 32ull * (NP + 1));
+    const int tiles = ceil_div(a.C, 32);
+    const int groups = std::max(1, std::min(tiles, ceil_div(4 * 152, a.nnode)));
+    dim3 grid(groups, a.nnode);
+#define HODLR_CAPF(MTV)                                 \
+  {                                                     \
+    auto k = cap_apply_f32_kernel<MTV>;                 \
+    cudaError_t e = set_smem(k, bytes);                 \
+    if (e != cudaSuccess) return e;                     \
+    HODLR_LAUNCH(k, grid, 256, bytes, s, a);            \
+  }
+    if (MT == 1) HODLR_CAPF(1) else if (MT == 2) HODLR_CAPF(2) else HODLR_CAPF(4)
+#undef HODLR_CAPF
+    return cudaGetLastError();
+  }
   if (a.nnode <= 0 || a.C <= 0) return cudaSuccess;
   if (a.r < 1 || a.r > 64) return cudaErrorInvalidValue;
   const int n2 = 2 * a.r;

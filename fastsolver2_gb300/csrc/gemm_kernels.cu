@@ -17,6 +17,7 @@
 // thread keeps an (RT/8) x 8 register tile; shared-memory rows are padded by
 // one element so the column-wise staging stores are bank-conflict free.
 #include <algorithm>
+#include <type_traits>
 
 #include "kernels.cuh"
 #include "tma.cuh"
@@ -67,10 +68,10 @@ const Tuning &current_tuning() { return g_tuning ? *g_tuning : kDefaultTuning; }
 TuningScope::TuningScope(const Tuning *t) : prev(g_tuning) { g_tuning = t; }
 TuningScope::~TuningScope() { g_tuning = prev; }
 
-template <typename T, int RT, int BN>
+template <typename T, int RT, int BN, typename OutT>
 __global__ void __launch_bounds__(256)
 reduce_tn_kernel(const T *__restrict__ A, long long lda, const T *__restrict__ X, long long ldx,
-                 long long nrows, int r, int C, int chunk_rows, int nchunks, int nct, double *out,
+                 long long nrows, int r, int C, int chunk_rows, int nchunks, int nct, OutT *out,
                  const int *skip) {
   if (skip && *skip) return;
   constexpr int RPT = RT / 8;           // ranks per thread (rows of the output)
@@ -127,14 +128,14 @@ reduce_tn_kernel(const T *__restrict__ A, long long lda, const T *__restrict__ X
 #pragma unroll
     for (int c = 0; c < CPT; ++c) sRed[(g * RT + tr * RPT + a) * (BN + 1) + tc * CPT + c] = acc[a][c];
   __syncthreads();
-  double *o = out + ((long long)b * nchunks + chunk) * r * C;
+  OutT *o = out + ((long long)b * nchunks + chunk) * r * C;
   for (int e = tid; e < RT * BN; e += 256) {
     const int q = e % RT, j = e / RT;
     if (q >= r || c0 + j >= C) continue;
     double s = 0.0;
 #pragma unroll
     for (int gg = 0; gg < 4; ++gg) s += (double)sRed[(gg * RT + q) * (BN + 1) + j];
-    o[q + (long long)(c0 + j) * r] = s;
+    o[q + (long long)(c0 + j) * r] = (OutT)s;
   }
 }
 
@@ -163,10 +164,10 @@ __device__ __forceinline__ void reduce_tma_issue(unsigned char *base, uint64_t *
   tma_load_2d(sa + A_BYTES, mapX, &bars[slot], row0 + s * 32, c0);
 }
 
-template <int RT>
+template <int RT, typename OutT>
 __global__ void __launch_bounds__(256, RT <= 32 ? 3 : 1)
 reduce_tma_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapX,
-                  long long nrows, int r, int C, int chunk_rows, int nchunks, int nct, double *out,
+                  long long nrows, int r, int C, int chunk_rows, int nchunks, int nct, OutT *out,
                   const int *skip, DevStatus *st) {
   if (skip && *skip) return;
   constexpr int BN = 64, BK = 32, RPT = RT / 8, CPT = BN / 8;
@@ -243,14 +244,14 @@ reduce_tma_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constan
 #pragma unroll
     for (int c = 0; c < CPT; ++c) sRed[(g * RT + tr + 8 * a) * (BN + 1) + tc + 8 * c] = acc[a][c];
   __syncthreads();
-  double *o = out + ((long long)b * nchunks + chunk) * r * C;
+  OutT *o = out + ((long long)b * nchunks + chunk) * r * C;
   for (int e = tid; e < RT * BN; e += 256) {
     const int q = e % RT, j = e / RT;
     if (q >= r || c0 + j >= C) continue;
-    float sum = 0.f;  // fixed-order FP32 sum of the groups; one conversion
+    float sum = 0.f;  // fixed-order FP32 sum of the groups
 #pragma unroll
     for (int gg = 0; gg < 4; ++gg) sum += sRed[(gg * RT + q) * (BN + 1) + j];
-    o[q + (long long)(c0 + j) * r] = (double)sum;
+    o[q + (long long)(c0 + j) * r] = (OutT)sum;
   }
 }
 
@@ -260,12 +261,12 @@ static size_t reduce_tma_smem() {
   return std::max(ring, red) + 1024;
 }
 
-template <int RT>
+template <int RT, typename OutT>
 static cudaError_t reduce_tma_rt(const CUtensorMap &ma, const CUtensorMap &mx, long long nrows, int nbatch, int r,
-                                 int C, int chunk_rows, int nchunks, int nct, double *dst, const int *skip,
+                                 int C, int chunk_rows, int nchunks, int nct, OutT *dst, const int *skip,
                                  DevStatus *st, cudaStream_t s) {
   const size_t bytes = reduce_tma_smem<RT>();
-  auto k = reduce_tma_kernel<RT>;
+  auto k = reduce_tma_kernel<RT, OutT>;
   static bool attr = false;
   if (!attr) {
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
@@ -278,8 +279,9 @@ static cudaError_t reduce_tma_rt(const CUtensorMap &ma, const CUtensorMap &mx, l
 }
 
 // The TMA path for FP32 operands, if its preconditions hold (else false).
+template <typename OutT>
 static bool reduce_tma_try(const float *A, long long lda, const float *X, long long ldx, long long nrows,
-                           int nbatch, int r, int C, int chunk_rows, int nchunks, double *dst, const int *skip,
+                           int nbatch, int r, int C, int chunk_rows, int nchunks, OutT *dst, const int *skip,
                            DevStatus *st, cudaStream_t s, cudaError_t &err) {
   if (nrows % 32 || chunk_rows % 32 || C <= 8) return false;
   const int RT = r <= 16 ? 16 : (r <= 32 ? 32 : 64);
@@ -289,16 +291,17 @@ static bool reduce_tma_try(const float *A, long long lda, const float *X, long l
   if (!make_tensor_map_f32(&mx, X, total, C, ldx, 32, 64, true)) return false;
   const int nct = ceil_div(C, 64);
   if (RT == 16)
-    err = reduce_tma_rt<16>(ma, mx, nrows, nbatch, r, C, chunk_rows, nchunks, nct, dst, skip, st, s);
+    err = reduce_tma_rt<16, OutT>(ma, mx, nrows, nbatch, r, C, chunk_rows, nchunks, nct, dst, skip, st, s);
   else if (RT == 32)
-    err = reduce_tma_rt<32>(ma, mx, nrows, nbatch, r, C, chunk_rows, nchunks, nct, dst, skip, st, s);
+    err = reduce_tma_rt<32, OutT>(ma, mx, nrows, nbatch, r, C, chunk_rows, nchunks, nct, dst, skip, st, s);
   else
-    err = reduce_tma_rt<64>(ma, mx, nrows, nbatch, r, C, chunk_rows, nchunks, nct, dst, skip, st, s);
+    err = reduce_tma_rt<64, OutT>(ma, mx, nrows, nbatch, r, C, chunk_rows, nchunks, nct, dst, skip, st, s);
   return true;
 }
 
+template <typename OutT>
 __global__ void reduce_pass2_kernel(const double *__restrict__ partial, int nchunks, long long blk,
-                                    double *out, const int *skip) {
+                                    OutT *out, const int *skip) {
   if (skip && *skip) return;
   const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   const int b = blockIdx.y;
@@ -328,12 +331,12 @@ size_t reduce_workspace_doubles(long long nrows, int nbatch, int r, int C, int) 
   return nchunks > 1 ? (size_t)nbatch * nchunks * r * C : 0;
 }
 
-template <typename T, int RT, int BN>
+template <typename T, int RT, int BN, typename OutT>
 static cudaError_t reduce_rt(const T *A, long long lda, const T *X, long long ldx, long long nrows, int nbatch,
-                             int r, int C, int chunk_rows, int nchunks, int nct, double *dst, const int *skip,
+                             int r, int C, int chunk_rows, int nchunks, int nct, OutT *dst, const int *skip,
                              cudaStream_t s) {
   const size_t bytes = sizeof(T) * ((size_t)kRedBK * (RT + 1) + (size_t)kRedBK * (BN + 1) + 4ull * RT * (BN + 1));
-  auto k = reduce_tn_kernel<T, RT, BN>;
+  auto k = reduce_tn_kernel<T, RT, BN, OutT>;
   if (bytes > 48 * 1024) {
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
     if (e != cudaSuccess) return e;
@@ -343,51 +346,66 @@ static cudaError_t reduce_rt(const T *A, long long lda, const T *X, long long ld
   return cudaGetLastError();
 }
 
-template <typename T>
-cudaError_t launch_reduce_tn(const T *A, long long lda, const T *X, long long ldx, long long nrows,
-                             int nbatch, int r, int C, double *out, double *work, const int *skip,
-                             cudaStream_t s, DevStatus *st) {
-  if (C <= 0 || nbatch <= 0) return cudaSuccess;
-  if (r < 1 || r > 64) return cudaErrorInvalidValue;
+template <typename T, typename OutT>
+static cudaError_t reduce_dispatch(const T *A, long long lda, const T *X, long long ldx, long long nrows,
+                                   int nbatch, int r, int C, OutT *out, double *work, const int *skip,
+                                   cudaStream_t s, DevStatus *st) {
   int nchunks, chunk_rows;
   reduce_plan(nrows, nbatch, C, current_tuning().red_ctas_per_sm * kNumSMs, nchunks, chunk_rows);
   const int bn = red_bn(C);
   const int nct = ceil_div(C, bn);
-  double *dst = nchunks > 1 ? work : out;
   cudaError_t e = cudaSuccess;
-  bool done = false;
-  if constexpr (sizeof(T) == 4)
-    done = reduce_tma_try(A, lda, X, ldx, nrows, nbatch, r, C, chunk_rows, nchunks, dst, skip, st, s, e);
-  if (done) {
-    if (e != cudaSuccess) return e;
-  } else {
+  // split-K partials are FP64 in the workspace; a single chunk writes the output type directly
+  auto run = [&](auto *dst) -> cudaError_t {
+    using D = typename std::remove_pointer<decltype(dst)>::type;
+    bool done = false;
+    cudaError_t err = cudaSuccess;
+    if constexpr (sizeof(T) == 4)
+      done = reduce_tma_try<D>(A, lda, X, ldx, nrows, nbatch, r, C, chunk_rows, nchunks, dst, skip, st, s, err);
+    if (done) return err;
 #define HODLR_RED(RTV, BNV) \
-  e = reduce_rt<T, RTV, BNV>(A, lda, X, ldx, nrows, nbatch, r, C, chunk_rows, nchunks, nct, dst, skip, s)
-  if (bn == 8) {
-    if (r <= 16) HODLR_RED(16, 8);
-    else if (r <= 32) HODLR_RED(32, 8);
-    else HODLR_RED(64, 8);
-  } else {
-    if (r <= 16) HODLR_RED(16, 64);
-    else if (r <= 32) HODLR_RED(32, 64);
-    else HODLR_RED(64, 64);
-  }
+  err = reduce_rt<T, RTV, BNV, D>(A, lda, X, ldx, nrows, nbatch, r, C, chunk_rows, nchunks, nct, dst, skip, s)
+    if (bn == 8) {
+      if (r <= 16) HODLR_RED(16, 8);
+      else if (r <= 32) HODLR_RED(32, 8);
+      else HODLR_RED(64, 8);
+    } else {
+      if (r <= 16) HODLR_RED(16, 64);
+      else if (r <= 32) HODLR_RED(32, 64);
+      else HODLR_RED(64, 64);
+    }
 #undef HODLR_RED
-  if (e != cudaSuccess) return e;
-  }
+    return err;
+  };
   if (nchunks > 1) {
+    e = run(work);
+    if (e != cudaSuccess) return e;
     const long long blk = (long long)r * C;
     dim3 grid(ceil_div(blk, 256), nbatch);
-    HODLR_LAUNCH(reduce_pass2_kernel, grid, 256, 0, s, work, nchunks, blk, out, skip);
+    HODLR_LAUNCH(reduce_pass2_kernel<OutT>, grid, 256, 0, s, work, nchunks, blk, out, skip);
+  } else {
+    e = run(out);
+    if (e != cudaSuccess) return e;
   }
   return cudaGetLastError();
 }
 
+template <typename T>
+cudaError_t launch_reduce_tn(const T *A, long long lda, const T *X, long long ldx, long long nrows,
+                             int nbatch, int r, int C, double *out, double *work, const int *skip,
+                             cudaStream_t s, DevStatus *st, float *out32) {
+  if (C <= 0 || nbatch <= 0) return cudaSuccess;
+  if (r < 1 || r > 64) return cudaErrorInvalidValue;
+  if (out32) return reduce_dispatch<T, float>(A, lda, X, ldx, nrows, nbatch, r, C, out32, work, skip, s, st);
+  return reduce_dispatch<T, double>(A, lda, X, ldx, nrows, nbatch, r, C, out, work, skip, s, st);
+}
+
 template cudaError_t launch_reduce_tn<double>(const double *, long long, const double *, long long, long long,
                                               int, int, int, double *, double *, const int *, cudaStream_t,
-                                              DevStatus *);
+                                              DevStatus *, float *);
 template cudaError_t launch_reduce_tn<float>(const float *, long long, const float *, long long, long long, int,
-                                             int, int, double *, double *, const int *, cudaStream_t, DevStatus *);
+                                             int, int, double *, double *, const int *, cudaStream_t, DevStatus *,
+                                             float *);
 
 // ------------------------------------------------------------------ K5
 // CTA tile 128 rows x 64 columns, K staged 32 at a time; each thread owns

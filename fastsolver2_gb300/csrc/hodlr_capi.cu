@@ -25,6 +25,7 @@
 #include <vector>
 
 #include "kernels.cuh"
+#include "ozaki.cuh"
 #include "resid_emul.cuh"
 
 namespace hodlr {
@@ -112,18 +113,26 @@ struct hodlr_ctx {
   double *capLU = nullptr;
   int *cap_ipiv = nullptr;
   double *Sinv = nullptr;     // [nnode][2r][2r] FP64 capacitance inverses
-  float2 *Sinv2 = nullptr;    // their double-word split (mixed mode)
+  float2 *Sinv2 = nullptr;    // their double-word split (unused by the sweeps)
+  float *Sinv32 = nullptr;    // mixed mode: FP32 inverses (from the FP64-factored systems)
   double *Dinv = nullptr;     // [nleaf][m][m] leaf inverses (FP64 mode)
   float *Dinv32 = nullptr;    // (mixed mode)
   bool factored = false;
   // workspaces
   double *Tbuf = nullptr, *Wbuf = nullptr, *eta = nullptr, *red = nullptr;
   float *eta32 = nullptr;   // mixed: capacitance solutions rounded for the FP32 updates
+  float *Tbuf32 = nullptr;  // mixed: FP32 reductions V^T X of the sweeps
   double *X64 = nullptr, *R64 = nullptr, *B64 = nullptr, *norms = nullptr, *nwork = nullptr;
   float *X32 = nullptr;
   // double-word (hi, lo) copies for the emulated FP64 residual (mixed mode)
   float2 *D2 = nullptr, *U2 = nullptr, *V2 = nullptr, *X2 = nullptr, *R2 = nullptr, *T2 = nullptr;
   bool emulated = false;
+  // tensor-core residual (HODLR_RESID_FP64_TENSOR): digit slices of D (row
+  // scaled), U (row scaled), V (64-row chunks), the iterate X and the
+  // coupling blocks T', with their power-of-two exponents
+  bool oz = false;
+  __nv_bfloat16 *Dsl = nullptr, *Usl = nullptr, *Vsl = nullptr, *Xsl = nullptr, *Tsl = nullptr;
+  int *Dexp = nullptr, *Uexp = nullptr, *Vexp = nullptr, *Xexp = nullptr, *Texp = nullptr;
   size_t tbuf_elems = 0, eta_elems = 0, red_elems = 0;
   DevStatus *dst = nullptr, *hst = nullptr;
   // timing
@@ -274,9 +283,14 @@ static void plan_sizes(hodlr_ctx *h) {
     et = std::max(et, (size_t)h->nodes(l) * 2 * r * (size_t)l * r);
     et = std::max(et, (size_t)h->nodes(l) * 2 * r * (size_t)k);
     red = std::max(red, reduce_workspace_doubles(rows, nb, r, (int)ct, 8));
-    red = std::max(red, reduce_workspace_doubles(rows, nb, r, k, 8));
     red = std::max(red, reduce_workspace_doubles(rows, nb, r, r, 8));
-    red = std::max(red, dw_reduce_workspace_doubles(rows, nb, r, k));
+    // a solve may use any nrhs <= kmax, and the split-K plans are not
+    // monotone in the column count: size for every count
+    for (int c = 1; c <= k; ++c) {
+      red = std::max(red, reduce_workspace_doubles(rows, nb, r, c, 8));
+      red = std::max(red, dw_reduce_workspace_doubles(rows, nb, r, c));
+      if (rows % kOzChunk == 0) red = std::max(red, oz_reduce_workspace_doubles(rows, nb, r, c));
+    }
   }
   h->tbuf_elems = tb;
   h->eta_elems = et;
@@ -390,9 +404,11 @@ static int cap_apply(hodlr_ctx *h, int l, int C, long long tb_stride, bool trans
   ca.tb_stride = tb_stride;
   ca.scale = h->slev(l);
   ca.sinv = h->Sinv;
-  ca.sinv2 = h->mixed ? h->Sinv2 : nullptr;
+  ca.sinv2 = nullptr;
+  ca.sinv32 = h->mixed ? h->Sinv32 : nullptr;
   ca.eta = h->eta;
-  if (h->mixed) {  // the consumers are FP32 updates: write FP32, with the solve's row scaling applied
+  if (h->mixed) {  // FP32 T blocks in, FP32 eta out for the FP32 updates (the solve's row scaling applied)
+    ca.Tb32 = h->Tbuf32;
     ca.eta32 = h->eta32;
     ca.out_scale = trans ? h->slev(l) : nullptr;
   }
@@ -433,16 +449,19 @@ template <typename T> static int factor_sweep(hodlr_ctx *h) {
     const long long rows = h->rows(l);
     const int Cd = l * r, Ct = Cd + r;
     PHASE(h, HODLR_PHASE_REDUCE,
-          launch_reduce_tn<T>(Vt + (long long)l * n * r, n, Ut, n, rows, nb, r, Ct, h->Tbuf, h->red, nullptr, s, h->dst));
+          launch_reduce_tn<T>(Vt + (long long)l * n * r, n, Ut, n, rows, nb, r, Ct, h->Tbuf, h->red, nullptr, s, h->dst,
+                              sizeof(T) == 4 ? h->Tbuf32 : nullptr));
     CapFactorArgs cf{};
     cf.Tb = h->Tbuf;
+    if (sizeof(T) == 4) cf.Tb32 = h->Tbuf32;
     cf.tb_stride = (long long)r * Ct;
     cf.scale = h->slev(l);
     cf.ucol = Cd;
     cf.cap_lu = h->capLU;
     cf.cap_ipiv = h->cap_ipiv;
     cf.sinv = h->Sinv;
-    cf.sinv2 = h->mixed ? h->Sinv2 : nullptr;
+    cf.sinv2 = nullptr;
+    cf.sinv32 = h->mixed ? h->Sinv32 : nullptr;
     cf.r = r;
     cf.nnode = h->nodes(l);
     cf.node_base = h->node_base(l);
@@ -488,7 +507,9 @@ static int solve_sweep(hodlr_ctx *h, T *X, long long ldx, int k, bool trans, con
     const long long rows = h->rows(l);
     const T *Ared = trans ? Ut + (long long)l * r * n : Vt + (long long)l * n * r;
     const T *Aupd = trans ? Vt + (long long)l * n * r : Ut + (long long)l * r * n;
-    PHASE(h, HODLR_PHASE_REDUCE, launch_reduce_tn<T>(Ared, n, X, ldx, rows, nb, r, k, h->Tbuf, h->red, skip, s, h->dst));
+    PHASE(h, HODLR_PHASE_REDUCE,
+          launch_reduce_tn<T>(Ared, n, X, ldx, rows, nb, r, k, h->Tbuf, h->red, skip, s, h->dst,
+                              sizeof(T) == 4 ? h->Tbuf32 : nullptr));
     CKS(cap_apply(h, l, k, (long long)r * k, trans, skip));
     UpdateArgs ua{};
     ua.A = Aupd;
@@ -635,9 +656,35 @@ static int residual_emulated(hodlr_ctx *h, bool trans, const double *X, long lon
   return HODLR_OK;
 }
 
+// R = B - A X with the digit-product GEMMs on the tensor cores (forward only).
+static int residual_tensor(hodlr_ctx *h, const double *X, long long ldx, const double *B, long long ldb,
+                           double *R, long long ldr, int k, const int *skip) {
+  const long long n = h->n;
+  const int m = h->m, L = h->L, r = h->r;
+  cudaStream_t s = h->st;
+  PHASE(h, HODLR_PHASE_MISC, launch_oz_slice_cols(X, ldx, n, k, h->Xsl, n, n * k, h->Xexp, skip, s));
+  PHASE(h, HODLR_PHASE_RESID_LEAF,
+        launch_oz_leaf(h->Dsl, h->Dexp, m, h->nleaf, h->Xsl, h->Xexp, n, k, B, ldb, h->R2, n, skip, s));
+  for (int l = 0; l < L; ++l) {
+    const int nb = h->nb(l);
+    const long long rows = h->rows(l);
+    PHASE(h, HODLR_PHASE_RESID_REDUCE,
+          launch_oz_reduce(h->Vsl + (long long)l * r * n, (long long)L * r * n,
+                           h->Vexp + (long long)l * (n / kOzChunk) * r, r, h->Xsl, h->Xexp, n, k, rows, nb, h->Tbuf,
+                           h->red, skip, s));
+    PHASE(h, HODLR_PHASE_MISC, launch_oz_slice_tprime(h->Tbuf, h->slev(l), r, k, nb, h->Tsl, h->Texp, skip, s));
+    PHASE(h, HODLR_PHASE_RESID_UPDATE,
+          launch_oz_update(h->Usl + (long long)l * n * r, (long long)L * n * r, h->Uexp + (long long)l * n, r,
+                           h->Tsl, h->Texp, k, rows, nb, h->R2, n, skip, s));
+  }
+  PHASE(h, HODLR_PHASE_MISC, launch_merge(h->R2, n, R, ldr, n, k, skip, s));
+  return HODLR_OK;
+}
+
 // R = B - op(A) X, FP64-accurate, with the handle's residual arithmetic.
 static int residual(hodlr_ctx *h, bool trans, const double *X, long long ldx, const double *B, long long ldb,
                     double *R, long long ldr, int k, const int *skip) {
+  if (h->oz && !trans) return residual_tensor(h, X, ldx, B, ldb, R, ldr, k, skip);
   if (h->emulated) return residual_emulated(h, trans, X, ldx, B, ldb, R, ldr, k, skip);
   return matvec_fp64(h, trans, X, ldx, B, ldb, R, ldr, k, -1.0, skip);
 }
@@ -684,6 +731,11 @@ static int prepare_leaves(hodlr_ctx *h, long long leaf0 = 0, long long count = -
     const long long mm = (long long)h->m * h->m, dm = count * mm;
     CK(launch_split(h->D + leaf0 * mm, dm, h->D2 + leaf0 * mm, dm, dm, 1, nullptr, h->st));
   }
+  if (h->oz && count > 0) {  // rows of the leaf blocks, each scaled by its own exponent
+    const long long m = h->m, mm = m * m;
+    CK(launch_oz_slice_rows(h->D + leaf0 * mm, m, mm, 1, m, count * m, (int)m, h->Dsl + leaf0 * mm, m,
+                            h->n * m, h->Dexp + leaf0 * m, h->st));
+  }
   return HODLR_OK;
 }
 
@@ -696,6 +748,15 @@ static int prepare_level(hodlr_ctx *h, int l, long long row0 = 0, long long coun
   if (h->emulated) {
     CK(launch_split(h->Ulev(l) + row0, n, h->U2 + off, n, count, h->r, nullptr, h->st));
     CK(launch_split(h->Vlev(l) + row0, n, h->V2 + off, n, count, h->r, nullptr, h->st));
+  }
+  if (h->oz) {
+    const long long r = h->r, L = h->L;
+    // U: row-scaled digits, rows of r contiguous entries
+    CK(launch_oz_slice_rows(h->Ulev(l) + row0, count, 0, 1, n, count, (int)r, h->Usl + l * n * r + row0 * r, r,
+                            L * n * r, h->Uexp + l * n + row0, h->st));
+    // V: digits scaled per 64-row chunk of each column, column-major
+    CK(launch_oz_slice_cols(h->Vlev(l) + row0, n, count, (int)r, h->Vsl + l * r * n + row0, n, L * r * n,
+                            h->Vexp + l * (n / kOzChunk) * r + (row0 / kOzChunk) * r, nullptr, h->st));
   }
   return HODLR_OK;
 }
@@ -732,6 +793,8 @@ static int check_common(const hodlr_desc &d) {
     return set_err(HODLR_ERR_INVALID_ARG, "unknown precision mode");
   if (d.precision == HODLR_PREC_MIXED && !(d.refine_tol > 0.0))
     return set_err(HODLR_ERR_INVALID_ARG, "mixed mode needs refine_tol > 0");
+  if (d.precision == HODLR_PREC_MIXED && (d.residual < HODLR_RESID_FP64 || d.residual > HODLR_RESID_FP64_TENSOR))
+    return set_err(HODLR_ERR_INVALID_ARG, "unknown residual mode");
   if ((long long)d.leaf * d.leaf * 8 > (1LL << 31)) return set_err(HODLR_ERR_INVALID_ARG, "leaf too large");
   return HODLR_OK;
 }
@@ -782,8 +845,8 @@ static int create_ctx(const hodlr_desc &d, const std::vector<int> &sys_levels, h
   ALLOC(h->ipiv, int, (size_t)n);
   ALLOC(h->capLU, double, (size_t)std::max(1, h->nnode) * 4 * r * r);
   ALLOC(h->cap_ipiv, int, (size_t)std::max(1, h->nnode) * 2 * r);
-  ALLOC(h->Sinv, double, (size_t)std::max(1, h->nnode) * 4 * r * r);
-  if (h->mixed) ALLOC(h->Sinv2, float2, (size_t)std::max(1, h->nnode) * 4 * r * r);
+  if (!h->mixed) ALLOC(h->Sinv, double, (size_t)std::max(1, h->nnode) * 4 * r * r);
+  if (h->mixed) ALLOC(h->Sinv32, float, (size_t)std::max(1, h->nnode) * 4 * r * r);
   if (leaf_apply_supported(m)) {
     if (h->mixed)
       ALLOC(h->Dinv32, float, (size_t)h->nleaf * m * m);
@@ -798,8 +861,23 @@ static int create_ctx(const hodlr_desc &d, const std::vector<int> &sys_levels, h
     ALLOC(h->X64, double, (size_t)n * k);
     ALLOC(h->R64, double, (size_t)n * k);
     ALLOC(h->B64, double, (size_t)n * k);
-    if (d.residual == HODLR_RESID_FP64_EMULATED) {
-      h->emulated = true;
+    if (d.residual == HODLR_RESID_FP64_TENSOR && L > 0 && oz_supported(m, r)) {
+      h->oz = true;
+      const size_t S = kOzSlices;
+      const int nbmax = h->nb(L - 1);
+      ALLOC(h->Dsl, __nv_bfloat16, S * n * m);
+      ALLOC(h->Dexp, int, (size_t)n);
+      ALLOC(h->Usl, __nv_bfloat16, S * n * L * r);
+      ALLOC(h->Uexp, int, (size_t)n * L);
+      ALLOC(h->Vsl, __nv_bfloat16, S * n * L * r);
+      ALLOC(h->Vexp, int, (size_t)(n / kOzChunk) * L * r);
+      ALLOC(h->Xsl, __nv_bfloat16, S * n * k);
+      ALLOC(h->Xexp, int, (size_t)(n / kOzChunk) * k);
+      ALLOC(h->Tsl, __nv_bfloat16, S * (size_t)nbmax * k * r);
+      ALLOC(h->Texp, int, (size_t)nbmax * k);
+    }
+    if (d.residual == HODLR_RESID_FP64_EMULATED || d.residual == HODLR_RESID_FP64_TENSOR) {
+      h->emulated = true;  // also the transposed solves of the tensor-core mode
       ALLOC(h->D2, float2, (size_t)h->nleaf * m * m);
       ALLOC(h->U2, float2, (size_t)n * L * r);
       ALLOC(h->V2, float2, (size_t)n * L * r);
@@ -814,7 +892,10 @@ static int create_ctx(const hodlr_desc &d, const std::vector<int> &sys_levels, h
   ALLOC(h->Tbuf, double, h->tbuf_elems);
   ALLOC(h->Wbuf, double, h->tbuf_elems);
   ALLOC(h->eta, double, h->eta_elems);
-  if (h->mixed) ALLOC(h->eta32, float, h->eta_elems);
+  if (h->mixed) {
+    ALLOC(h->eta32, float, h->eta_elems);
+    ALLOC(h->Tbuf32, float, h->tbuf_elems);
+  }
   ALLOC(h->red, double, h->red_elems);
   ALLOC(h->norms, double, 2 * (size_t)k * h->nsys);
   ALLOC(h->nwork, double, (size_t)k * std::max(64, h->forest ? h->nleaf : 0));
@@ -852,6 +933,12 @@ static int create_ctx(const hodlr_desc &d, const std::vector<int> &sys_levels, h
     if (h->V32) ok = ok && cudaMemsetAsync(h->V32, 0, sizeof(float) * nlr, h->st) == cudaSuccess;
     if (h->U2) ok = ok && cudaMemsetAsync(h->U2, 0, sizeof(float2) * nlr, h->st) == cudaSuccess;
     if (h->V2) ok = ok && cudaMemsetAsync(h->V2, 0, sizeof(float2) * nlr, h->st) == cudaSuccess;
+    if (h->oz) {
+      ok = ok && cudaMemsetAsync(h->Usl, 0, sizeof(__nv_bfloat16) * kOzSlices * nlr, h->st) == cudaSuccess;
+      ok = ok && cudaMemsetAsync(h->Vsl, 0, sizeof(__nv_bfloat16) * kOzSlices * nlr, h->st) == cudaSuccess;
+      ok = ok && cudaMemsetAsync(h->Uexp, 0, sizeof(int) * n * L, h->st) == cudaSuccess;
+      ok = ok && cudaMemsetAsync(h->Vexp, 0, sizeof(int) * (n / kOzChunk) * L * r, h->st) == cudaSuccess;
+    }
     if (!ok) {
       free_ctx(h);
       return set_err(HODLR_ERR_CUDA, "forest initialisation");

@@ -48,13 +48,14 @@ cudaError_t launch_leaf_getrs(const T *LU, const int *ipiv, int m, int nleaf, T 
 // K3: Out_b = A_b^T X_b (r x C, FP64 result) for batches b in [0, nbatch),
 // A_b / X_b = rows [b*nrows, (b+1)*nrows) of A (N x r, lda) / X (N x C, ldx).
 // Split over row chunks with a deterministic second pass.  Out: [nbatch]
-// blocks of r x C column-major (ld r).  work: scratch of at least
-// reduce_workspace_doubles(...) doubles.
+// blocks of r x C column-major (ld r); with out32 set, the result goes there
+// in FP32 instead.  work: scratch of at least reduce_workspace_doubles(...)
+// doubles.
 size_t reduce_workspace_doubles(long long nrows, int nbatch, int r, int C, int elem_bytes);
 template <typename T>
 cudaError_t launch_reduce_tn(const T *A, long long lda, const T *X, long long ldx, long long nrows,
                              int nbatch, int r, int C, double *out, double *work, const int *skip,
-                             cudaStream_t s, DevStatus *st = nullptr);
+                             cudaStream_t s, DevStatus *st = nullptr, float *out32 = nullptr);
 
 // K5: C_b += alpha * A_b * diag(scale) * op(B_b) for b in [0, nbatch):
 //   A_b = A + b*a_bstride (M x K, lda), C_b = C + b*c_bstride (M x N, ldc),
@@ -89,10 +90,12 @@ cudaError_t launch_leaf_apply(const T *Dinv, int m, int nleaf, T *X, long long l
 // inverse Sinv (plus its double-word split in sinv2 when given).
 struct CapFactorArgs {
   const double *Tb; long long tb_stride;
+  const float *Tb32;  // if set, the T blocks are read from here (FP32, same layout)
   const double *scale;
   int ucol;
   double *cap_lu; int *cap_ipiv;
   double *sinv; float2 *sinv2;
+  float *sinv32;  // mixed path: LU in FP64 only, the inverse in FP32 (from S) written here instead
   int r, nnode, node_base;
   DevStatus *st;
 };
@@ -103,6 +106,8 @@ cudaError_t launch_cap_factor(const CapFactorArgs &a, cudaStream_t s);
 // arithmetic on the FP32 pipes when sinv2 is given, DFMA otherwise.
 struct CapApplyArgs {
   const double *Tb; long long tb_stride;
+  const float *Tb32;      // mixed path: FP32 T blocks, applied with the FP32 inverse sinv32
+  const float *sinv32;
   const double *scale;
   const double *sinv; const float2 *sinv2;
   double *eta;

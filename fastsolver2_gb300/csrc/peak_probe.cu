@@ -59,9 +59,73 @@ static cudaError_t time_chain(int iters, double *tflops) {
   return cudaSuccess;
 }
 
+// Warp-level bf16 MMA (m16n8k16, FP32 accumulate) issue rate: eight
+// independent accumulator tiles per warp, register operands only.
+__global__ void __launch_bounds__(256) mma_chain_kernel(float *out, int iters) {
+  const unsigned a0 = 0x3f803f80u + threadIdx.x, a1 = a0 ^ 1u, a2 = a0 ^ 2u, a3 = a0 ^ 3u;
+  const unsigned b0 = 0x3f003f00u + threadIdx.x, b1 = b0 ^ 1u;
+  float c[8][4];
+#pragma unroll
+  for (int j = 0; j < 8; ++j)
+#pragma unroll
+    for (int q = 0; q < 4; ++q) c[j][q] = 0.f;
+  for (int i = 0; i < iters; ++i) {
+#pragma unroll
+    for (int j = 0; j < 8; ++j)
+      asm volatile(
+          "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+          "{%0,%1,%2,%3};\n"
+          : "+f"(c[j][0]), "+f"(c[j][1]), "+f"(c[j][2]), "+f"(c[j][3])
+          : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
+  }
+  float s = 0.f;
+#pragma unroll
+  for (int j = 0; j < 8; ++j) s += c[j][0] + c[j][1] + c[j][2] + c[j][3];
+  out[(long long)blockIdx.x * blockDim.x + threadIdx.x] = s;
+}
+
+static cudaError_t time_mma(int iters, double *tflops) {
+  int dev = 0, sms = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if (e != cudaSuccess) return e;
+  const int threads = 256, blocks = sms * 4;
+  float *out = nullptr;
+  e = cudaMalloc(&out, sizeof(float) * threads * blocks);
+  if (e != cudaSuccess) return e;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  float best = 0.f;
+  for (int rep = 0; rep < 3; ++rep) {
+    cudaEventRecord(e0, 0);
+    HODLR_LAUNCH(mma_chain_kernel, blocks, threads, 0, 0, out, iters);
+    cudaEventRecord(e1, 0);
+    e = cudaEventSynchronize(e1);
+    if (e == cudaSuccess) e = cudaGetLastError();
+    if (e != cudaSuccess) break;
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    if (rep > 0 && (best == 0.f || ms < best)) best = ms;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(out);
+  if (e != cudaSuccess) return e;
+  *tflops = 2.0 * 16 * 8 * 16 * 8.0 * iters * (double)(threads / 32) * blocks / (best * 1e-3) / 1e12;
+  return cudaSuccess;
+}
+
 }  // namespace hodlr
 
 using namespace hodlr;
+
+extern "C" int hodlr_probe_mma_bf16(double *tflops) {
+  if (!tflops) return set_last_error(HODLR_ERR_INVALID_ARG, "probe: null argument");
+  cudaError_t e = time_mma(4096, tflops);
+  if (e != cudaSuccess) return set_last_error(HODLR_ERR_CUDA, cudaGetErrorString(e));
+  return HODLR_OK;
+}
 
 extern "C" int hodlr_probe_fp_peaks(double *ffma_tflops, double *dfma_tflops) {
   if (!ffma_tflops || !dfma_tflops) return set_last_error(HODLR_ERR_INVALID_ARG, "probe: null argument");

@@ -56,9 +56,16 @@ enum {
 /* Residual arithmetic of the mixed path. */
 enum {
   HODLR_RESID_FP64 = 0,          /* native FP64 (DFMA) */
-  HODLR_RESID_FP64_EMULATED = 1  /* FP64-accurate double-FP32 arithmetic on
+  HODLR_RESID_FP64_EMULATED = 1, /* FP64-accurate double-FP32 arithmetic on
                                     the FP32 pipes (error-free products,
                                     double-word sums) */
+  HODLR_RESID_FP64_TENSOR = 2    /* FP64-accurate products on the tensor cores:
+                                    operands cut into exact 7-bit bf16 digits,
+                                    exact FP32 digit-product sums, double-word
+                                    combination (leaf sizes multiple of 64 up
+                                    to 256, ranks multiple of 8 up to 64; other
+                                    shapes and transposed solves use the
+                                    double-word residual) */
 };
 
 typedef struct hodlr_desc {
@@ -351,6 +358,9 @@ HODLR_API int hodlr_batch_autotune(hodlr_batch b, hodlr_tuning *per_forest, int 
  * denominators of the roofline fractions of the CUDA-core kernels.  No
  * counterpart in the reference.  Legacy default stream; synchronous. */
 HODLR_API int hodlr_probe_fp_peaks(double *ffma_tflops, double *dfma_tflops);
+/* Measured rate of the warp-level bf16 MMA (mma.sync m16n8k16, FP32
+ * accumulate) that the tensor-core residual runs on (TFLOP/s). */
+HODLR_API int hodlr_probe_mma_bf16(double *tflops);
 
 /* Kernels launched by this library since load (for launch accounting). */
 HODLR_API int64_t hodlr_kernel_launches(void);

@@ -146,7 +146,7 @@ def test_hsolve_matches_restated_oracle_bigger(hodlr):
     assert rel(W, Wo) < 1e-12
 
 
-@pytest.mark.parametrize("resid", [0, 1])
+@pytest.mark.parametrize("resid", [0, 1, 2])
 def test_mixed_refinement_reaches_tolerance(hodlr, resid):
     pr = P.gaussian_problem(128, 6, 32, nrhs=4, seed=9, orthonormal=True, decay=6.0, shift=1.5)
     s = make_solver(hodlr, pr, precision=hodlr.PREC_MIXED, residual=resid, refine_tol=1e-12)
@@ -285,3 +285,21 @@ def test_autotune_picks_valid_shapes_and_keeps_results(hodlr, precision):
             B2 = to_dev(pr.B)
             s.solve(B2)
             assert rel(to_host(B2), Xo) < (1e-12 if precision == 0 else 1e-10)
+
+
+@pytest.mark.parametrize("m,L,r,k", [(128, 6, 32, 4), (64, 5, 16, 3), (256, 3, 64, 2), (128, 4, 24, 70)])
+def test_tensor_residual_matches_fp64_residual(hodlr, m, L, r, k):
+    """The digit-product residual against a native FP64 residual of the same
+    iterate: the refinement's reported residual must be the true one."""
+    pr = P.gaussian_problem(m, L, r, nrhs=k, seed=21, orthonormal=True, decay=3.0, shift=1.5)
+    s2 = make_solver(hodlr, pr, precision=hodlr.PREC_MIXED, residual=2, refine_tol=1e-12)
+    s0 = make_solver(hodlr, pr, precision=hodlr.PREC_MIXED, residual=0, refine_tol=1e-12)
+    s2.factor()
+    s0.factor()
+    B2, B0 = to_dev(pr.B), to_dev(pr.B)
+    i2, i0 = s2.solve(B2), s0.solve(B0)
+    X2 = to_host(B2)
+    true = P.rel_residual(pr, X2)
+    assert true < 2e-12
+    assert abs(i2.rel_residual - i0.rel_residual) < 0.3 * max(i0.rel_residual, 1e-14) or true < 1e-13
+    assert i2.iterations == i0.iterations
