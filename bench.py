@@ -561,7 +561,7 @@ def run_ragged(args, fs, torch, stream, colmajor):
 
     V0, V = views(big0), views(big)
     for prec, name in ((fs.PREC_FP64, "fp64"), (fs.PREC_MIXED, "mixed")):
-        b = fs.Batch(systems, precision=prec, refine_tol=1e-12, stream=sp)
+        b = fs.Batch(systems, precision=prec, residual=args.resid, refine_tol=1e-12, stream=sp)
         b.generate(SEED, shift=4.0, Bs=V0)
         # per-forest launch shapes (mixed only: an FP64 tuning pass would take a minute)
         tunes = b.autotune() if (prec == fs.PREC_MIXED and not args.no_tune) else None

@@ -172,7 +172,7 @@ class Solver:
     returns results (factor, solve, matvec, adjoint, get_*) has finished its
     device work when it returns."""
 
-    def __init__(self, n, leaf, levels, rank, nrhs_max=1, precision=PREC_FP64, residual=RESID_FP64_EMULATED,
+    def __init__(self, n, leaf, levels, rank, nrhs_max=1, precision=PREC_FP64, residual=RESID_FP64_TENSOR,
                  refine_tol=1e-12, refine_max_iter=10, stream=None):
         self.h = None
         self.desc = Desc(n, leaf, levels, rank, nrhs_max, precision, residual, refine_tol, refine_max_iter, 0,
@@ -267,7 +267,7 @@ class Batch:
     column-major float64 CUDA tensors, one per system.  As for Solver, torch
     work that produced an input must be finished before it is passed in."""
 
-    def __init__(self, systems, precision=PREC_FP64, residual=RESID_FP64_EMULATED, refine_tol=1e-12,
+    def __init__(self, systems, precision=PREC_FP64, residual=RESID_FP64_TENSOR, refine_tol=1e-12,
                  refine_max_iter=10, stream=None):
         self.h = None
         self.systems = [tuple(int(v) for v in s) for s in systems]

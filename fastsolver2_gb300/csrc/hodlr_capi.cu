@@ -1363,7 +1363,7 @@ int hodlr_hsolve_ex(int nrow, int nrhs, int rank, int nPart, int LD, double *K, 
   d.rank = r;
   d.nrhs_max = nrhs;
   d.precision = precision;
-  d.residual = HODLR_RESID_FP64_EMULATED;
+  d.residual = HODLR_RESID_FP64_TENSOR;
   d.refine_tol = 1e-12;
   d.refine_max_iter = 10;
   d.stream = stream;

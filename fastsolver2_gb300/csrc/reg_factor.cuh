@@ -142,16 +142,20 @@ __device__ void reg_factor(Load load, T *buf, T *lu_out, int *ipiv_out, StoreInv
           }
         }
         __syncthreads();
-        T cv[TB], rv[TB];
+        // tiles wholly above or left of the trailing matrix are finished: the
+        // threads owning them skip the update (whole warps once k passes their rows)
+        if (ty * TB + TB - 1 > k && tx * TB + TB - 1 > k) {
+          T cv[TB], rv[TB];
 #pragma unroll
-        for (int i = 0; i < TB; ++i) cv[i] = colbuf[ty * TB + i];
+          for (int i = 0; i < TB; ++i) cv[i] = colbuf[ty * TB + i];
 #pragma unroll
-        for (int j = 0; j < TB; ++j) rv[j] = rowb[tx * TB + j];
+          for (int j = 0; j < TB; ++j) rv[j] = rowb[tx * TB + j];
 #pragma unroll
-        for (int i = 0; i < TB; ++i)
+          for (int i = 0; i < TB; ++i)
 #pragma unroll
-          for (int j = 0; j < TB; ++j)
-            if (ty * TB + i > k && tx * TB + j > k) a[i][j] -= cv[i] * rv[j];
+            for (int j = 0; j < TB; ++j)
+              if (ty * TB + i > k && tx * TB + j > k) a[i][j] -= cv[i] * rv[j];
+        }
         __syncthreads();
       }
     }

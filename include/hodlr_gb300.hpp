@@ -60,7 +60,7 @@ class HMatrix {
   // General form: leaf blocks in the KTree layout (ld, leaf_stride) and
   // per-level factors (set_level).
   void create(int64_t N, int rank, int nrhs_max = 1, int precision = HODLR_PREC_FP64, double refine_tol = 1e-12,
-              int residual = HODLR_RESID_FP64_EMULATED, void *stream = nullptr) {
+              int residual = HODLR_RESID_FP64_TENSOR, void *stream = nullptr) {
     destroy();
     hodlr_desc d{};
     d.n = N;
