@@ -652,17 +652,25 @@ static int residual_emulated(hodlr_ctx *h, bool trans, const double *X, long lon
     ua.skip = skip;
     PHASE(h, HODLR_PHASE_RESID_UPDATE, launch_dw_update(ua, s));
   }
-  PHASE(h, HODLR_PHASE_MISC, launch_merge(h->R2, n, R, ldr, n, k, skip, s));
+  if (R) PHASE(h, HODLR_PHASE_MISC, launch_merge(h->R2, n, R, ldr, n, k, skip, s));
   return HODLR_OK;
 }
 
 // R = B - A X with the digit-product GEMMs on the tensor cores (forward only).
-static int residual_tensor(hodlr_ctx *h, const double *X, long long ldx, const double *B, long long ldb,
-                           double *R, long long ldr, int k, const int *skip) {
+// With corr, the iterate is first updated in place: X := (first ? 0 : X) +
+// corr (the FP32 correction), fused with its slicing.  With R == nullptr the
+// result stays in the double-word buffer R2.
+static int residual_tensor(hodlr_ctx *h, double *X, long long ldx, const double *B, long long ldb, double *R,
+                           long long ldr, int k, const int *skip, const float *corr = nullptr,
+                           bool first = false) {
   const long long n = h->n;
   const int m = h->m, L = h->L, r = h->r;
   cudaStream_t s = h->st;
-  PHASE(h, HODLR_PHASE_MISC, launch_oz_slice_cols(X, ldx, n, k, h->Xsl, n, n * k, h->Xexp, skip, s));
+  if (corr)
+    PHASE(h, HODLR_PHASE_MISC,
+          launch_oz_slice_cols(first ? nullptr : X, ldx, n, k, h->Xsl, n, n * k, h->Xexp, skip, s, corr, X));
+  else
+    PHASE(h, HODLR_PHASE_MISC, launch_oz_slice_cols(X, ldx, n, k, h->Xsl, n, n * k, h->Xexp, skip, s));
   PHASE(h, HODLR_PHASE_RESID_LEAF,
         launch_oz_leaf(h->Dsl, h->Dexp, m, h->nleaf, h->Xsl, h->Xexp, n, k, B, ldb, h->R2, n, skip, s));
   for (int l = 0; l < L; ++l) {
@@ -677,14 +685,14 @@ static int residual_tensor(hodlr_ctx *h, const double *X, long long ldx, const d
           launch_oz_update(h->Usl + (long long)l * n * r, (long long)L * n * r, h->Uexp + (long long)l * n, r,
                            h->Tsl, h->Texp, k, rows, nb, h->R2, n, skip, s));
   }
-  PHASE(h, HODLR_PHASE_MISC, launch_merge(h->R2, n, R, ldr, n, k, skip, s));
+  if (R) PHASE(h, HODLR_PHASE_MISC, launch_merge(h->R2, n, R, ldr, n, k, skip, s));
   return HODLR_OK;
 }
 
 // R = B - op(A) X, FP64-accurate, with the handle's residual arithmetic.
 static int residual(hodlr_ctx *h, bool trans, const double *X, long long ldx, const double *B, long long ldb,
                     double *R, long long ldr, int k, const int *skip) {
-  if (h->oz && !trans) return residual_tensor(h, X, ldx, B, ldb, R, ldr, k, skip);
+  if (h->oz && !trans) return residual_tensor(h, const_cast<double *>(X), ldx, B, ldb, R, ldr, k, skip);
   if (h->emulated) return residual_emulated(h, trans, X, ldx, B, ldb, R, ldr, k, skip);
   return matvec_fp64(h, trans, X, ldx, B, ldb, R, ldr, k, -1.0, skip);
 }
@@ -698,7 +706,36 @@ static int mixed_solve(hodlr_ctx *h, double *B, long long ldb, int k, bool trans
   cudaStream_t s = h->st;
   const int *done = &h->dst->done;
   double *bn = h->norms, *rn = h->norms + (size_t)h->kmax * h->nsys;
-  // column norms per system (a forest's refinement test is per system)
+  const int maxit = std::max(0, h->d.refine_max_iter);
+  // the double-word residuals land in R2, and their norms and the next
+  // right-hand side come from one fused pass; the tensor-core residual also
+  // folds the correction into the slicing of the iterate
+  const bool fused = h->emulated || (h->oz && !trans);
+  const bool tensor = h->oz && !trans;
+  if (fused) {
+    const int P = h->forest ? h->nleaf : 64;
+    const int *seg = h->forest ? h->seg_leaf : nullptr;
+    PHASE(h, HODLR_PHASE_MISC, launch_rhs_prepare(B, ldb, n, k, P, h->B64, h->X32, h->nwork, s));
+    PHASE(h, HODLR_PHASE_MISC, launch_partial_norms(h->nwork, P, k, seg, h->nsys, bn, nullptr, s));
+    CKS(solve_sweep<float>(h, h->X32, n, k, trans, nullptr));
+    if (!tensor) PHASE(h, HODLR_PHASE_MISC, (launch_convert<float, double>(h->X32, n, h->X64, n, n, k, s)));
+    for (int it = 0; it <= maxit; ++it) {
+      if (tensor)
+        CKS(residual_tensor(h, h->X64, n, h->B64, n, nullptr, n, k, done, h->X32, it == 0));
+      else
+        CKS(residual(h, trans, h->X64, n, h->B64, n, nullptr, n, k, done));
+      PHASE(h, HODLR_PHASE_MISC, launch_resid_finish(h->R2, n, k, P, h->X32, h->nwork, done, s));
+      PHASE(h, HODLR_PHASE_MISC, launch_partial_norms(h->nwork, P, k, seg, h->nsys, rn, done, s));
+      CK(launch_refine_check(rn, bn, k * h->nsys, h->d.refine_tol, h->dst, it < maxit ? 1 : 0, s));
+      if (it == maxit) break;
+      CKS(solve_sweep<float>(h, h->X32, n, k, trans, done));
+      if (!tensor)
+        PHASE(h, HODLR_PHASE_MISC, (launch_add_correction<float>(h->X64, n, h->X32, n, h->X64, n, n, k, done, s)));
+    }
+    CK(launch_axpy(h->X64, n, B, ldb, n, k, 1.0, false, nullptr, s));
+    return HODLR_OK;
+  }
+  // native FP64 residual
   auto norms = [&](const double *X, double *out, const int *skip) {
     if (!h->forest) return launch_colnorms(X, n, n, k, out, h->nwork, skip, s);
     return launch_seg_colnorms(X, n, h->m, h->nleaf, k, h->seg_leaf, h->nsys, out, h->nwork, skip, s);
@@ -708,7 +745,6 @@ static int mixed_solve(hodlr_ctx *h, double *B, long long ldb, int k, bool trans
   CK((launch_convert<double, float>(h->B64, n, h->X32, n, n, k, s)));
   CKS(solve_sweep<float>(h, h->X32, n, k, trans, nullptr));
   CK((launch_convert<float, double>(h->X32, n, h->X64, n, n, k, s)));
-  const int maxit = std::max(0, h->d.refine_max_iter);
   for (int it = 0; it <= maxit; ++it) {
     CKS(residual(h, trans, h->X64, n, h->B64, n, h->R64, n, k, done));
     CK(norms(h->R64, rn, done));

@@ -148,6 +148,18 @@ cudaError_t launch_colnorms(const double *X, long long ldx, long long n, int c, 
 // work: nleaf*c doubles.  Deterministic.
 cudaError_t launch_seg_colnorms(const double *X, long long ldx, int m, int nleaf, int c, const int *seg_leaf,
                                 int nsys, double *out, double *work, const int *skip, cudaStream_t s);
+// Fused refinement passes.  Partial sums of squares go to work[j * P + p]
+// for P row blocks (P = 64 for one system; P = nleaf, one leaf per block, for
+// a forest), and launch_partial_norms turns them into column norms (seg =
+// nullptr) or per-system norms (seg = the systems' leaf offsets).
+//   rhs_prepare:  B64 = B, X32 = fl32(B)
+//   resid_finish: X32 = fl32(hi + lo) of the double-word residual R2
+cudaError_t launch_rhs_prepare(const double *B, long long ldb, long long n, int k, int P, double *B64, float *X32,
+                               double *work, cudaStream_t s);
+cudaError_t launch_resid_finish(const float2 *R2, long long n, int k, int P, float *X32, double *work,
+                                const int *skip, cudaStream_t s);
+cudaError_t launch_partial_norms(const double *work, int P, int k, const int *seg, int nseg, double *out,
+                                 const int *skip, cudaStream_t s);
 // X[:, j] *= sc[j] for the n x c tile X (FP64).
 cudaError_t launch_scale_cols(double *X, long long ldx, long long n, int c, const double *sc, cudaStream_t s);
 // Right-hand sides of the systems of a ragged batch and the stacked n x kmax

@@ -243,6 +243,73 @@ cudaError_t launch_scatter_rhs(const RhsCopy *tab, int count, long long maxn, co
   return cudaGetLastError();
 }
 
+// Fused passes of the refinement loop.  Partial sums of squares per (row
+// block, column): P blocks of `per` rows (64 slices for one system, one leaf
+// per block for a forest), each summed by its CTA in a fixed order.
+__device__ __forceinline__ void block_sumsq_store(double acc, double *work, long long idx) {
+  __shared__ double red[256];
+  red[threadIdx.x] = acc;
+  __syncthreads();
+  for (int w = 128; w; w >>= 1) {
+    if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) work[idx] = red[0];
+}
+
+// B64 = B, X32 = fl32(B), partial sums of squares of B
+__global__ void rhs_prepare_kernel(const double *B, long long ldb, long long n, int P, long long per,
+                                   double *B64, float *X32, double *work) {
+  const int j = blockIdx.y, pb = blockIdx.x;
+  const long long lo = pb * per, hi = min(n, lo + per);
+  double acc = 0.0;
+  for (long long i = lo + threadIdx.x; i < hi; i += blockDim.x) {
+    const double v = B[i + (long long)j * ldb];
+    B64[i + (long long)j * n] = v;
+    X32[i + (long long)j * n] = (float)v;
+    acc += v * v;
+  }
+  block_sumsq_store(acc, work, (long long)j * P + pb);
+}
+
+cudaError_t launch_rhs_prepare(const double *B, long long ldb, long long n, int k, int P, double *B64, float *X32,
+                               double *work, cudaStream_t s) {
+  if (n <= 0 || k <= 0) return cudaSuccess;
+  const long long per = (n + P - 1) / P;
+  HODLR_LAUNCH(rhs_prepare_kernel, dim3(P, k), 256, 0, s, B, ldb, n, P, per, B64, X32, work);
+  return cudaGetLastError();
+}
+
+// R = hi + lo of the double-word residual: X32 = fl32(R) (the correction's
+// right-hand side) and the partial sums of squares of R
+__global__ void resid_finish_kernel(const float2 *R2, long long n, int P, long long per, float *X32, double *work,
+                                    const int *skip) {
+  if (skip && *skip) return;
+  const int j = blockIdx.y, pb = blockIdx.x;
+  const long long lo = pb * per, hi = min(n, lo + per);
+  double acc = 0.0;
+  for (long long i = lo + threadIdx.x; i < hi; i += blockDim.x) {
+    const float2 rv = R2[i + (long long)j * n];
+    const double v = (double)rv.x + (double)rv.y;
+    X32[i + (long long)j * n] = (float)v;
+    acc += v * v;
+  }
+  block_sumsq_store(acc, work, (long long)j * P + pb);
+}
+
+cudaError_t launch_resid_finish(const float2 *R2, long long n, int k, int P, float *X32, double *work,
+                                const int *skip, cudaStream_t s) {
+  if (n <= 0 || k <= 0) return cudaSuccess;
+  const long long per = (n + P - 1) / P;
+  HODLR_LAUNCH(resid_finish_kernel, dim3(P, k), 256, 0, s, R2, n, P, per, X32, work, skip);
+  return cudaGetLastError();
+}
+
+// out[j*nseg + i] = sqrt(sum of the partials of segment i of column j); one
+// segment covering all P partials gives plain column norms
+cudaError_t launch_partial_norms(const double *work, int P, int k, const int *seg, int nseg, double *out,
+                                 const int *skip, cudaStream_t s);
+
 __global__ void refine_check_kernel(const double *rnorm, const double *bnorm, int c, double tol,
                                     DevStatus *st, int advance) {
   if (threadIdx.x != 0) return;
@@ -256,6 +323,26 @@ __global__ void refine_check_kernel(const double *rnorm, const double *bnorm, in
   st->resid = rel;
   if (rel <= tol) st->done = 1;
   if (advance && !st->done) st->iters += 1;
+}
+
+__global__ void partial_norm_final_kernel(const double *work, int P, int k, double *out, const int *skip) {
+  if (skip && *skip) return;
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= k) return;
+  double acc = 0.0;
+  for (int q = 0; q < P; ++q) acc += work[(long long)j * P + q];
+  out[j] = sqrt(acc);
+}
+
+cudaError_t launch_partial_norms(const double *work, int P, int k, const int *seg, int nseg, double *out,
+                                 const int *skip, cudaStream_t s) {
+  if (k <= 0) return cudaSuccess;
+  if (!seg) {
+    HODLR_LAUNCH(partial_norm_final_kernel, ceil_div(k, 64), 64, 0, s, work, P, k, out, skip);
+  } else {
+    HODLR_LAUNCH(seg_norm_kernel, ceil_div(nseg * k, 128), 128, 0, s, work, P, k, seg, nseg, out, skip);
+  }
+  return cudaGetLastError();
 }
 
 cudaError_t launch_refine_check(const double *rnorm, const double *bnorm, int c, double tol, DevStatus *st,

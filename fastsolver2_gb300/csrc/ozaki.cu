@@ -76,9 +76,11 @@ cudaError_t launch_oz_slice_rows(const double *A, long long rpb, long long bstri
   return cudaGetLastError();
 }
 
-// one warp per (64-row chunk, column)
+// one warp per (64-row chunk, column).  The value sliced is X (if given)
+// plus the FP32 correction add (if given); with xout it is also stored.
 __global__ void oz_slice_cols_kernel(const double *X, long long ldx, long long nchunk, int c, __nv_bfloat16 *out,
-                                     long long ld_out, long long sstride, int *exps, const int *skip) {
+                                     long long ld_out, long long sstride, int *exps, const int *skip,
+                                     const float *add, double *xout) {
   if (skip && *skip) return;
   const long long w = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
@@ -86,7 +88,15 @@ __global__ void oz_slice_cols_kernel(const double *X, long long ldx, long long n
   const long long ch = w / c;
   const int j = (int)(w % c);
   const long long i0 = ch * kOzChunk + lane, i1 = i0 + 32;
-  const double v0 = X[i0 + j * ldx], v1 = X[i1 + j * ldx];
+  double v0 = X ? X[i0 + j * ldx] : 0.0, v1 = X ? X[i1 + j * ldx] : 0.0;
+  if (add) {
+    v0 += (double)add[i0 + j * ldx];
+    v1 += (double)add[i1 + j * ldx];
+  }
+  if (xout) {
+    xout[i0 + j * ldx] = v0;
+    xout[i1 + j * ldx] = v1;
+  }
   unsigned long long mb = max(abs_bits(v0), abs_bits(v1));
 #pragma unroll
   for (int o = 16; o; o >>= 1) mb = max(mb, __shfl_xor_sync(0xffffffffu, mb, o));
@@ -99,12 +109,12 @@ __global__ void oz_slice_cols_kernel(const double *X, long long ldx, long long n
 
 cudaError_t launch_oz_slice_cols(const double *X, long long ldx, long long n, int c, __nv_bfloat16 *out,
                                  long long ld_out, long long slice_stride, int *exps, const int *skip,
-                                 cudaStream_t s) {
+                                 cudaStream_t s, const float *add, double *xout) {
   if (n <= 0 || c <= 0) return cudaSuccess;
   if (n % kOzChunk) return cudaErrorInvalidValue;
   const long long warps = (n / kOzChunk) * c;
   HODLR_LAUNCH(oz_slice_cols_kernel, ceil_div(warps * 32, 256), 256, 0, s, X, ldx, n / kOzChunk, c, out, ld_out,
-               slice_stride, exps, skip);
+               slice_stride, exps, skip, add, xout);
   return cudaGetLastError();
 }
 

@@ -37,10 +37,11 @@ cudaError_t launch_oz_slice_rows(const double *A, long long rpb, long long bstri
                                  long long slice_stride, int *exps, cudaStream_t s);
 // Column-scaled digits per 64-row chunk of an n x c column-major matrix
 // (n a multiple of 64): digit s of (i, j) to out[s * slice_stride + j * ld_out
-// + i]; exps[(i / 64) * c + j].
+// + i]; exps[(i / 64) * c + j].  The sliced value is X (may be null: zero)
+// plus the FP32 add (may be null); xout (may be null) receives it.
 cudaError_t launch_oz_slice_cols(const double *X, long long ldx, long long n, int c, __nv_bfloat16 *out,
                                  long long ld_out, long long slice_stride, int *exps, const int *skip,
-                                 cudaStream_t s);
+                                 cudaStream_t s, const float *add = nullptr, double *xout = nullptr);
 // Digits of the coupling blocks T'_b = diag(scale) T_{b^1} (r x k blocks of
 // T at T + b * r * k, ld r), scaled per column: digit s of (q, j) of block b
 // to out[((b * kOzSlices + s) * k + j) * r + q]; exps[b * k + j].
