@@ -267,6 +267,214 @@ __global__ void __launch_bounds__(256, 1) cap_factor_reg_kernel(CapFactorArgs a)
   if (s_info && threadIdx.x == 0) report_error(a.st, HODLR_ERR_SINGULAR_CAPACITANCE, node);
 }
 
+// Mixed path, 2r <= M (M = 32 or 64; S padded with the identity): one CTA of
+// eight warps per node, the system in registers in a column-cyclic layout --
+// warp w holds the columns j = w + 8c, lane q the rows q + 32s.  Pivot
+// search, row interchanges and the pivot row are then warp-local (integer
+// compares of |a|'s bit pattern, redux, shuffles) and each elimination step
+// costs one block barrier: the warp owning column k+1 updates, pivots and
+// scales it first and publishes its multipliers in a double buffer while
+// the other warps are still on step k (lookahead).  The FP64 LU performs
+// dgetf2's operations in its order (first row of largest |a|, whole-row
+// interchanges, reciprocal scaling unless the pivot is below the safe
+// minimum, rank-1 update of the trailing matrix).  The FP32 inverse comes
+// from these factors: the identity rides along as FP32 columns in the same
+// layout, receiving the same interchanges and (rounded) multipliers, which
+// leaves L^{-1} P there; a warp-local FP32 back substitution with U then
+// gives S^{-1} = U^{-1} L^{-1} P.
+template <int RS, typename V>
+__device__ __forceinline__ V slot_get(const V (&v)[RS], int s) {
+  V x = v[0];
+#pragma unroll
+  for (int q = 1; q < RS; ++q) x = (s == q) ? v[q] : x;
+  return x;
+}
+template <int RS, typename V>
+__device__ __forceinline__ void slot_set(V (&v)[RS], int s, V x) {
+#pragma unroll
+  for (int q = 0; q < RS; ++q) v[q] = (s == q) ? x : v[q];
+}
+// Interchange rows k and p of a warp-held column (row i at lane i % 32, slot
+// i / 32); returns the new row k (the old row p) to every lane.
+template <int RS, typename V>
+__device__ __forceinline__ V swap_rows_warp(V (&v)[RS], int k, int p, int lane) {
+  const V vp = __shfl_sync(0xffffffffu, slot_get<RS>(v, p >> 5), p & 31);
+  if (p != k) {
+    const V vk = __shfl_sync(0xffffffffu, slot_get<RS>(v, k >> 5), k & 31);
+    if (lane == (k & 31)) slot_set<RS>(v, k >> 5, vp);
+    if (lane == (p & 31)) slot_set<RS>(v, p >> 5, vk);
+  }
+  return vp;
+}
+
+template <int M>
+__global__ void __launch_bounds__(256, 2) cap_factor_cols_kernel(CapFactorArgs a) {
+  constexpr int RS = M / 32, CW = M / 8;
+  __shared__ double s_l[2][M];
+  __shared__ float s_l32[2][M];
+  __shared__ int s_p[2];
+  __shared__ int s_info;
+  __shared__ float s_u[M * M];  // U rounded to FP32, [j][i]
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int pn = blockIdx.x, node = a.node_base + pn, r = a.r, n2 = 2 * r;
+  const long long o0 = (long long)(2 * pn) * a.tb_stride, o1 = (long long)(2 * pn + 1) * a.tb_stride;
+  int *ipiv = a.cap_ipiv + (long long)node * n2;
+  double A[CW][RS];
+  float Z[CW][RS];
+#pragma unroll
+  for (int c = 0; c < CW; ++c)
+#pragma unroll
+    for (int s = 0; s < RS; ++s) {
+      const int i = lane + 32 * s, j = warp + 8 * c;
+      double v = (i == j) ? 1.0 : 0.0;
+      if (j < n2 && i < n2) {
+        auto T = [&](long long off) -> double { return a.Tb32 ? (double)a.Tb32[off] : a.Tb[off]; };
+        if (i >= r && j < r) v = (a.scale ? a.scale[i - r] : 1.0) * T(o0 + (i - r) + (long long)(a.ucol + j) * r);
+        if (i < r && j >= r) v = (a.scale ? a.scale[i] : 1.0) * T(o1 + i + (long long)(a.ucol + j - r) * r);
+      }
+      A[c][s] = v;
+      Z[c][s] = (i == j) ? 1.f : 0.f;
+    }
+  if (threadIdx.x == 0) s_info = 0;
+
+  // Owner warp of column k (its register column ck): pivot search over rows
+  // k..n2-1, interchange in this column, scaling, publication in buffer k & 1.
+  auto pivot_column = [&](int k, int ck) {
+    unsigned long long best = 0;
+    int bi = M;
+#pragma unroll
+    for (int s = 0; s < RS; ++s) {
+      const int i = lane + 32 * s;
+      unsigned long long key = static_cast<unsigned long long>(__double_as_longlong(A[ck][s])) & 0x7fffffffffffffffull;
+      if (key > 0x7ff0000000000000ull) key = 0;  // NaN is never preferred
+      if (i >= k && i < n2 && (bi == M || key > best)) {
+        best = key;
+        bi = i;
+      }
+    }
+    const unsigned hi = static_cast<unsigned>(best >> 32), lo = static_cast<unsigned>(best);
+    const unsigned mhi = __reduce_max_sync(0xffffffffu, hi);
+    const unsigned mlo = __reduce_max_sync(0xffffffffu, hi == mhi ? lo : 0u);
+    const int piv = static_cast<int>(
+        __reduce_min_sync(0xffffffffu, (hi == mhi && lo == mlo) ? static_cast<unsigned>(bi) : static_cast<unsigned>(M)));
+    const double pv = swap_rows_warp<RS>(A[ck], k, piv, lane);
+    const bool tiny = fabs(pv) < safe_min<double>();
+    const double rcp = pv != 0.0 ? 1.0 / pv : 0.0;
+    const int b = k & 1;
+#pragma unroll
+    for (int s = 0; s < RS; ++s) {
+      const int i = lane + 32 * s;
+      double l = 0.0;
+      if (i > k && i < n2) {
+        l = A[ck][s];
+        if (pv != 0.0) l = tiny ? l / pv : l * rcp;
+        A[ck][s] = l;
+      }
+      s_l[b][i] = l;
+      s_l32[b][i] = static_cast<float>(l);
+    }
+    if (lane == 0) {
+      s_p[b] = piv;
+      ipiv[k] = piv + 1;
+      if (pv == 0.0 && s_info == 0) s_info = k + 1;
+    }
+  };
+
+  if (warp == 0) pivot_column(0, 0);
+  __syncthreads();
+  for (int k = 0; k < n2; ++k) {
+    const int b = k & 1, pk = s_p[b];
+    double l[RS];
+    float l32[RS];
+#pragma unroll
+    for (int s = 0; s < RS; ++s) {
+      l[s] = s_l[b][lane + 32 * s];
+      l32[s] = s_l32[b][lane + 32 * s];
+    }
+    // rank-1 update of one column j > k (rows k+1..n2-1) with its new row-k entry u
+    auto update = [&](double(&v)[RS], double u) {
+#pragma unroll
+      for (int s = 0; s < RS; ++s) {
+        if (32 * s + 31 <= k) continue;  // slot finished (warp-uniform)
+        const int i = lane + 32 * s;
+        if (i > k && i < n2) v[s] -= l[s] * u;
+      }
+    };
+    // lookahead: the owner of column k+1 finishes it and publishes step k+1
+    const int k1 = k + 1;
+    if (k1 < n2 && (k1 & 7) == warp) {
+#pragma unroll
+      for (int c = 0; c < CW; ++c)  // constant register index: the column stays in registers
+        if (warp + 8 * c == k1) {
+          update(A[c], swap_rows_warp<RS>(A[c], k, pk, lane));
+          pivot_column(k1, c);
+        }
+    }
+#pragma unroll
+    for (int c = 0; c < CW; ++c) {
+      const int j = warp + 8 * c;
+      if (j < n2 && j != k && j != k1) {
+        const double u = swap_rows_warp<RS>(A[c], k, pk, lane);
+        if (j > k) update(A[c], u);
+      }
+      if (j < n2) {  // identity column j: same interchange, FP32 multipliers
+        const float z = swap_rows_warp<RS>(Z[c], k, pk, lane);
+#pragma unroll
+        for (int s = 0; s < RS; ++s) {
+          if (32 * s + 31 <= k) continue;
+          const int i = lane + 32 * s;
+          if (i > k && i < n2) Z[c][s] -= l32[s] * z;
+        }
+      }
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0 && s_info) report_error(a.st, HODLR_ERR_SINGULAR_CAPACITANCE, node);
+  double *gS = a.cap_lu + (long long)node * n2 * n2;
+#pragma unroll
+  for (int c = 0; c < CW; ++c)
+#pragma unroll
+    for (int s = 0; s < RS; ++s) {
+      const int i = lane + 32 * s, j = warp + 8 * c;
+      s_u[i + j * M] = static_cast<float>(A[c][s]);
+      if (i < n2 && j < n2) gS[i + (long long)j * n2] = A[c][s];
+    }
+  __syncthreads();
+  // X = U^{-1} Z, column by column in the warps that hold them
+  for (int k = n2 - 1; k >= 0; --k) {
+    const float rd = 1.f / s_u[k + k * M];
+    float u[RS];
+#pragma unroll
+    for (int s = 0; s < RS; ++s) u[s] = s_u[lane + 32 * s + k * M];
+#pragma unroll
+    for (int c = 0; c < CW; ++c) {
+      if (warp + 8 * c >= n2) continue;
+      const float x = __shfl_sync(0xffffffffu, slot_get<RS>(Z[c], k >> 5), k & 31) * rd;
+      if (lane == (k & 31)) slot_set<RS>(Z[c], k >> 5, x);
+#pragma unroll
+      for (int s = 0; s < RS; ++s) {
+        if (32 * s > k) continue;
+        const int i = lane + 32 * s;
+        if (i < k) Z[c][s] -= u[s] * x;
+      }
+    }
+  }
+  float *g32 = a.sinv32 + (long long)node * n2 * n2;
+#pragma unroll
+  for (int c = 0; c < CW; ++c)
+#pragma unroll
+    for (int s = 0; s < RS; ++s) {
+      const int i = lane + 32 * s, j = warp + 8 * c;
+      if (i < n2 && j < n2) g32[i + (long long)j * n2] = Z[c][s];
+    }
+}
+
+template <int M>
+static cudaError_t launch_cap_cols(const CapFactorArgs &a, cudaStream_t s) {
+  HODLR_LAUNCH(cap_factor_cols_kernel<M>, a.nnode, 256, 0, s, a);
+  return cudaGetLastError();
+}
+
 template <int N2>
 static cudaError_t launch_cap_reg(const CapFactorArgs &a, cudaStream_t s) {
   const size_t bytes = (size_t)N2 * N2 * 8;
@@ -281,6 +489,8 @@ cudaError_t launch_cap_factor(const CapFactorArgs &a, cudaStream_t s) {
   if (a.nnode <= 0) return cudaSuccess;
   if (a.r < 1 || a.r > 64) return cudaErrorInvalidValue;
   const int n2 = 2 * a.r;
+  if (a.sinv32 && n2 <= 32) return launch_cap_cols<32>(a, s);
+  if (a.sinv32 && n2 <= 64) return launch_cap_cols<64>(a, s);
   if (n2 == 32) return launch_cap_reg<32>(a, s);
   if (n2 == 64) return launch_cap_reg<64>(a, s);
   if (n2 == 128) return launch_cap_reg<128>(a, s);

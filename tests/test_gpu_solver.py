@@ -84,6 +84,30 @@ def test_factors_match_oracle(hodlr, m, L, r, decay):
     assert rel(cap, f["cap_lu"]) < 1e-12
 
 
+@pytest.mark.parametrize("m,L,r", [(128, 4, 32), (64, 4, 20), (64, 3, 16), (32, 3, 5), (16, 2, 1)])
+def test_mixed_capacitance_lu_matches_fp64(hodlr, m, L, r):
+    # the mixed path factors S (assembled from FP32 reductions) in FP64 with
+    # the same pivoting: same interchanges and factors within FP32 rounding
+    # of S's entries; its FP32 inverse is checked through the solves below
+    pr = P.gaussian_problem(m, L, r, nrhs=1, seed=21)
+    nnode = (1 << L) - 1
+    got = []
+    for precision in (0, 1):
+        s = make_solver(hodlr, pr, precision=precision)
+        s.factor()
+        cap = torch.empty(nnode * 4 * r * r, dtype=torch.float64, device="cuda")
+        cpiv = torch.empty(nnode * 2 * r, dtype=torch.int32, device="cuda")
+        s.get_factors(cap_lu=cap, cap_ipiv=cpiv)
+        got.append((cap.cpu().numpy(), cpiv.cpu().numpy()))
+        if precision == 1:
+            B = to_dev(pr.B)
+            info = s.solve(B)
+            assert info.status == hodlr.HODLR_OK
+            assert P.rel_residual(pr, to_host(B)) <= 1.5e-12
+    np.testing.assert_array_equal(got[0][1], got[1][1])
+    assert rel(got[1][0], got[0][0]) < 1e-4
+
+
 @pytest.mark.parametrize("m,L,r,k", [(256, 4, 16, 1), (128, 5, 32, 8), (64, 6, 8, 3), (16, 0, 1, 2)])
 def test_fp64_solve_matches_oracle(hodlr, m, L, r, k):
     pr = P.gaussian_problem(m, L, r, nrhs=k, seed=3)
