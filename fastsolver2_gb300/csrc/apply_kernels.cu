@@ -269,19 +269,23 @@ __global__ void __launch_bounds__(256, 1) cap_factor_reg_kernel(CapFactorArgs a)
 
 // Mixed path, 2r <= M (M = 32 or 64; S padded with the identity): one CTA of
 // eight warps per node, the system in registers in a column-cyclic layout --
-// warp w holds the columns j = w + 8c, lane q the rows q + 32s.  Pivot
-// search, row interchanges and the pivot row are then warp-local (integer
-// compares of |a|'s bit pattern, redux, shuffles) and each elimination step
-// costs one block barrier: the warp owning column k+1 updates, pivots and
-// scales it first and publishes its multipliers in a double buffer while
-// the other warps are still on step k (lookahead).  The FP64 LU performs
-// dgetf2's operations in its order (first row of largest |a|, whole-row
-// interchanges, reciprocal scaling unless the pivot is below the safe
-// minimum, rank-1 update of the trailing matrix).  The FP32 inverse comes
-// from these factors: the identity rides along as FP32 columns in the same
-// layout, receiving the same interchanges and (rounded) multipliers, which
-// leaves L^{-1} P there; a warp-local FP32 back substitution with U then
-// gives S^{-1} = U^{-1} L^{-1} P.
+// warp w holds the columns j = w + 8c, lane q the rows q + 32s -- for the
+// whole factorisation.  Row interchanges are implicit: rows never move, each
+// lane tracks the current position of its rows, so an elimination step
+// costs per column one shuffle of the pivot row's entry and the update of
+// the rows not yet pivotal; the factors are stored by position at the end.
+// Pivot search is warp-local (integer compares of |a|'s bit pattern, ties to
+// the lowest position, redux), and each step costs one block barrier: the
+// warp owning column k+1 updates, pivots and scales it first and publishes
+// its multipliers in a double buffer while the other warps are still on
+// step k (lookahead).  The FP64 LU performs dgetf2's operations in its order
+// (first row of largest |a|, whole-row interchanges, reciprocal scaling
+// unless the pivot is below the safe minimum, rank-1 update of the trailing
+// matrix), so factors and pivots equal the explicit-interchange ones bit for
+// bit.  The FP32 inverse comes from these factors: the identity rides along
+// as FP32 columns in the same layout, receiving the same row operations with
+// the rounded multipliers, which leaves L^{-1} P there; an FP32 back
+// substitution with U then gives S^{-1} = U^{-1} L^{-1} P.
 template <int RS, typename V>
 __device__ __forceinline__ V slot_get(const V (&v)[RS], int s) {
   V x = v[0];
@@ -289,38 +293,30 @@ __device__ __forceinline__ V slot_get(const V (&v)[RS], int s) {
   for (int q = 1; q < RS; ++q) x = (s == q) ? v[q] : x;
   return x;
 }
+// Entry of physical row p of a warp-held column (row p at lane p % 32, slot p / 32), to every lane.
 template <int RS, typename V>
-__device__ __forceinline__ void slot_set(V (&v)[RS], int s, V x) {
-#pragma unroll
-  for (int q = 0; q < RS; ++q) v[q] = (s == q) ? x : v[q];
-}
-// Interchange rows k and p of a warp-held column (row i at lane i % 32, slot
-// i / 32); returns the new row k (the old row p) to every lane.
-template <int RS, typename V>
-__device__ __forceinline__ V swap_rows_warp(V (&v)[RS], int k, int p, int lane) {
-  const V vp = __shfl_sync(0xffffffffu, slot_get<RS>(v, p >> 5), p & 31);
-  if (p != k) {
-    const V vk = __shfl_sync(0xffffffffu, slot_get<RS>(v, k >> 5), k & 31);
-    if (lane == (k & 31)) slot_set<RS>(v, k >> 5, vp);
-    if (lane == (p & 31)) slot_set<RS>(v, p >> 5, vk);
-  }
-  return vp;
+__device__ __forceinline__ V row_entry(const V (&v)[RS], int p) {
+  return __shfl_sync(0xffffffffu, slot_get<RS>(v, p >> 5), p & 31);
 }
 
 template <int M>
 __global__ void __launch_bounds__(256, 2) cap_factor_cols_kernel(CapFactorArgs a) {
   constexpr int RS = M / 32, CW = M / 8;
-  __shared__ double s_l[2][M];
+  __shared__ double s_l[2][M];   // multipliers by physical row
   __shared__ float s_l32[2][M];
-  __shared__ int s_p[2];
+  __shared__ int4 s_piv[2];      // (pivot row, row at position k, pivot row's position, -)
   __shared__ int s_info;
-  __shared__ float s_u[M * M];  // U rounded to FP32, [j][i]
+  __shared__ float s_u[M * M];   // U rounded to FP32, by position, [j][i]
+  __shared__ float s_z[M * M];   // L^{-1} P by position, [j][i]
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int pn = blockIdx.x, node = a.node_base + pn, r = a.r, n2 = 2 * r;
   const long long o0 = (long long)(2 * pn) * a.tb_stride, o1 = (long long)(2 * pn + 1) * a.tb_stride;
   int *ipiv = a.cap_ipiv + (long long)node * n2;
   double A[CW][RS];
   float Z[CW][RS];
+  int pos[RS];  // current position of this lane's rows
+#pragma unroll
+  for (int s = 0; s < RS; ++s) pos[s] = lane + 32 * s;
 #pragma unroll
   for (int c = 0; c < CW; ++c)
 #pragma unroll
@@ -337,68 +333,79 @@ __global__ void __launch_bounds__(256, 2) cap_factor_cols_kernel(CapFactorArgs a
     }
   if (threadIdx.x == 0) s_info = 0;
 
-  // Owner warp of column k (its register column ck): pivot search over rows
-  // k..n2-1, interchange in this column, scaling, publication in buffer k & 1.
-  auto pivot_column = [&](int k, int ck) {
+  // Owner warp of column k (register column c), rows at positions >= k
+  // still unpivoted: pivot choice, scaling, publication in buffer k & 1.
+  auto pivot_column = [&](int k, double(&col)[RS]) {
     unsigned long long best = 0;
-    int bi = M;
+    int bpos = M;
 #pragma unroll
     for (int s = 0; s < RS; ++s) {
-      const int i = lane + 32 * s;
-      unsigned long long key = static_cast<unsigned long long>(__double_as_longlong(A[ck][s])) & 0x7fffffffffffffffull;
+      unsigned long long key = static_cast<unsigned long long>(__double_as_longlong(col[s])) & 0x7fffffffffffffffull;
       if (key > 0x7ff0000000000000ull) key = 0;  // NaN is never preferred
-      if (i >= k && i < n2 && (bi == M || key > best)) {
+      if (pos[s] >= k && pos[s] < n2 && (bpos == M || key > best || (key == best && pos[s] < bpos))) {
         best = key;
-        bi = i;
+        bpos = pos[s];
       }
     }
     const unsigned hi = static_cast<unsigned>(best >> 32), lo = static_cast<unsigned>(best);
     const unsigned mhi = __reduce_max_sync(0xffffffffu, hi);
     const unsigned mlo = __reduce_max_sync(0xffffffffu, hi == mhi ? lo : 0u);
-    const int piv = static_cast<int>(
-        __reduce_min_sync(0xffffffffu, (hi == mhi && lo == mlo) ? static_cast<unsigned>(bi) : static_cast<unsigned>(M)));
-    const double pv = swap_rows_warp<RS>(A[ck], k, piv, lane);
-    const bool tiny = fabs(pv) < safe_min<double>();
-    const double rcp = pv != 0.0 ? 1.0 / pv : 0.0;
+    const int pp = static_cast<int>(
+        __reduce_min_sync(0xffffffffu, (hi == mhi && lo == mlo) ? static_cast<unsigned>(bpos) : static_cast<unsigned>(M)));
+    int pb = 0, pa = 0;  // physical rows at positions pp and k
+#pragma unroll
+    for (int s = 0; s < RS; ++s) {
+      const unsigned mb = __ballot_sync(0xffffffffu, pos[s] == pp), ma = __ballot_sync(0xffffffffu, pos[s] == k);
+      if (mb) pb = 32 * s + __ffs(mb) - 1;
+      if (ma) pa = 32 * s + __ffs(ma) - 1;
+    }
+    const double pv = row_entry<RS>(col, pb);
+    const unsigned long long pbits = static_cast<unsigned long long>(__double_as_longlong(pv)) & 0x7fffffffffffffffull;
+    const bool zero = pbits == 0, tiny = pbits < 0x0010000000000000ull;  // |pv| < DBL_MIN
+    const double rcp = zero ? 0.0 : 1.0 / pv;
     const int b = k & 1;
 #pragma unroll
     for (int s = 0; s < RS; ++s) {
-      const int i = lane + 32 * s;
+      const int phys = lane + 32 * s;
+      const int np = phys == pb ? k : (phys == pa ? pp : pos[s]);  // position after the interchange
       double l = 0.0;
-      if (i > k && i < n2) {
-        l = A[ck][s];
-        if (pv != 0.0) l = tiny ? l / pv : l * rcp;
-        A[ck][s] = l;
+      if (np > k && np < n2) {
+        l = col[s];
+        if (!zero) l = tiny ? l / pv : l * rcp;
+        col[s] = l;
       }
-      s_l[b][i] = l;
-      s_l32[b][i] = static_cast<float>(l);
+      s_l[b][phys] = l;
+      s_l32[b][phys] = static_cast<float>(l);
     }
     if (lane == 0) {
-      s_p[b] = piv;
-      ipiv[k] = piv + 1;
-      if (pv == 0.0 && s_info == 0) s_info = k + 1;
+      s_piv[b] = make_int4(pb, pa, pp, 0);
+      ipiv[k] = pp + 1;
+      if (zero && s_info == 0) s_info = k + 1;
     }
   };
 
-  if (warp == 0) pivot_column(0, 0);
+  if (warp == 0) pivot_column(0, A[0]);
   __syncthreads();
   for (int k = 0; k < n2; ++k) {
-    const int b = k & 1, pk = s_p[b];
+    const int b = k & 1;
+    const int4 pv4 = s_piv[b];
+    const int pb = pv4.x, pa = pv4.y, pp = pv4.z;
+    bool rem[RS];
     double l[RS];
     float l32[RS];
 #pragma unroll
     for (int s = 0; s < RS; ++s) {
-      l[s] = s_l[b][lane + 32 * s];
-      l32[s] = s_l32[b][lane + 32 * s];
+      const int phys = lane + 32 * s;
+      pos[s] = phys == pb ? k : (phys == pa ? pp : pos[s]);
+      rem[s] = pos[s] > k && pos[s] < n2;
+      l[s] = s_l[b][phys];
+      l32[s] = s_l32[b][phys];
     }
-    // rank-1 update of one column j > k (rows k+1..n2-1) with its new row-k entry u
-    auto update = [&](double(&v)[RS], double u) {
+    auto update = [&](double(&v)[RS]) {
+      const double u = row_entry<RS>(v, pb);
 #pragma unroll
-      for (int s = 0; s < RS; ++s) {
-        if (32 * s + 31 <= k) continue;  // slot finished (warp-uniform)
-        const int i = lane + 32 * s;
-        if (i > k && i < n2) v[s] -= l[s] * u;
-      }
+      for (int s = 0; s < RS; ++s)
+        if (rem[s]) v[s] -= l[s] * u;
     };
     // lookahead: the owner of column k+1 finishes it and publishes step k+1
     const int k1 = k + 1;
@@ -406,25 +413,19 @@ __global__ void __launch_bounds__(256, 2) cap_factor_cols_kernel(CapFactorArgs a
 #pragma unroll
       for (int c = 0; c < CW; ++c)  // constant register index: the column stays in registers
         if (warp + 8 * c == k1) {
-          update(A[c], swap_rows_warp<RS>(A[c], k, pk, lane));
-          pivot_column(k1, c);
+          update(A[c]);
+          pivot_column(k1, A[c]);
         }
     }
 #pragma unroll
     for (int c = 0; c < CW; ++c) {
       const int j = warp + 8 * c;
-      if (j < n2 && j != k && j != k1) {
-        const double u = swap_rows_warp<RS>(A[c], k, pk, lane);
-        if (j > k) update(A[c], u);
-      }
-      if (j < n2) {  // identity column j: same interchange, FP32 multipliers
-        const float z = swap_rows_warp<RS>(Z[c], k, pk, lane);
+      if (j < n2 && j > k1) update(A[c]);
+      if (j < n2) {  // identity column j: the same row operation with the FP32 multipliers
+        const float z = row_entry<RS>(Z[c], pb);
 #pragma unroll
-        for (int s = 0; s < RS; ++s) {
-          if (32 * s + 31 <= k) continue;
-          const int i = lane + 32 * s;
-          if (i > k && i < n2) Z[c][s] -= l32[s] * z;
-        }
+        for (int s = 0; s < RS; ++s)
+          if (rem[s]) Z[c][s] -= l32[s] * z;
       }
     }
     __syncthreads();
@@ -435,12 +436,17 @@ __global__ void __launch_bounds__(256, 2) cap_factor_cols_kernel(CapFactorArgs a
   for (int c = 0; c < CW; ++c)
 #pragma unroll
     for (int s = 0; s < RS; ++s) {
-      const int i = lane + 32 * s, j = warp + 8 * c;
-      s_u[i + j * M] = static_cast<float>(A[c][s]);
-      if (i < n2 && j < n2) gS[i + (long long)j * n2] = A[c][s];
+      const int j = warp + 8 * c;
+      s_u[pos[s] + j * M] = static_cast<float>(A[c][s]);
+      s_z[pos[s] + j * M] = Z[c][s];
+      if (pos[s] < n2 && j < n2) gS[pos[s] + (long long)j * n2] = A[c][s];
     }
   __syncthreads();
-  // X = U^{-1} Z, column by column in the warps that hold them
+#pragma unroll
+  for (int c = 0; c < CW; ++c)
+#pragma unroll
+    for (int s = 0; s < RS; ++s) Z[c][s] = s_z[lane + 32 * s + (warp + 8 * c) * M];
+  // X = U^{-1} Z, column by column in the warps that hold them (rows by position now)
   for (int k = n2 - 1; k >= 0; --k) {
     const float rd = 1.f / s_u[k + k * M];
     float u[RS];
@@ -449,13 +455,12 @@ __global__ void __launch_bounds__(256, 2) cap_factor_cols_kernel(CapFactorArgs a
 #pragma unroll
     for (int c = 0; c < CW; ++c) {
       if (warp + 8 * c >= n2) continue;
-      const float x = __shfl_sync(0xffffffffu, slot_get<RS>(Z[c], k >> 5), k & 31) * rd;
-      if (lane == (k & 31)) slot_set<RS>(Z[c], k >> 5, x);
+      const float x = row_entry<RS>(Z[c], k) * rd;
 #pragma unroll
       for (int s = 0; s < RS; ++s) {
-        if (32 * s > k) continue;
         const int i = lane + 32 * s;
-        if (i < k) Z[c][s] -= u[s] * x;
+        if (i == k) Z[c][s] = x;
+        else if (i < k) Z[c][s] -= u[s] * x;
       }
     }
   }
