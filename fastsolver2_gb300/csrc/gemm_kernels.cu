@@ -58,6 +58,25 @@ bool make_tensor_map_f32(CUtensorMap *map, const float *base, long long rows, lo
            CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
+bool make_tensor_map_bf16(CUtensorMap *map, const void *base, long long inner, long long outer, long long ld,
+                          int box_inner, int box_outer, int swizzle_bytes) {
+  EncodeTiledFn f = encode_fn();
+  if (!f || !base || inner < 1 || outer < 1) return false;
+  if ((reinterpret_cast<uintptr_t>(base) & 15) || (ld * 2) % 16 || ld < inner) return false;
+  if (box_inner * 2 > swizzle_bytes && swizzle_bytes > 0) return false;
+  cuuint64_t dims[2] = {(cuuint64_t)inner, (cuuint64_t)outer};
+  cuuint64_t strides[1] = {(cuuint64_t)ld * 2};
+  cuuint32_t box[2] = {(cuuint32_t)box_inner, (cuuint32_t)box_outer};
+  cuuint32_t es[2] = {1, 1};
+  const CUtensorMapSwizzle sw = swizzle_bytes == 128  ? CU_TENSOR_MAP_SWIZZLE_128B
+                                : swizzle_bytes == 64 ? CU_TENSOR_MAP_SWIZZLE_64B
+                                : swizzle_bytes == 32 ? CU_TENSOR_MAP_SWIZZLE_32B
+                                                      : CU_TENSOR_MAP_SWIZZLE_NONE;
+  return f(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void *>(base), dims, strides, box, es,
+           CU_TENSOR_MAP_INTERLEAVE_NONE, sw, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+           CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
 // ------------------------------------------------------------------ K3
 // output columns per CTA: 64, or 8 for narrow right-hand sides (C <= 8)
 static inline int red_bn(int C) { return C <= 8 ? 8 : 64; }

@@ -18,6 +18,7 @@
 #include <atomic>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <string>
@@ -131,6 +132,9 @@ struct hodlr_ctx {
   // scaled), U (row scaled), V (64-row chunks), the iterate X and the
   // coupling blocks T', with their power-of-two exponents
   bool oz = false;
+  // the leaf and update products in one tcgen05 pass (oz_tc.cu); Tsl / Texp
+  // then hold every level's T' digits one level after another
+  bool oz_tc = false;
   __nv_bfloat16 *Dsl = nullptr, *Usl = nullptr, *Vsl = nullptr, *Xsl = nullptr, *Tsl = nullptr;
   int *Dexp = nullptr, *Uexp = nullptr, *Vexp = nullptr, *Xexp = nullptr, *Texp = nullptr;
   size_t tbuf_elems = 0, eta_elems = 0, red_elems = 0;
@@ -671,6 +675,27 @@ static int residual_tensor(hodlr_ctx *h, double *X, long long ldx, const double 
           launch_oz_slice_cols(first ? nullptr : X, ldx, n, k, h->Xsl, n, n * k, h->Xexp, skip, s, corr, X));
   else
     PHASE(h, HODLR_PHASE_MISC, launch_oz_slice_cols(X, ldx, n, k, h->Xsl, n, n * k, h->Xexp, skip, s));
+  if (h->oz_tc) {
+    // every level's reduction and T' digits first, then the leaf and all
+    // update products in one pass
+    long long toff = 0, eoff = 0;
+    for (int l = 0; l < L; ++l) {
+      const int nb = h->nb(l);
+      PHASE(h, HODLR_PHASE_RESID_REDUCE,
+            launch_oz_reduce(h->Vsl + (long long)l * r * n, (long long)L * r * n,
+                             h->Vexp + (long long)l * (n / kOzChunk) * r, r, h->Xsl, h->Xexp, n, k, h->rows(l), nb,
+                             h->Tbuf, h->red, skip, s));
+      PHASE(h, HODLR_PHASE_MISC,
+            launch_oz_slice_tprime(h->Tbuf, h->slev(l), r, k, nb, h->Tsl + toff * r, h->Texp + eoff, skip, s));
+      toff += (long long)nb * kOzSlices * k;
+      eoff += (long long)nb * k;
+    }
+    PHASE(h, HODLR_PHASE_RESID_UPDATE,
+          launch_oz_tc_resid(h->Dsl, h->Dexp, h->Xsl, h->Xexp, h->Usl, h->Uexp, h->Tsl, h->Texp, n, m, L, r, k,
+                             h->lev_nb.data(), h->lev_rows.data(), B, ldb, h->R2, n, skip, h->dst, s));
+    if (R) PHASE(h, HODLR_PHASE_MISC, launch_merge(h->R2, n, R, ldr, n, k, skip, s));
+    return HODLR_OK;
+  }
   PHASE(h, HODLR_PHASE_RESID_LEAF,
         launch_oz_leaf(h->Dsl, h->Dexp, m, h->nleaf, h->Xsl, h->Xexp, n, k, B, ldb, h->R2, n, skip, s));
   for (int l = 0; l < L; ++l) {
@@ -909,8 +934,13 @@ static int create_ctx(const hodlr_desc &d, const std::vector<int> &sys_levels, h
       ALLOC(h->Vexp, int, (size_t)(n / kOzChunk) * L * r);
       ALLOC(h->Xsl, __nv_bfloat16, S * n * k);
       ALLOC(h->Xexp, int, (size_t)(n / kOzChunk) * k);
-      ALLOC(h->Tsl, __nv_bfloat16, S * (size_t)nbmax * k * r);
-      ALLOC(h->Texp, int, (size_t)nbmax * k);
+      const char *no_tc = getenv("HODLR_NO_TCGEN05");  // A/B switch for the mma.sync kernels
+      h->oz_tc = oz_tc_supported(m, r, k) && L <= 32 && !(no_tc && no_tc[0] == '1');
+      size_t nball = 0;
+      for (int l = 0; l < L; ++l) nball += (size_t)h->nb(l);
+      const size_t nbt = h->oz_tc ? nball : (size_t)nbmax;
+      ALLOC(h->Tsl, __nv_bfloat16, S * nbt * k * r);
+      ALLOC(h->Texp, int, nbt * k);
     }
     if (d.residual == HODLR_RESID_FP64_EMULATED || d.residual == HODLR_RESID_FP64_TENSOR) {
       h->emulated = true;  // also the transposed solves of the tensor-core mode

@@ -1,0 +1,468 @@
+// FP64-accurate residual R2 = split(B) - D X - sum_l U_l T'_l on the
+// 5th-generation tensor cores (tcgen05, accumulators in tensor memory).
+//
+// One pass over 128-row tiles: the leaf term and every level's update term
+// of a tile accumulate in the registers of the epilogue warps, so the
+// double-word residual is written once, not once per level.  The operands
+// are the exact 7-bit bf16 digits of the Ozaki splitting (ozaki.cuh): a
+// "group" is one exponent-scaled product -- a 64-row chunk of the leaf
+// product (A = D digits, scaled per row; B = X digits, scaled per 64-row
+// chunk and column) or one level's update (A = U_l digits per row, B = T'_l
+// digits per column) -- and its 28 digit pairs (s + t <= 6) accumulate into
+// seven per-diagonal FP32 sums, which are exact (at most 7 x 64 products
+// below 2^14 each).
+//
+// CTA (persistent, one per SM): warp 0 streams the digit tiles with TMA
+// (64-byte swizzled K-major 32-wide slabs, A 128 x 32, B 64 x 32) through a
+// 16-stage ring; one thread of warp 1 issues tcgen05.mma (M 128, N 64,
+// K 16, bf16 -> f32) into tensor memory, diagonals 0-3 in one region and
+// 4-6 in another so that the epilogue drains one while the next group's
+// products fill the other; eight epilogue warps read the sums with
+// tcgen05.ld (warp w sees lanes 32 (w % 4) .. + 31, i.e. those rows; warps
+// 2-5 take columns 0-31, warps 6-9 columns 32-63), fold them with the
+// group's exponents into the double-word running sum and finally write
+// R2 = split(B) - sum.  Every wait is bounded: on timeout the kernel
+// records HODLR_ERR_TIMEOUT, all roles stop, in-flight products and copies
+// are waited for (bounded) and the tensor memory is released.
+#include <algorithm>
+
+#include "kernels.cuh"
+#include "ozaki.cuh"
+#include "tma.cuh"
+
+namespace hodlr {
+
+namespace {
+
+constexpr int kRows = 128;   // tile rows (MMA M)
+constexpr int kCols = 64;    // tile columns (MMA N)
+constexpr int kSlab = 32;    // K per stage: one 64-byte swizzled row
+constexpr int kStages = 16;
+constexpr int kABytes = kRows * kSlab * 2;
+constexpr int kBBytes = kCols * kSlab * 2;
+constexpr int kStageBytes = kABytes + kBBytes;
+constexpr int kEpiWarps = 8;
+constexpr int kThreads = 64 + 32 * kEpiWarps;
+constexpr unsigned kTmemCols = 512;
+// kind::f16 instruction descriptor: D f32 (bits 4-5 = 1), A and B bf16
+// (bits 7-9, 10-12 = 1), both K-major, N >> 3 at bit 17, M >> 4 at bit 24.
+constexpr unsigned kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((unsigned)(kCols >> 3) << 17) |
+                            ((unsigned)(kRows >> 4) << 24);
+constexpr long long kWaitCycles = 2000000000LL;  // about one second
+
+struct Shared {
+  uint64_t full[kStages], empty[kStages];
+  uint64_t acc_full[2], acc_empty[2], drain;
+  unsigned tmem;
+  int abort;
+  int consumed;  // stages the MMA thread consumed (for the drain after an abort)
+};
+
+// Shared-memory matrix descriptor: K-major, 64-byte swizzle (rows of 64
+// bytes, 8-row atoms of 512 bytes = stride-dimension offset), version 1.
+__device__ __forceinline__ uint64_t desc_sw64(unsigned saddr) {
+  return (uint64_t)((saddr >> 4) & 0x3FFFu) | ((uint64_t)1 << 16) | ((uint64_t)(512 >> 4) << 32) |
+         ((uint64_t)1 << 46) | ((uint64_t)4 << 61);
+}
+
+__device__ __forceinline__ void tc_alloc(unsigned *dst, unsigned ncols) {
+  asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(dst)), "r"(ncols)
+               : "memory");
+}
+__device__ __forceinline__ void tc_relinquish() {
+  asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+}
+__device__ __forceinline__ void tc_dealloc(unsigned taddr, unsigned ncols) {
+  asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols) : "memory");
+}
+__device__ __forceinline__ void tc_mma(unsigned d, uint64_t a, uint64_t b, unsigned accumulate) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "setp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(d),
+      "l"(a), "l"(b), "r"(kIdesc), "r"(accumulate)
+      : "memory");
+}
+// The barrier receives one arrival when every tcgen05.mma this thread issued has completed.
+__device__ __forceinline__ void tc_commit(uint64_t *bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
+               : "memory");
+}
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_ld8(unsigned taddr, unsigned (&v)[8]) {
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+               : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7])
+               : "r"(taddr));
+}
+// Waits for this thread's tensor-memory loads; the registers pass through
+// so that no use of them is scheduled before the wait.
+template <int N>
+__device__ __forceinline__ void tc_wait_ld(unsigned (&v)[N][8]) {
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int a = 0; a < N; ++a)
+#pragma unroll
+    for (int b = 0; b < 8; ++b) asm volatile("" : "+r"(v[a][b]));
+}
+
+__device__ __forceinline__ void arrive(uint64_t *bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
+// Bounded wait that also ends when another role has aborted.
+__device__ __forceinline__ bool wait_or_abort(uint64_t *bar, unsigned parity, Shared *sh) {
+  if (mbar_try_wait(bar, parity)) return true;
+  const long long t0 = clock64();
+  while (!mbar_try_wait(bar, parity)) {
+    if (*(volatile int *)&sh->abort) return false;
+    if (clock64() - t0 > kWaitCycles) {
+      *(volatile int *)&sh->abort = 1;
+      return false;
+    }
+  }
+  return true;
+}
+
+__device__ __forceinline__ void two_sum(float a, float b, float &s, float &e) {
+  s = a + b;
+  const float bb = s - a;
+  e = (a - (s - bb)) + (b - bb);
+}
+
+// (rh, rl) += 2^ex (sum of the exact terms v[d] 2^(-7 (d0 + d)))
+template <int ND>
+__device__ __forceinline__ void fold(float &rh, float &rl, const unsigned (&v)[ND][8], int c, int d0, int ex) {
+  // 2^(-7 d) as a bit pattern (exact; d <= 6)
+  float sh = __uint_as_float(v[0][c]) * __int_as_float((127 - 7 * d0) << 23), sl = 0.f;
+#pragma unroll
+  for (int d = 1; d < ND; ++d) {
+    float s, e;
+    two_sum(sh, __uint_as_float(v[d][c]) * __int_as_float((127 - 7 * (d0 + d)) << 23), s, e);
+    sh = s;
+    sl += e;
+  }
+  sh = ldexpf(sh, ex);
+  sl = ldexpf(sl, ex);
+  float s, e;
+  two_sum(rh, sh, s, e);
+  e += rl + sl;
+  rh = s + e;
+  rl = e - (rh - s);
+}
+
+}  // namespace
+
+constexpr int kMaxLevels = 32;
+
+struct OzTcArgs {
+  // level l: blocks of lrows[l] rows from row 0 (lnb[l] of them); block b's
+  // T' digits start at line ltrow[l] + 7 k b, its column exponents at
+  // Texp + lteo[l] + k b
+  long long lrows[kMaxLevels], ltrow[kMaxLevels], lteo[kMaxLevels];
+  int lnb[kMaxLevels];
+  const int *Dexp, *Xexp, *Uexp, *Texp;
+  const double *B;
+  long long ldb;
+  float2 *R2;
+  long long ldr;
+  long long n;
+  int m, L, r, k;
+  long long items;  // row tiles x column tiles
+  int nct;          // column tiles
+  const int *skip;
+  DevStatus *st;
+};
+
+// Group g of the tile at row0: the leaf chunks always, level l when a block of it covers the tile.
+__device__ __forceinline__ bool has_group(const OzTcArgs &a, int g, int leaf_groups, long long row0) {
+  if (g < leaf_groups) return true;
+  const int l = g - leaf_groups;
+  return row0 < (long long)a.lnb[l] * a.lrows[l];
+}
+
+__global__ void __launch_bounds__(kThreads, 1)
+oz_tc_resid_kernel(const __grid_constant__ CUtensorMap mapD, const __grid_constant__ CUtensorMap mapX,
+                   const __grid_constant__ CUtensorMap mapU, const __grid_constant__ CUtensorMap mapT, OzTcArgs a) {
+  if (a.skip && *a.skip) return;
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  unsigned char *stages =
+      reinterpret_cast<unsigned char *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+  Shared *sh = reinterpret_cast<Shared *>(stages + kStages * kStageBytes);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int leaf_groups = a.m / 64, khl = (a.r + kSlab - 1) / kSlab;
+  const int groups = leaf_groups + a.L;
+
+  if (threadIdx.x == 0) {
+    for (int i = 0; i < kStages; ++i) {
+      mbar_init(&sh->full[i], 1);
+      mbar_init(&sh->empty[i], 1);
+    }
+    for (int i = 0; i < 2; ++i) {
+      mbar_init(&sh->acc_full[i], 1);
+      mbar_init(&sh->acc_empty[i], kEpiWarps);
+    }
+    mbar_init(&sh->drain, 1);
+    sh->abort = 0;
+    sh->consumed = 0;
+    mbar_fence_init();
+  }
+  if (warp == 1) {
+    tc_alloc(&sh->tmem, kTmemCols);
+    tc_relinquish();
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const unsigned tmem = sh->tmem;
+  long long issued = 0;  // stages issued by the producer thread
+
+  if (warp == 0) {
+    // ------------------------------------------------------------ producer
+    if (lane == 0) {
+      prefetch_tensormap(&mapD);
+      prefetch_tensormap(&mapX);
+      prefetch_tensormap(&mapU);
+      prefetch_tensormap(&mapT);
+      bool ok = true;
+      for (long long item = blockIdx.x; ok && item < a.items; item += gridDim.x) {
+        const long long row0 = (item / a.nct) * kRows;
+        const int j0 = (int)(item % a.nct) * kCols;
+        const long long lrow0 = row0 - row0 % a.m;
+        for (int g = 0; ok && g < groups; ++g) {
+          if (!has_group(a, g, leaf_groups, row0)) continue;
+          const int nkh = g < leaf_groups ? 2 : khl;
+          for (int kh = 0; ok && kh < nkh; ++kh)
+            for (int s = 0; s < kOzSlices; ++s) {
+              const int slot = (int)(issued % kStages);
+              if (!wait_or_abort(&sh->empty[slot], (unsigned)(((issued / kStages) & 1) ^ 1), sh)) {
+                ok = false;
+                break;
+              }
+              unsigned char *sa = stages + slot * kStageBytes, *sb = sa + kABytes;
+              mbar_arrive_expect_tx(&sh->full[slot], kStageBytes);
+              if (g < leaf_groups) {
+                const int q0 = g * 64 + kh * kSlab;  // leaf column (K) offset
+                tma_load_2d(sa, &mapD, &sh->full[slot], q0, (int)((long long)s * a.n + row0));
+                tma_load_2d(sb, &mapX, &sh->full[slot], (int)(lrow0 + q0), s * a.k + j0);
+              } else {
+                const int l = g - leaf_groups;
+                const long long b = row0 / a.lrows[l];
+                const long long trow = a.ltrow[l] + b * kOzSlices * a.k;  // block b's T' digits
+                tma_load_2d(sa, &mapU, &sh->full[slot], kh * kSlab,
+                            (int)(((long long)s * a.L + l) * a.n + row0));
+                tma_load_2d(sb, &mapT, &sh->full[slot], kh * kSlab, (int)(trow + (long long)s * a.k + j0));
+              }
+              ++issued;
+            }
+        }
+      }
+    }
+  } else if (warp == 1) {
+    // ----------------------------------------------------------- MMA issue
+    if (lane == 0) {
+      long long it = 0, gcount = 0;
+      bool ok = true;
+      for (long long item = blockIdx.x; ok && item < a.items; item += gridDim.x)
+        for (int g = 0; ok && g < groups; ++g) {
+          const long long row0 = (item / a.nct) * kRows;
+          if (!has_group(a, g, leaf_groups, row0)) continue;
+          const int nkh = g < leaf_groups ? 2 : khl;
+          const unsigned par_empty = (unsigned)((gcount & 1) ^ 1);
+          ++gcount;
+          for (int kh = 0; ok && kh < nkh; ++kh) {
+            for (int d = 0; ok && d < kOzSlices; ++d) {
+              const long long sd = it + d;
+              if (!wait_or_abort(&sh->full[sd % kStages], (unsigned)((sd / kStages) & 1), sh)) {
+                ok = false;
+                break;
+              }
+              if (kh == 0 && (d == 0 || d == 4)) {
+                if (!wait_or_abort(&sh->acc_empty[d == 0 ? 0 : 1], par_empty, sh)) {
+                  ok = false;
+                  break;
+                }
+              }
+              tc_fence_after();
+              const unsigned dt = tmem + (unsigned)(d * kCols);
+              for (int s = 0; s <= d; ++s) {
+                const unsigned sa = smem_u32(stages + ((it + s) % kStages) * kStageBytes);
+                const unsigned sb = smem_u32(stages + ((it + d - s) % kStages) * kStageBytes + kABytes);
+#pragma unroll
+                for (int kk = 0; kk < kSlab / 16; ++kk)
+                  tc_mma(dt, desc_sw64(sa + kk * 32), desc_sw64(sb + kk * 32), (kh > 0 || s > 0 || kk > 0) ? 1u : 0u);
+              }
+              if (kh == nkh - 1 && d == 3) tc_commit(&sh->acc_full[0]);
+              if (kh == nkh - 1 && d == kOzSlices - 1) tc_commit(&sh->acc_full[1]);
+            }
+            if (!ok) break;
+            for (int s = 0; s < kOzSlices; ++s) tc_commit(&sh->empty[(it + s) % kStages]);
+            it += kOzSlices;
+          }
+        }
+      sh->consumed = (int)it;
+      tc_commit(&sh->drain);  // completes once every product issued above has
+      if (!wait_or_abort(&sh->drain, 0, sh)) {
+        // the products were still running after the bounded wait: keep waiting,
+        // bounded, since the tensor memory is freed below
+        const long long t0 = clock64();
+        while (!mbar_try_wait(&sh->drain, 0) && clock64() - t0 < kWaitCycles) {
+        }
+      }
+    }
+  } else {
+    // ------------------------------------------------------------ epilogue
+    const int q = warp & 3, half = (warp - 2) >> 2;
+    const unsigned tl = tmem + ((unsigned)(32 * q) << 16);
+    long long gcount = 0;
+    bool ok = true;
+    for (long long item = blockIdx.x; ok && item < a.items; item += gridDim.x) {
+      const long long row0 = (item / a.nct) * kRows, i = row0 + 32 * q + lane;
+      const int jb = (int)(item % a.nct) * kCols + 32 * half;
+      const long long lrow0 = row0 - row0 % a.m;
+      float rh[32], rl[32];
+#pragma unroll
+      for (int c = 0; c < 32; ++c) rh[c] = rl[c] = 0.f;
+      for (int g = 0; ok && g < groups; ++g) {
+        if (!has_group(a, g, leaf_groups, row0)) continue;
+        const unsigned par = (unsigned)(gcount & 1);
+        ++gcount;
+        int erow;
+        const int *ecol;  // column exponents of the group, + j
+        if (g < leaf_groups) {
+          erow = a.Dexp[i];
+          ecol = a.Xexp + ((lrow0 + g * 64) / kOzChunk) * a.k;
+        } else {
+          const int l = g - leaf_groups;
+          const long long b = row0 / a.lrows[l];
+          erow = a.Uexp[(long long)l * a.n + i];
+          ecol = a.Texp + a.lteo[l] + b * a.k;
+        }
+        for (int reg = 0; reg < 2; ++reg) {
+          if (!wait_or_abort(&sh->acc_full[reg], par, sh)) {
+            ok = false;
+            break;
+          }
+          tc_fence_after();
+#pragma unroll
+          for (int cc = 0; cc < 4; ++cc) {
+            const int c0 = 32 * half + 8 * cc;
+            int ex[8];
+#pragma unroll
+            for (int c = 0; c < 8; ++c) {
+              const int j = jb + 8 * cc + c;
+              ex[c] = j < a.k ? erow + ecol[j] - 14 : 0;
+            }
+            if (reg == 0) {
+              unsigned v[4][8];
+#pragma unroll
+              for (int d = 0; d < 4; ++d) tc_ld8(tl + (unsigned)(d * kCols + c0), v[d]);
+              tc_wait_ld(v);
+#pragma unroll
+              for (int c = 0; c < 8; ++c) fold<4>(rh[8 * cc + c], rl[8 * cc + c], v, c, 0, ex[c]);
+            } else {
+              unsigned v[3][8];
+#pragma unroll
+              for (int d = 0; d < 3; ++d) tc_ld8(tl + (unsigned)((4 + d) * kCols + c0), v[d]);
+              tc_wait_ld(v);
+#pragma unroll
+              for (int c = 0; c < 8; ++c) fold<3>(rh[8 * cc + c], rl[8 * cc + c], v, c, 4, ex[c]);
+            }
+          }
+          tc_fence_before();
+          __syncwarp();
+          if (lane == 0) arrive(&sh->acc_empty[reg]);
+        }
+      }
+      if (!ok) break;
+#pragma unroll
+      for (int c = 0; c < 32; ++c) {
+        const int j = jb + c;
+        if (j >= a.k) continue;
+        const double bv = a.B[i + (long long)j * a.ldb];
+        const float bh = __double2float_rn(bv), bl = __double2float_rn(bv - (double)bh);
+        float s, e;
+        two_sum(bh, -rh[c], s, e);
+        e += bl - rl[c];
+        const float h = s + e;
+        a.R2[i + (long long)j * a.ldr] = make_float2(h, e - (h - s));
+      }
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x == 0 && sh->abort) report_error(a.st, HODLR_ERR_TIMEOUT, blockIdx.x);
+  if (threadIdx.x == 0 && sh->abort) {
+    // copies the producer issued but nobody consumed: wait (bounded) for them to land
+    for (long long it = sh->consumed; it < issued; ++it) {
+      const long long t0 = clock64();
+      while (!mbar_try_wait(&sh->full[it % kStages], (unsigned)((it / kStages) & 1)) && clock64() - t0 < kWaitCycles) {
+      }
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 1) {
+    tc_fence_after();
+    tc_dealloc(tmem, kTmemCols);
+  }
+}
+
+bool oz_tc_supported(int m, int r, int k) {
+  return (m == 128 || m == 256) && r % 8 == 0 && r >= 8 && r <= 64 && k >= 1;
+}
+
+cudaError_t launch_oz_tc_resid(const __nv_bfloat16 *Dsl, const int *Dexp, const __nv_bfloat16 *Xsl, const int *Xexp,
+                               const __nv_bfloat16 *Usl, const int *Uexp, const __nv_bfloat16 *Tsl, const int *Texp,
+                               long long n, int m, int L, int r, int k, const int *lev_nb, const long long *lev_rows,
+                               const double *B, long long ldb, float2 *R2, long long ldr, const int *skip,
+                               DevStatus *st, cudaStream_t s) {
+  if (k <= 0 || n <= 0) return cudaSuccess;
+  if (!oz_tc_supported(m, r, k) || n % kRows || L > kMaxLevels) return cudaErrorInvalidValue;
+  OzTcArgs a{};
+  long long nt_rows = 0, neo = 0;
+  for (int l = 0; l < L; ++l) {
+    if (lev_rows[l] % kRows) return cudaErrorInvalidValue;
+    a.lrows[l] = lev_rows[l];
+    a.lnb[l] = lev_nb[l];
+    a.ltrow[l] = nt_rows;
+    a.lteo[l] = neo;
+    nt_rows += (long long)lev_nb[l] * kOzSlices * k;
+    neo += (long long)lev_nb[l] * k;
+  }
+  CUtensorMap mD, mX, mU, mT;
+  if (!make_tensor_map_bf16(&mD, Dsl, m, (long long)kOzSlices * n, m, kSlab, kRows, 64) ||
+      !make_tensor_map_bf16(&mX, Xsl, n, (long long)kOzSlices * k, n, kSlab, kCols, 64) ||
+      !make_tensor_map_bf16(&mU, L > 0 ? (const void *)Usl : (const void *)Dsl, L > 0 ? r : m,
+                            L > 0 ? (long long)kOzSlices * L * n : 1, L > 0 ? r : m, kSlab, kRows, 64) ||
+      !make_tensor_map_bf16(&mT, L > 0 ? (const void *)Tsl : (const void *)Dsl, L > 0 ? r : m,
+                            L > 0 ? nt_rows : 1, L > 0 ? r : m, kSlab, kCols, 64))
+    return cudaErrorInvalidValue;
+  a.Dexp = Dexp;
+  a.Xexp = Xexp;
+  a.Uexp = Uexp;
+  a.Texp = Texp;
+  a.B = B;
+  a.ldb = ldb;
+  a.R2 = R2;
+  a.ldr = ldr;
+  a.n = n;
+  a.m = m;
+  a.L = L;
+  a.r = r;
+  a.k = k;
+  a.nct = (k + kCols - 1) / kCols;
+  a.items = (n / kRows) * a.nct;
+  a.skip = skip;
+  a.st = st;
+  const size_t bytes = (size_t)kStages * kStageBytes + sizeof(Shared) + 1024;
+  cudaError_t e = cudaFuncSetAttribute(oz_tc_resid_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  if (e != cudaSuccess) return e;
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const long long grid = std::min<long long>(a.items, sms > 0 ? sms : 148);
+  HODLR_LAUNCH(oz_tc_resid_kernel, (unsigned)grid, kThreads, bytes, s, mD, mX, mU, mT, a);
+  return cudaGetLastError();
+}
+
+}  // namespace hodlr

@@ -71,4 +71,16 @@ cudaError_t launch_oz_update(const __nv_bfloat16 *Usl, long long uslice, const i
                              const __nv_bfloat16 *Tsl, const int *Texp, int k, long long rows, int nb, float2 *R2,
                              long long ldr, const int *skip, cudaStream_t s);
 
+// R2 = split(B) - D X - sum_l U_l T'_l in one pass over 128-row tiles on
+// the tcgen05 tensor cores (oz_tc.cu): leaf size 128 or 256, the T' digits
+// of every level stored one level after another (level l's block b at line
+// offset sum_{l' < l} 7 k nb(l') + 7 k b, exponents at sum_{l' < l} k nb(l')
+// + k b); lev_nb / lev_rows: host arrays of the level geometry.
+bool oz_tc_supported(int m, int r, int k);
+cudaError_t launch_oz_tc_resid(const __nv_bfloat16 *Dsl, const int *Dexp, const __nv_bfloat16 *Xsl, const int *Xexp,
+                               const __nv_bfloat16 *Usl, const int *Uexp, const __nv_bfloat16 *Tsl, const int *Texp,
+                               long long n, int m, int L, int r, int k, const int *lev_nb, const long long *lev_rows,
+                               const double *B, long long ldb, float2 *R2, long long ldr, const int *skip,
+                               DevStatus *st, cudaStream_t s);
+
 }  // namespace hodlr

@@ -92,5 +92,11 @@ __device__ __forceinline__ int swz128(int row, int chunk) { return row * 128 + (
 // caller then takes its non-TMA path).
 bool make_tensor_map_f32(CUtensorMap *map, const float *base, long long rows, long long cols, long long ld,
                          int box_rows, int box_cols, bool swizzle128);
+// 2-D tensor map over a bf16 matrix stored with `inner` contiguous elements
+// per line (line pitch `ld` elements, `outer` lines); box box_inner x
+// box_outer, swizzle 0, 32, 64 or 128 bytes.  Out-of-range elements load as
+// zero.
+bool make_tensor_map_bf16(CUtensorMap *map, const void *base, long long inner, long long outer, long long ld,
+                          int box_inner, int box_outer, int swizzle_bytes);
 
 }  // namespace hodlr

@@ -327,3 +327,25 @@ def test_tensor_residual_matches_fp64_residual(hodlr, m, L, r, k):
     assert true < 2e-12
     assert abs(i2.rel_residual - i0.rel_residual) < 0.3 * max(i0.rel_residual, 1e-14) or true < 1e-13
     assert i2.iterations == i0.iterations
+
+
+@pytest.mark.parametrize("m,L,r,k", [(128, 3, 32, 4), (256, 2, 16, 3), (128, 4, 24, 70), (128, 5, 8, 64),
+                                     (256, 3, 64, 2), (128, 1, 40, 9)])
+def test_tcgen05_residual_matches_mma_sync_residual(hodlr, m, L, r, k, monkeypatch):
+    """The one-pass tcgen05 residual (leaf sizes 128 and 256) against the
+    per-level mma.sync kernels on the same digits: same refinement path,
+    residuals and solutions equal to FP64 refinement accuracy."""
+    pr = P.gaussian_problem(m, L, r, nrhs=k, seed=33, orthonormal=True, decay=3.0, shift=1.5)
+    out = {}
+    for tc in ("0", "1"):
+        monkeypatch.setenv("HODLR_NO_TCGEN05", "1" if tc == "0" else "0")
+        s = make_solver(hodlr, pr, precision=hodlr.PREC_MIXED, residual=2, refine_tol=1e-12)
+        s.factor()
+        B = to_dev(pr.B)
+        info = s.solve(B)
+        out[tc] = (to_host(B), info.iterations, info.rel_residual)
+    (X0, it0, r0), (X1, it1, r1) = out["0"], out["1"]
+    assert it0 == it1
+    assert abs(r1 - r0) <= 0.05 * r0 + 1e-15, (r0, r1)
+    assert rel(X1, X0) < 1e-11
+    assert P.rel_residual(pr, X1) < 2e-12
