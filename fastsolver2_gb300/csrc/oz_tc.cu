@@ -41,8 +41,9 @@ constexpr int kStages = 16;
 constexpr int kABytes = kRows * kSlab * 2;
 constexpr int kBBytes = kCols * kSlab * 2;
 constexpr int kStageBytes = kABytes + kBBytes;
-constexpr int kEpiWarps = 8;
+constexpr int kEpiWarps = 16;  // four per SM sub-partition; each thread one row, 16 columns
 constexpr int kThreads = 64 + 32 * kEpiWarps;
+constexpr int kEpiCols = kCols / (kEpiWarps / 4);
 constexpr unsigned kTmemCols = 512;
 // kind::f16 instruction descriptor: D f32 (bits 4-5 = 1), A and B bf16
 // (bits 7-9, 10-12 = 1), both K-major, N >> 3 at bit 17, M >> 4 at bit 24.
@@ -130,25 +131,76 @@ __device__ __forceinline__ void two_sum(float a, float b, float &s, float &e) {
   e = (a - (s - bb)) + (b - bb);
 }
 
-// (rh, rl) += 2^ex (sum of the exact terms v[d] 2^(-7 (d0 + d)))
-template <int ND>
-__device__ __forceinline__ void fold(float &rh, float &rl, const unsigned (&v)[ND][8], int c, int d0, int ex) {
-  // 2^(-7 d) as a bit pattern (exact; d <= 6)
-  float sh = __uint_as_float(v[0][c]) * __int_as_float((127 - 7 * d0) << 23), sl = 0.f;
+// 2^e for e in [-126, 127], from its bit pattern
+__device__ __forceinline__ float pow2f(int e) { return __int_as_float((e + 127) << 23); }
+
+// Running double-word sum (rh, rl) += 2^ex sum_d v[d] 2^(-7 d) for the
+// exact diagonal sums v of one group.  Diagonals 0-3 enter through
+// error-free two-sums; diagonals 4-6 are at most 2^-5 of a unit of
+// diagonal 0 and go straight into rl (rounding 2^-29 of that unit, 2^-52
+// of the largest possible leading term); rl is renormalised once per group.
+// The scale factors are built from exponent bits: the caller checks that
+// ex - 42 .. ex is a normal range (else fold_any).
+__device__ __forceinline__ void fold_hi(float &rh, float &rl, const unsigned (&v)[4][8], int c, int ex) {
+  float p = pow2f(ex);
 #pragma unroll
-  for (int d = 1; d < ND; ++d) {
+  for (int d = 0; d < 4; ++d) {
     float s, e;
-    two_sum(sh, __uint_as_float(v[d][c]) * __int_as_float((127 - 7 * (d0 + d)) << 23), s, e);
-    sh = s;
-    sl += e;
+    two_sum(rh, __uint_as_float(v[d][c]) * p, s, e);
+    rh = s;
+    rl += e;
+    p *= 0.0078125f;  // 2^-7
   }
-  sh = ldexpf(sh, ex);
-  sl = ldexpf(sl, ex);
+}
+__device__ __forceinline__ void fold_lo(float &rh, float &rl, const unsigned (&v)[3][8], int c, int ex) {
+  float p = pow2f(ex - 28);
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    rl = fmaf(__uint_as_float(v[d][c]), p, rl);
+    p *= 0.0078125f;
+  }
   float s, e;
-  two_sum(rh, sh, s, e);
-  e += rl + sl;
-  rh = s + e;
-  rl = e - (rh - s);
+  two_sum(rh, rl, s, e);
+  rh = s;
+  rl = e;
+}
+// Any exponent (scaling by ldexpf): (rh, rl) += 2^ex sum_{d < nd} w[d] 2^(-7 (d0 + d)).
+__device__ __noinline__ float2 fold_any(float rh, float rl, float w0, float w1, float w2, float w3, int nd, int d0,
+                                        int ex) {
+  const float w[4] = {w0, w1, w2, w3};
+  for (int d = 0; d < nd; ++d) {
+    float s, e;
+    two_sum(rh, ldexpf(w[d], ex - 7 * (d0 + d)), s, e);
+    rh = s;
+    rl += e;
+  }
+  float s, e;
+  two_sum(rh, rl, s, e);
+  return make_float2(s, e);
+}
+
+// (hi, lo) with hi + lo = v to 2^-48 relative: hi the significand rounded
+// to 24 bits, lo the exact remainder rounded to FP32 -- from the bit
+// pattern, without FP64 arithmetic (normal magnitudes 2^-70 .. 2^100;
+// others through FP64 conversions).
+__device__ __forceinline__ float2 split_bits(double v) {
+  const long long b = __double_as_longlong(v);
+  const long long mag = b & 0x7fffffffffffffffLL;
+  const int ex = (int)(mag >> 52) - 1023;
+  if (mag == 0) return make_float2(0.f, 0.f);
+  if (ex < -70 || ex > 100) {
+    const float h = __double2float_rn(v);
+    return make_float2(h, __double2float_rn(v - (double)h));
+  }
+  const long long hb = (mag + (1LL << 28)) & ~((1LL << 29) - 1);  // 24-bit significand, rounded
+  const int eh = (int)(hb >> 52) - 1023;
+  float hi = __uint_as_float(((unsigned)(eh + 127) << 23) | (unsigned)((hb >> 29) & 0x7fffff));
+  float lo = (float)(mag - hb) * pow2f(ex - 52);  // |mag - hb| <= 2^28 units of 2^(ex - 52)
+  if (b < 0) {
+    hi = -hi;
+    lo = -lo;
+  }
+  return make_float2(hi, lo);
 }
 
 }  // namespace
@@ -312,23 +364,25 @@ oz_tc_resid_kernel(const __grid_constant__ CUtensorMap mapD, const __grid_consta
     }
   } else {
     // ------------------------------------------------------------ epilogue
-    const int q = warp & 3, half = (warp - 2) >> 2;
+    constexpr int NCH = kEpiCols / 8;  // 8-column chunks per thread
+    const int q = warp & 3, cq = (warp - 2) >> 2;
     const unsigned tl = tmem + ((unsigned)(32 * q) << 16);
     long long gcount = 0;
     bool ok = true;
     for (long long item = blockIdx.x; ok && item < a.items; item += gridDim.x) {
       const long long row0 = (item / a.nct) * kRows, i = row0 + 32 * q + lane;
-      const int jb = (int)(item % a.nct) * kCols + 32 * half;
+      const int jb = (int)(item % a.nct) * kCols + kEpiCols * cq;
       const long long lrow0 = row0 - row0 % a.m;
-      float rh[32], rl[32];
+      float rh[kEpiCols], rl[kEpiCols];
 #pragma unroll
-      for (int c = 0; c < 32; ++c) rh[c] = rl[c] = 0.f;
+      for (int c = 0; c < kEpiCols; ++c) rh[c] = rl[c] = 0.f;
       for (int g = 0; ok && g < groups; ++g) {
         if (!has_group(a, g, leaf_groups, row0)) continue;
         const unsigned par = (unsigned)(gcount & 1);
         ++gcount;
+        // the group's exponents, loaded before the wait for its products
         int erow;
-        const int *ecol;  // column exponents of the group, + j
+        const int *ecol;
         if (g < leaf_groups) {
           erow = a.Dexp[i];
           ecol = a.Xexp + ((lrow0 + g * 64) / kOzChunk) * a.k;
@@ -338,6 +392,13 @@ oz_tc_resid_kernel(const __grid_constant__ CUtensorMap mapD, const __grid_consta
           erow = a.Uexp[(long long)l * a.n + i];
           ecol = a.Texp + a.lteo[l] + b * a.k;
         }
+        // column exponents are the same for every row: lane c holds column
+        // jb + c's, handed out by shuffles
+        const int jl = jb + (lane & (kEpiCols - 1));
+        const int ec = jl < a.k ? __ldg(ecol + jl) : 0;
+        const int er = erow - 14;
+        const bool fast = er + __reduce_max_sync(0xffffffffu, ec) <= 127 &&
+                          er + __reduce_min_sync(0xffffffffu, ec) - 42 >= -126;
         for (int reg = 0; reg < 2; ++reg) {
           if (!wait_or_abort(&sh->acc_full[reg], par, sh)) {
             ok = false;
@@ -345,28 +406,45 @@ oz_tc_resid_kernel(const __grid_constant__ CUtensorMap mapD, const __grid_consta
           }
           tc_fence_after();
 #pragma unroll
-          for (int cc = 0; cc < 4; ++cc) {
-            const int c0 = 32 * half + 8 * cc;
-            int ex[8];
-#pragma unroll
-            for (int c = 0; c < 8; ++c) {
-              const int j = jb + 8 * cc + c;
-              ex[c] = j < a.k ? erow + ecol[j] - 14 : 0;
-            }
+          for (int cc = 0; cc < NCH; ++cc) {
+            const unsigned c0 = (unsigned)(kEpiCols * cq + 8 * cc);
             if (reg == 0) {
               unsigned v[4][8];
 #pragma unroll
-              for (int d = 0; d < 4; ++d) tc_ld8(tl + (unsigned)(d * kCols + c0), v[d]);
+              for (int d = 0; d < 4; ++d) tc_ld8(tl + (unsigned)(d * kCols) + c0, v[d]);
               tc_wait_ld(v);
+              if (fast) {
 #pragma unroll
-              for (int c = 0; c < 8; ++c) fold<4>(rh[8 * cc + c], rl[8 * cc + c], v, c, 0, ex[c]);
+                for (int c = 0; c < 8; ++c) fold_hi(rh[8 * cc + c], rl[8 * cc + c], v, c, er + __shfl_sync(0xffffffffu, ec, 8 * cc + c));
+              } else {
+#pragma unroll
+                for (int c = 0; c < 8; ++c) {
+                  const float2 t = fold_any(rh[8 * cc + c], rl[8 * cc + c], __uint_as_float(v[0][c]),
+                                            __uint_as_float(v[1][c]), __uint_as_float(v[2][c]),
+                                            __uint_as_float(v[3][c]), 4, 0,
+                                            er + __shfl_sync(0xffffffffu, ec, 8 * cc + c));
+                  rh[8 * cc + c] = t.x;
+                  rl[8 * cc + c] = t.y;
+                }
+              }
             } else {
               unsigned v[3][8];
 #pragma unroll
-              for (int d = 0; d < 3; ++d) tc_ld8(tl + (unsigned)((4 + d) * kCols + c0), v[d]);
+              for (int d = 0; d < 3; ++d) tc_ld8(tl + (unsigned)((4 + d) * kCols) + c0, v[d]);
               tc_wait_ld(v);
+              if (fast) {
 #pragma unroll
-              for (int c = 0; c < 8; ++c) fold<3>(rh[8 * cc + c], rl[8 * cc + c], v, c, 4, ex[c]);
+                for (int c = 0; c < 8; ++c) fold_lo(rh[8 * cc + c], rl[8 * cc + c], v, c, er + __shfl_sync(0xffffffffu, ec, 8 * cc + c));
+              } else {
+#pragma unroll
+                for (int c = 0; c < 8; ++c) {
+                  const float2 t = fold_any(rh[8 * cc + c], rl[8 * cc + c], __uint_as_float(v[0][c]),
+                                            __uint_as_float(v[1][c]), __uint_as_float(v[2][c]), 0.f, 3, 4,
+                                            er + __shfl_sync(0xffffffffu, ec, 8 * cc + c));
+                  rh[8 * cc + c] = t.x;
+                  rl[8 * cc + c] = t.y;
+                }
+              }
             }
           }
           tc_fence_before();
@@ -376,14 +454,13 @@ oz_tc_resid_kernel(const __grid_constant__ CUtensorMap mapD, const __grid_consta
       }
       if (!ok) break;
 #pragma unroll
-      for (int c = 0; c < 32; ++c) {
+      for (int c = 0; c < kEpiCols; ++c) {
         const int j = jb + c;
         if (j >= a.k) continue;
-        const double bv = a.B[i + (long long)j * a.ldb];
-        const float bh = __double2float_rn(bv), bl = __double2float_rn(bv - (double)bh);
+        const float2 bv = split_bits(a.B[i + (long long)j * a.ldb]);
         float s, e;
-        two_sum(bh, -rh[c], s, e);
-        e += bl - rl[c];
+        two_sum(bv.x, -rh[c], s, e);
+        e += bv.y - rl[c];
         const float h = s + e;
         a.R2[i + (long long)j * a.ldr] = make_float2(h, e - (h - s));
       }
