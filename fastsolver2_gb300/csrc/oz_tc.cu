@@ -96,15 +96,20 @@ __device__ __forceinline__ void tc_ld8(unsigned taddr, unsigned (&v)[8]) {
                : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7])
                : "r"(taddr));
 }
+__device__ __forceinline__ void tc_ld4(unsigned taddr, unsigned (&v)[4]) {
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x4.b32 {%0,%1,%2,%3}, [%4];"
+               : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3])
+               : "r"(taddr));
+}
 // Waits for this thread's tensor-memory loads; the registers pass through
 // so that no use of them is scheduled before the wait.
-template <int N>
-__device__ __forceinline__ void tc_wait_ld(unsigned (&v)[N][8]) {
+template <int N, int W>
+__device__ __forceinline__ void tc_wait_ld(unsigned (&v)[N][W]) {
   asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
   for (int a = 0; a < N; ++a)
 #pragma unroll
-    for (int b = 0; b < 8; ++b) asm volatile("" : "+r"(v[a][b]));
+    for (int b = 0; b < W; ++b) asm volatile("" : "+r"(v[a][b]));
 }
 
 __device__ __forceinline__ void arrive(uint64_t *bar) {
@@ -141,7 +146,8 @@ __device__ __forceinline__ float pow2f(int e) { return __int_as_float((e + 127) 
 // of the largest possible leading term); rl is renormalised once per group.
 // The scale factors are built from exponent bits: the caller checks that
 // ex - 42 .. ex is a normal range (else fold_any).
-__device__ __forceinline__ void fold_hi(float &rh, float &rl, const unsigned (&v)[4][8], int c, int ex) {
+template <int W>
+__device__ __forceinline__ void fold_hi(float &rh, float &rl, const unsigned (&v)[4][W], int c, int ex) {
   float p = pow2f(ex);
 #pragma unroll
   for (int d = 0; d < 4; ++d) {
@@ -152,7 +158,8 @@ __device__ __forceinline__ void fold_hi(float &rh, float &rl, const unsigned (&v
     p *= 0.0078125f;  // 2^-7
   }
 }
-__device__ __forceinline__ void fold_lo(float &rh, float &rl, const unsigned (&v)[3][8], int c, int ex) {
+template <int W>
+__device__ __forceinline__ void fold_lo(float &rh, float &rl, const unsigned (&v)[3][W], int c, int ex) {
   float p = pow2f(ex - 28);
 #pragma unroll
   for (int d = 0; d < 3; ++d) {
@@ -164,19 +171,81 @@ __device__ __forceinline__ void fold_lo(float &rh, float &rl, const unsigned (&v
   rh = s;
   rl = e;
 }
-// Any exponent (scaling by ldexpf): (rh, rl) += 2^ex sum_{d < nd} w[d] 2^(-7 (d0 + d)).
-__device__ __noinline__ float2 fold_any(float rh, float rl, float w0, float w1, float w2, float w3, int nd, int d0,
-                                        int ex) {
-  const float w[4] = {w0, w1, w2, w3};
-  for (int d = 0; d < nd; ++d) {
-    float s, e;
-    two_sum(rh, ldexpf(w[d], ex - 7 * (d0 + d)), s, e);
-    rh = s;
-    rl += e;
+// One accumulator region of this thread's row and 16 columns: diagonals
+// D0 .. D0 + ND - 1 at tensor-memory columns tl0 + d * kCols + c, read in
+// 4-column chunks with the next chunk's load in flight while the current
+// one is folded into (rh, rl).  Warp-uniform `fast`: every scale factor of
+// the warp's rows and columns is a normal float.
+struct Acc16 {
+  float h[16], l[16];
+};
+// Exponents outside that range: ldexpf scaling (rare; not inlined).
+template <int ND, int D0>
+__device__ __noinline__ Acc16 drain_any(unsigned tl0, Acc16 acc, int er, int ec) {
+  for (int cc = 0; cc < 16; cc += 4) {
+    unsigned v[1][ND][4];
+#pragma unroll
+    for (int d = 0; d < ND; ++d) tc_ld4(tl0 + (unsigned)(d * kCols + cc), v[0][d]);
+    tc_wait_ld(v[0]);
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+      const int ex = er + __shfl_sync(0xffffffffu, ec, cc + c);
+      float rh = acc.h[cc + c], rl = acc.l[cc + c];
+#pragma unroll
+      for (int d = 0; d < ND; ++d) {
+        float s, e;
+        two_sum(rh, ldexpf(__uint_as_float(v[0][d][c]), ex - 7 * (D0 + d)), s, e);
+        rh = s;
+        rl += e;
+      }
+      float s, e;
+      two_sum(rh, rl, s, e);
+      acc.h[cc + c] = s;
+      acc.l[cc + c] = e;
+    }
   }
-  float s, e;
-  two_sum(rh, rl, s, e);
-  return make_float2(s, e);
+  return acc;
+}
+
+template <int ND, int D0>
+__device__ __forceinline__ void drain_region(unsigned tl0, float (&rh)[16], float (&rl)[16], int er, int ec,
+                                             bool fast) {
+  if (!fast) {
+    Acc16 acc;
+#pragma unroll
+    for (int c = 0; c < 16; ++c) {
+      acc.h[c] = rh[c];
+      acc.l[c] = rl[c];
+    }
+    acc = drain_any<ND, D0>(tl0, acc, er, ec);
+#pragma unroll
+    for (int c = 0; c < 16; ++c) {
+      rh[c] = acc.h[c];
+      rl[c] = acc.l[c];
+    }
+    return;
+  }
+  unsigned v[2][ND][4];
+#pragma unroll
+  for (int d = 0; d < ND; ++d) tc_ld4(tl0 + (unsigned)(d * kCols), v[0][d]);
+  tc_wait_ld(v[0]);
+#pragma unroll
+  for (int ch = 0; ch < 4; ++ch) {
+    const int cur = ch & 1;
+    if (ch + 1 < 4) {
+#pragma unroll
+      for (int d = 0; d < ND; ++d) tc_ld4(tl0 + (unsigned)(d * kCols + 4 * (ch + 1)), v[cur ^ 1][d]);
+    }
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+      const int cc = 4 * ch + c, ex = er + __shfl_sync(0xffffffffu, ec, cc);
+      if constexpr (D0 == 0)
+        fold_hi(rh[cc], rl[cc], v[cur], c, ex);
+      else
+        fold_lo(rh[cc], rl[cc], v[cur], c, ex);
+    }
+    if (ch + 1 < 4) tc_wait_ld(v[cur ^ 1]);
+  }
 }
 
 // (hi, lo) with hi + lo = v to 2^-48 relative: hi the significand rounded
@@ -323,9 +392,20 @@ oz_tc_resid_kernel(const __grid_constant__ CUtensorMap mapD, const __grid_consta
           const unsigned par_empty = (unsigned)((gcount & 1) ^ 1);
           ++gcount;
           for (int kh = 0; ok && kh < nkh; ++kh) {
-            for (int d = 0; ok && d < kOzSlices; ++d) {
-              const long long sd = it + d;
-              if (!wait_or_abort(&sh->full[sd % kStages], (unsigned)((sd / kStages) & 1), sh)) {
+            // the K-half's seven stages: descriptors of their A and B slabs
+            const unsigned slot0 = (unsigned)(it & (kStages - 1)), ph0 = (unsigned)((it / kStages) & 1);
+            uint64_t ad[kOzSlices], bd[kOzSlices];
+#pragma unroll
+            for (int t = 0; t < kOzSlices; ++t) {
+              const unsigned sa = smem_u32(stages + ((slot0 + t) & (kStages - 1)) * kStageBytes);
+              ad[t] = desc_sw64(sa);
+              bd[t] = desc_sw64(sa + kABytes);
+            }
+            const unsigned first = kh == 0 ? 0u : 1u;  // the K-half that starts each diagonal's sum
+#pragma unroll
+            for (int d = 0; d < kOzSlices; ++d) {
+              const unsigned slot = (slot0 + d) & (kStages - 1);
+              if (!wait_or_abort(&sh->full[slot], ph0 ^ (slot < slot0 ? 1u : 0u), sh)) {
                 ok = false;
                 break;
               }
@@ -337,18 +417,17 @@ oz_tc_resid_kernel(const __grid_constant__ CUtensorMap mapD, const __grid_consta
               }
               tc_fence_after();
               const unsigned dt = tmem + (unsigned)(d * kCols);
-              for (int s = 0; s <= d; ++s) {
-                const unsigned sa = smem_u32(stages + ((it + s) % kStages) * kStageBytes);
-                const unsigned sb = smem_u32(stages + ((it + d - s) % kStages) * kStageBytes + kABytes);
 #pragma unroll
-                for (int kk = 0; kk < kSlab / 16; ++kk)
-                  tc_mma(dt, desc_sw64(sa + kk * 32), desc_sw64(sb + kk * 32), (kh > 0 || s > 0 || kk > 0) ? 1u : 0u);
-              }
+              for (int s = 0; s <= d; ++s)
+#pragma unroll
+                for (int kk = 0; kk < kSlab / 16; ++kk)  // +32 bytes = +2 in the descriptor's address field
+                  tc_mma(dt, ad[s] + 2 * kk, bd[d - s] + 2 * kk, (s > 0 || kk > 0) ? 1u : first);
               if (kh == nkh - 1 && d == 3) tc_commit(&sh->acc_full[0]);
               if (kh == nkh - 1 && d == kOzSlices - 1) tc_commit(&sh->acc_full[1]);
             }
             if (!ok) break;
-            for (int s = 0; s < kOzSlices; ++s) tc_commit(&sh->empty[(it + s) % kStages]);
+#pragma unroll
+            for (int t = 0; t < kOzSlices; ++t) tc_commit(&sh->empty[(slot0 + t) & (kStages - 1)]);
             it += kOzSlices;
           }
         }
@@ -364,93 +443,66 @@ oz_tc_resid_kernel(const __grid_constant__ CUtensorMap mapD, const __grid_consta
     }
   } else {
     // ------------------------------------------------------------ epilogue
-    constexpr int NCH = kEpiCols / 8;  // 8-column chunks per thread
     const int q = warp & 3, cq = (warp - 2) >> 2;
-    const unsigned tl = tmem + ((unsigned)(32 * q) << 16);
+    const unsigned tl = tmem + ((unsigned)(32 * q) << 16) + (unsigned)(kEpiCols * cq);
     long long gcount = 0;
     bool ok = true;
     for (long long item = blockIdx.x; ok && item < a.items; item += gridDim.x) {
       const long long row0 = (item / a.nct) * kRows, i = row0 + 32 * q + lane;
       const int jb = (int)(item % a.nct) * kCols + kEpiCols * cq;
+      const int jl = jb + (lane & (kEpiCols - 1));  // lane c holds column jb + c's exponent
       const long long lrow0 = row0 - row0 % a.m;
-      float rh[kEpiCols], rl[kEpiCols];
-#pragma unroll
-      for (int c = 0; c < kEpiCols; ++c) rh[c] = rl[c] = 0.f;
-      for (int g = 0; ok && g < groups; ++g) {
-        if (!has_group(a, g, leaf_groups, row0)) continue;
-        const unsigned par = (unsigned)(gcount & 1);
-        ++gcount;
-        // the group's exponents, loaded before the wait for its products
-        int erow;
+      // the row exponent of this thread's row and the column exponent of
+      // column jl in group g (loaded one group ahead of their use)
+      auto exps = [&](int g, int &erow, int &ec) {
         const int *ecol;
         if (g < leaf_groups) {
           erow = a.Dexp[i];
           ecol = a.Xexp + ((lrow0 + g * 64) / kOzChunk) * a.k;
         } else {
           const int l = g - leaf_groups;
-          const long long b = row0 / a.lrows[l];
           erow = a.Uexp[(long long)l * a.n + i];
-          ecol = a.Texp + a.lteo[l] + b * a.k;
+          ecol = a.Texp + a.lteo[l] + (row0 / a.lrows[l]) * a.k;
         }
-        // column exponents are the same for every row: lane c holds column
-        // jb + c's, handed out by shuffles
-        const int jl = jb + (lane & (kEpiCols - 1));
-        const int ec = jl < a.k ? __ldg(ecol + jl) : 0;
-        const int er = erow - 14;
-        const bool fast = er + __reduce_max_sync(0xffffffffu, ec) <= 127 &&
-                          er + __reduce_min_sync(0xffffffffu, ec) - 42 >= -126;
-        for (int reg = 0; reg < 2; ++reg) {
-          if (!wait_or_abort(&sh->acc_full[reg], par, sh)) {
-            ok = false;
-            break;
-          }
-          tc_fence_after();
+        ec = jl < a.k ? __ldg(ecol + jl) : 0;
+      };
+      auto next_group = [&](int g) {
+        do ++g;
+        while (g < groups && !has_group(a, g, leaf_groups, row0));
+        return g;
+      };
+      float rh[kEpiCols], rl[kEpiCols];
 #pragma unroll
-          for (int cc = 0; cc < NCH; ++cc) {
-            const unsigned c0 = (unsigned)(kEpiCols * cq + 8 * cc);
-            if (reg == 0) {
-              unsigned v[4][8];
-#pragma unroll
-              for (int d = 0; d < 4; ++d) tc_ld8(tl + (unsigned)(d * kCols) + c0, v[d]);
-              tc_wait_ld(v);
-              if (fast) {
-#pragma unroll
-                for (int c = 0; c < 8; ++c) fold_hi(rh[8 * cc + c], rl[8 * cc + c], v, c, er + __shfl_sync(0xffffffffu, ec, 8 * cc + c));
-              } else {
-#pragma unroll
-                for (int c = 0; c < 8; ++c) {
-                  const float2 t = fold_any(rh[8 * cc + c], rl[8 * cc + c], __uint_as_float(v[0][c]),
-                                            __uint_as_float(v[1][c]), __uint_as_float(v[2][c]),
-                                            __uint_as_float(v[3][c]), 4, 0,
-                                            er + __shfl_sync(0xffffffffu, ec, 8 * cc + c));
-                  rh[8 * cc + c] = t.x;
-                  rl[8 * cc + c] = t.y;
-                }
-              }
-            } else {
-              unsigned v[3][8];
-#pragma unroll
-              for (int d = 0; d < 3; ++d) tc_ld8(tl + (unsigned)((4 + d) * kCols) + c0, v[d]);
-              tc_wait_ld(v);
-              if (fast) {
-#pragma unroll
-                for (int c = 0; c < 8; ++c) fold_lo(rh[8 * cc + c], rl[8 * cc + c], v, c, er + __shfl_sync(0xffffffffu, ec, 8 * cc + c));
-              } else {
-#pragma unroll
-                for (int c = 0; c < 8; ++c) {
-                  const float2 t = fold_any(rh[8 * cc + c], rl[8 * cc + c], __uint_as_float(v[0][c]),
-                                            __uint_as_float(v[1][c]), __uint_as_float(v[2][c]), 0.f, 3, 4,
-                                            er + __shfl_sync(0xffffffffu, ec, 8 * cc + c));
-                  rh[8 * cc + c] = t.x;
-                  rl[8 * cc + c] = t.y;
-                }
-              }
-            }
-          }
-          tc_fence_before();
-          __syncwarp();
-          if (lane == 0) arrive(&sh->acc_empty[reg]);
+      for (int c = 0; c < kEpiCols; ++c) rh[c] = rl[c] = 0.f;
+      int erow_n, ec_n;
+      exps(0, erow_n, ec_n);
+      for (int g = 0; ok && g < groups; g = next_group(g)) {
+        const unsigned par = (unsigned)(gcount & 1);
+        ++gcount;
+        const int er = erow_n - 14, ec = ec_n;
+        const int gn = next_group(g);
+        if (gn < groups) exps(gn, erow_n, ec_n);
+        const bool fast = __all_sync(0xffffffffu, er + __reduce_max_sync(0xffffffffu, ec) <= 127 &&
+                                                      er + __reduce_min_sync(0xffffffffu, ec) - 42 >= -126);
+        // region 0: diagonals 0-3; region 1: diagonals 4-6
+        if (!wait_or_abort(&sh->acc_full[0], par, sh)) {
+          ok = false;
+          break;
         }
+        tc_fence_after();
+        drain_region<4, 0>(tl, rh, rl, er, ec, fast);
+        tc_fence_before();
+        __syncwarp();
+        if (lane == 0) arrive(&sh->acc_empty[0]);
+        if (!wait_or_abort(&sh->acc_full[1], par, sh)) {
+          ok = false;
+          break;
+        }
+        tc_fence_after();
+        drain_region<3, 4>(tl + (unsigned)(4 * kCols), rh, rl, er, ec, fast);
+        tc_fence_before();
+        __syncwarp();
+        if (lane == 0) arrive(&sh->acc_empty[1]);
       }
       if (!ok) break;
 #pragma unroll

@@ -349,3 +349,21 @@ def test_tcgen05_residual_matches_mma_sync_residual(hodlr, m, L, r, k, monkeypat
     assert abs(r1 - r0) <= 0.05 * r0 + 1e-15, (r0, r1)
     assert rel(X1, X0) < 1e-11
     assert P.rel_residual(pr, X1) < 2e-12
+
+
+def test_tcgen05_residual_extreme_exponents(hodlr, monkeypatch):
+    """Right-hand sides near the bottom of the FP32 range (B scaled by
+    2^-80): the digit groups' scale factors leave the normal float range,
+    which the tcgen05 epilogue handles on its ldexpf path; the scaled solve
+    must match the unscaled one."""
+    monkeypatch.setenv("HODLR_NO_TCGEN05", "0")
+    pr = P.gaussian_problem(128, 3, 32, nrhs=4, seed=41, orthonormal=True, decay=3.0, shift=1.5)
+    sc = 2.0 ** -80
+    s = make_solver(hodlr, pr, precision=hodlr.PREC_MIXED, residual=2, refine_tol=1e-12)
+    s.factor()
+    B1, Bs = to_dev(pr.B), to_dev(pr.B * sc)
+    i1, i2 = s.solve(B1), s.solve(Bs)
+    X1, X2 = to_host(B1), to_host(Bs) / sc
+    assert i2.status == hodlr.HODLR_OK and i2.rel_residual <= 1e-12
+    assert rel(X2, X1) < 1e-11
+    assert P.rel_residual(pr, X2) < 2e-12
