@@ -135,6 +135,7 @@ struct hodlr_ctx {
   // the leaf and update products in one tcgen05 pass (oz_tc.cu); Tsl / Texp
   // then hold every level's T' digits one level after another
   bool oz_tc = false;
+  double *Tall = nullptr, *Tpart = nullptr;  // every level's V^T X blocks, and their range partials
   __nv_bfloat16 *Dsl = nullptr, *Usl = nullptr, *Vsl = nullptr, *Xsl = nullptr, *Tsl = nullptr;
   int *Dexp = nullptr, *Uexp = nullptr, *Vexp = nullptr, *Xexp = nullptr, *Texp = nullptr;
   size_t tbuf_elems = 0, eta_elems = 0, red_elems = 0;
@@ -678,17 +679,18 @@ static int residual_tensor(hodlr_ctx *h, double *X, long long ldx, const double 
   if (h->oz_tc) {
     // every level's reduction and T' digits first, then the leaf and all
     // update products in one pass
-    long long toff = 0, eoff = 0;
+    PHASE(h, HODLR_PHASE_RESID_REDUCE,
+          launch_oz_tc_reduce(h->Vsl, h->Vexp, h->Xsl, h->Xexp, n, L, r, k, h->lev_nb.data(), h->lev_rows.data(),
+                              h->Tall, h->Tpart, skip, h->dst, s));
+    long long toff = 0, eoff = 0, tboff = 0;
     for (int l = 0; l < L; ++l) {
       const int nb = h->nb(l);
-      PHASE(h, HODLR_PHASE_RESID_REDUCE,
-            launch_oz_reduce(h->Vsl + (long long)l * r * n, (long long)L * r * n,
-                             h->Vexp + (long long)l * (n / kOzChunk) * r, r, h->Xsl, h->Xexp, n, k, h->rows(l), nb,
-                             h->Tbuf, h->red, skip, s));
       PHASE(h, HODLR_PHASE_MISC,
-            launch_oz_slice_tprime(h->Tbuf, h->slev(l), r, k, nb, h->Tsl + toff * r, h->Texp + eoff, skip, s));
+            launch_oz_slice_tprime(h->Tall + tboff, h->slev(l), r, k, nb, h->Tsl + toff * r, h->Texp + eoff, skip,
+                                   s));
       toff += (long long)nb * kOzSlices * k;
       eoff += (long long)nb * k;
+      tboff += (long long)nb * r * k;
     }
     PHASE(h, HODLR_PHASE_RESID_UPDATE,
           launch_oz_tc_resid(h->Dsl, h->Dexp, h->Xsl, h->Xexp, h->Usl, h->Uexp, h->Tsl, h->Texp, n, m, L, r, k,
@@ -941,6 +943,11 @@ static int create_ctx(const hodlr_desc &d, const std::vector<int> &sys_levels, h
       const size_t nbt = h->oz_tc ? nball : (size_t)nbmax;
       ALLOC(h->Tsl, __nv_bfloat16, S * nbt * k * r);
       ALLOC(h->Texp, int, nbt * k);
+      if (h->oz_tc) {
+        ALLOC(h->Tall, double, nball * k * r);
+        const size_t np = oz_tc_reduce_partials(n, L, r, k, h->lev_nb.data(), h->lev_rows.data());
+        if (np) ALLOC(h->Tpart, double, np);
+      }
     }
     if (d.residual == HODLR_RESID_FP64_EMULATED || d.residual == HODLR_RESID_FP64_TENSOR) {
       h->emulated = true;  // also the transposed solves of the tensor-core mode

@@ -276,43 +276,101 @@ __device__ __forceinline__ float2 split_bits(double v) {
 
 constexpr int kMaxLevels = 32;
 
+// Two products share the pipeline below.  Mode 0, the residual: a work item
+// is a 128-row tile x 64 columns; its groups are the leaf term's 64-row
+// chunks (A = D digits, B = X digits) and every level with a block over the
+// tile (A = U_l digits, B = T'_l digits); R2 is written once per item.
+// Mode 1, the reductions T_l = V_l^T X of every level: a work item is a
+// range of R rows x a stack of QL = 128 / r levels x 64 columns; A = the
+// stacked levels' V digits (row (l, q) = line l r + q of the V digit
+// matrix), B = X digits, one group per 64-row chunk of the range.  A level
+// block that ends inside the range is written to T when it ends; a block
+// longer than the range gets one partial per range, summed by
+// oz_tc_pass2_kernel in a fixed order.
 struct OzTcArgs {
-  // level l: blocks of lrows[l] rows from row 0 (lnb[l] of them); block b's
-  // T' digits start at line ltrow[l] + 7 k b, its column exponents at
-  // Texp + lteo[l] + k b
-  long long lrows[kMaxLevels], ltrow[kMaxLevels], lteo[kMaxLevels];
+  // level l: blocks of lrows[l] rows from row 0 (lnb[l] of them)
+  long long lrows[kMaxLevels];
   int lnb[kMaxLevels];
-  const int *Dexp, *Xexp, *Uexp, *Texp;
+  // mode 0: block b's T' digits start at line ltrow[l] + 7 k b, its column
+  // exponents at Texp + lteo[l] + k b
+  long long ltrow[kMaxLevels], lteo[kMaxLevels];
+  // mode 1: level l's T blocks at T + toff[l] (r x k each, ld r), its
+  // partials at P + poff[l] ((b parts[l] + part) r k)
+  long long toff[kMaxLevels], poff[kMaxLevels];
+  int parts[kMaxLevels];
+  const int *Dexp, *Xexp, *Uexp, *Texp, *Vexp;
   const double *B;
   long long ldb;
   float2 *R2;
   long long ldr;
-  long long n;
-  int m, L, r, k;
-  long long items;  // row tiles x column tiles
-  int nct;          // column tiles
+  double *T, *P;
+  long long n, R;
+  int m, L, r, k, QL, nstack;
+  long long items;
+  int nct;  // column tiles
   const int *skip;
   DevStatus *st;
 };
 
-// Group g of the tile at row0: the leaf chunks always, level l when a block of it covers the tile.
+// Group g of the mode-0 tile at row0: the leaf chunks always, level l when a block of it covers the tile.
 __device__ __forceinline__ bool has_group(const OzTcArgs &a, int g, int leaf_groups, long long row0) {
   if (g < leaf_groups) return true;
   const int l = g - leaf_groups;
   return row0 < (long long)a.lnb[l] * a.lrows[l];
 }
 
+struct ItemGeo {
+  long long row0;  // mode 0: the tile's first row; mode 1: the range's
+  int j0, stack, g0, g1;
+};
+
+template <int MODE>
+__device__ __forceinline__ ItemGeo item_geo(const OzTcArgs &a, long long item) {
+  ItemGeo it;
+  it.j0 = (int)(item % a.nct) * kCols;
+  const long long t = item / a.nct;
+  if (MODE == 0) {
+    it.row0 = t * kRows;
+    it.stack = 0;
+    it.g0 = 0;
+    it.g1 = a.m / 64 + a.L;
+  } else {
+    it.stack = (int)(t % a.nstack);
+    it.row0 = (t / a.nstack) * a.R;
+    it.g0 = (int)(it.row0 / 64);
+    it.g1 = (int)(std::min<long long>(it.row0 + a.R, a.n) / 64);
+  }
+  return it;
+}
+
+template <int MODE>
+__device__ __forceinline__ bool group_exists(const OzTcArgs &a, const ItemGeo &it, int g) {
+  return MODE == 1 || has_group(a, g, a.m / 64, it.row0);
+}
+template <int MODE>
+__device__ __forceinline__ int group_khalves(const OzTcArgs &a, int g) {
+  return (MODE == 1 || g < a.m / 64) ? 2 : (a.r + kSlab - 1) / kSlab;
+}
+
+// Writes 16 columns of this thread's row, as FP64, at out + j * ld (j < k).
+__device__ __forceinline__ void store_fp64(double *out, long long ld, const float (&rh)[kEpiCols],
+                                           const float (&rl)[kEpiCols], int jb, int k) {
+#pragma unroll
+  for (int c = 0; c < kEpiCols; ++c)
+    if (jb + c < k) out[(long long)(jb + c) * ld] = (double)rh[c] + (double)rl[c];
+}
+
+template <int MODE>
 __global__ void __launch_bounds__(kThreads, 1)
-oz_tc_resid_kernel(const __grid_constant__ CUtensorMap mapD, const __grid_constant__ CUtensorMap mapX,
-                   const __grid_constant__ CUtensorMap mapU, const __grid_constant__ CUtensorMap mapT, OzTcArgs a) {
+oz_tc_kernel(const __grid_constant__ CUtensorMap mapA0, const __grid_constant__ CUtensorMap mapB0,
+             const __grid_constant__ CUtensorMap mapA1, const __grid_constant__ CUtensorMap mapB1, OzTcArgs a) {
   if (a.skip && *a.skip) return;
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   unsigned char *stages =
       reinterpret_cast<unsigned char *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
   Shared *sh = reinterpret_cast<Shared *>(stages + kStages * kStageBytes);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int leaf_groups = a.m / 64, khl = (a.r + kSlab - 1) / kSlab;
-  const int groups = leaf_groups + a.L;
+  const int leaf_groups = a.m / 64;
 
   if (threadIdx.x == 0) {
     for (int i = 0; i < kStages; ++i) {
@@ -341,20 +399,52 @@ oz_tc_resid_kernel(const __grid_constant__ CUtensorMap mapD, const __grid_consta
   if (warp == 0) {
     // ------------------------------------------------------------ producer
     if (lane == 0) {
-      prefetch_tensormap(&mapD);
-      prefetch_tensormap(&mapX);
-      prefetch_tensormap(&mapU);
-      prefetch_tensormap(&mapT);
+      prefetch_tensormap(&mapA0);
+      prefetch_tensormap(&mapB0);
+      if (MODE == 0) {
+        prefetch_tensormap(&mapA1);
+        prefetch_tensormap(&mapB1);
+      }
       bool ok = true;
       for (long long item = blockIdx.x; ok && item < a.items; item += gridDim.x) {
-        const long long row0 = (item / a.nct) * kRows;
-        const int j0 = (int)(item % a.nct) * kCols;
-        const long long lrow0 = row0 - row0 % a.m;
-        for (int g = 0; ok && g < groups; ++g) {
-          if (!has_group(a, g, leaf_groups, row0)) continue;
-          const int nkh = g < leaf_groups ? 2 : khl;
+        const ItemGeo it = item_geo<MODE>(a, item);
+        const long long lrow0 = it.row0 - it.row0 % a.m;
+        for (int g = it.g0; ok && g < it.g1; ++g) {
+          if (!group_exists<MODE>(a, it, g)) continue;
+          const int nkh = group_khalves<MODE>(a, g);
+          // slab coordinates of slice 0, K-half 0, and the per-slice line strides
+          const CUtensorMap *ma, *mb;
+          int ax, bx;
+          long long ay, by, as, bs;
+          if (MODE == 1) {
+            ma = &mapA0;
+            mb = &mapB0;
+            ax = bx = g * 64;
+            ay = (long long)it.stack * a.QL * a.r;
+            as = (long long)a.L * a.r;
+            by = it.j0;
+            bs = a.k;
+          } else if (g < leaf_groups) {
+            ma = &mapA0;
+            mb = &mapB0;
+            ax = g * 64;
+            ay = it.row0;
+            as = a.n;
+            bx = (int)(lrow0 + g * 64);
+            by = it.j0;
+            bs = a.k;
+          } else {
+            const int l = g - leaf_groups;
+            ma = &mapA1;
+            mb = &mapB1;
+            ax = bx = 0;
+            ay = (long long)l * a.n + it.row0;
+            as = (long long)a.L * a.n;
+            by = a.ltrow[l] + (it.row0 / a.lrows[l]) * kOzSlices * a.k + it.j0;
+            bs = a.k;
+          }
           for (int kh = 0; ok && kh < nkh; ++kh)
-            for (int s = 0; s < kOzSlices; ++s) {
+            for (int sl = 0; sl < kOzSlices; ++sl) {
               const int slot = (int)(issued % kStages);
               if (!wait_or_abort(&sh->empty[slot], (unsigned)(((issued / kStages) & 1) ^ 1), sh)) {
                 ok = false;
@@ -362,18 +452,8 @@ oz_tc_resid_kernel(const __grid_constant__ CUtensorMap mapD, const __grid_consta
               }
               unsigned char *sa = stages + slot * kStageBytes, *sb = sa + kABytes;
               mbar_arrive_expect_tx(&sh->full[slot], kStageBytes);
-              if (g < leaf_groups) {
-                const int q0 = g * 64 + kh * kSlab;  // leaf column (K) offset
-                tma_load_2d(sa, &mapD, &sh->full[slot], q0, (int)((long long)s * a.n + row0));
-                tma_load_2d(sb, &mapX, &sh->full[slot], (int)(lrow0 + q0), s * a.k + j0);
-              } else {
-                const int l = g - leaf_groups;
-                const long long b = row0 / a.lrows[l];
-                const long long trow = a.ltrow[l] + b * kOzSlices * a.k;  // block b's T' digits
-                tma_load_2d(sa, &mapU, &sh->full[slot], kh * kSlab,
-                            (int)(((long long)s * a.L + l) * a.n + row0));
-                tma_load_2d(sb, &mapT, &sh->full[slot], kh * kSlab, (int)(trow + (long long)s * a.k + j0));
-              }
+              tma_load_2d(sa, ma, &sh->full[slot], ax + kh * kSlab, (int)(ay + sl * as));
+              tma_load_2d(sb, mb, &sh->full[slot], bx + kh * kSlab, (int)(by + sl * bs));
               ++issued;
             }
         }
@@ -382,18 +462,18 @@ oz_tc_resid_kernel(const __grid_constant__ CUtensorMap mapD, const __grid_consta
   } else if (warp == 1) {
     // ----------------------------------------------------------- MMA issue
     if (lane == 0) {
-      long long it = 0, gcount = 0;
+      long long it_s = 0, gcount = 0;
       bool ok = true;
-      for (long long item = blockIdx.x; ok && item < a.items; item += gridDim.x)
-        for (int g = 0; ok && g < groups; ++g) {
-          const long long row0 = (item / a.nct) * kRows;
-          if (!has_group(a, g, leaf_groups, row0)) continue;
-          const int nkh = g < leaf_groups ? 2 : khl;
+      for (long long item = blockIdx.x; ok && item < a.items; item += gridDim.x) {
+        const ItemGeo it = item_geo<MODE>(a, item);
+        for (int g = it.g0; ok && g < it.g1; ++g) {
+          if (!group_exists<MODE>(a, it, g)) continue;
+          const int nkh = group_khalves<MODE>(a, g);
           const unsigned par_empty = (unsigned)((gcount & 1) ^ 1);
           ++gcount;
           for (int kh = 0; ok && kh < nkh; ++kh) {
             // the K-half's seven stages: descriptors of their A and B slabs
-            const unsigned slot0 = (unsigned)(it & (kStages - 1)), ph0 = (unsigned)((it / kStages) & 1);
+            const unsigned slot0 = (unsigned)(it_s & (kStages - 1)), ph0 = (unsigned)((it_s / kStages) & 1);
             uint64_t ad[kOzSlices], bd[kOzSlices];
 #pragma unroll
             for (int t = 0; t < kOzSlices; ++t) {
@@ -428,10 +508,11 @@ oz_tc_resid_kernel(const __grid_constant__ CUtensorMap mapD, const __grid_consta
             if (!ok) break;
 #pragma unroll
             for (int t = 0; t < kOzSlices; ++t) tc_commit(&sh->empty[(slot0 + t) & (kStages - 1)]);
-            it += kOzSlices;
+            it_s += kOzSlices;
           }
         }
-      sh->consumed = (int)it;
+      }
+      sh->consumed = (int)it_s;
       tc_commit(&sh->drain);  // completes once every product issued above has
       if (!wait_or_abort(&sh->drain, 0, sh)) {
         // the products were still running after the bounded wait: keep waiting,
@@ -444,44 +525,54 @@ oz_tc_resid_kernel(const __grid_constant__ CUtensorMap mapD, const __grid_consta
   } else {
     // ------------------------------------------------------------ epilogue
     const int q = warp & 3, cq = (warp - 2) >> 2;
+    const int p = 32 * q + lane;  // the thread's row of the product
     const unsigned tl = tmem + ((unsigned)(32 * q) << 16) + (unsigned)(kEpiCols * cq);
+    // mode 1: the row is rank qq of stacked level lq
+    const int lq = MODE == 1 ? p / a.r : 0, qq = MODE == 1 ? p - lq * a.r : 0;
     long long gcount = 0;
     bool ok = true;
     for (long long item = blockIdx.x; ok && item < a.items; item += gridDim.x) {
-      const long long row0 = (item / a.nct) * kRows, i = row0 + 32 * q + lane;
-      const int jb = (int)(item % a.nct) * kCols + kEpiCols * cq;
+      const ItemGeo it = item_geo<MODE>(a, item);
+      const long long i = it.row0 + p;  // mode 0: the thread's matrix row
+      const int jb = it.j0 + kEpiCols * cq;
       const int jl = jb + (lane & (kEpiCols - 1));  // lane c holds column jb + c's exponent
-      const long long lrow0 = row0 - row0 % a.m;
+      const long long lrow0 = it.row0 - it.row0 % a.m;
+      const int l1 = it.stack * a.QL + lq;          // mode 1: the row's level
+      const bool valid = MODE == 0 || (lq < a.QL && l1 < a.L);
+      const long long rows1 = (MODE == 1 && valid) ? a.lrows[l1] : 0;
       // the row exponent of this thread's row and the column exponent of
       // column jl in group g (loaded one group ahead of their use)
       auto exps = [&](int g, int &erow, int &ec) {
         const int *ecol;
-        if (g < leaf_groups) {
+        if (MODE == 1) {
+          erow = valid ? a.Vexp[((long long)l1 * (a.n / kOzChunk) + g) * a.r + qq] : 0;
+          ecol = a.Xexp + (long long)g * a.k;
+        } else if (g < leaf_groups) {
           erow = a.Dexp[i];
           ecol = a.Xexp + ((lrow0 + g * 64) / kOzChunk) * a.k;
         } else {
           const int l = g - leaf_groups;
           erow = a.Uexp[(long long)l * a.n + i];
-          ecol = a.Texp + a.lteo[l] + (row0 / a.lrows[l]) * a.k;
+          ecol = a.Texp + a.lteo[l] + (it.row0 / a.lrows[l]) * a.k;
         }
         ec = jl < a.k ? __ldg(ecol + jl) : 0;
       };
       auto next_group = [&](int g) {
         do ++g;
-        while (g < groups && !has_group(a, g, leaf_groups, row0));
+        while (g < it.g1 && !group_exists<MODE>(a, it, g));
         return g;
       };
       float rh[kEpiCols], rl[kEpiCols];
 #pragma unroll
       for (int c = 0; c < kEpiCols; ++c) rh[c] = rl[c] = 0.f;
       int erow_n, ec_n;
-      exps(0, erow_n, ec_n);
-      for (int g = 0; ok && g < groups; g = next_group(g)) {
+      exps(it.g0, erow_n, ec_n);
+      for (int g = it.g0; ok && g < it.g1; g = next_group(g)) {
         const unsigned par = (unsigned)(gcount & 1);
         ++gcount;
         const int er = erow_n - 14, ec = ec_n;
         const int gn = next_group(g);
-        if (gn < groups) exps(gn, erow_n, ec_n);
+        if (gn < it.g1) exps(gn, erow_n, ec_n);
         const bool fast = __all_sync(0xffffffffu, er + __reduce_max_sync(0xffffffffu, ec) <= 127 &&
                                                       er + __reduce_min_sync(0xffffffffu, ec) - 42 >= -126);
         // region 0: diagonals 0-3; region 1: diagonals 4-6
@@ -503,18 +594,36 @@ oz_tc_resid_kernel(const __grid_constant__ CUtensorMap mapD, const __grid_consta
         tc_fence_before();
         __syncwarp();
         if (lane == 0) arrive(&sh->acc_empty[1]);
+        if (MODE == 1 && valid && rows1 <= a.R) {
+          // a block of this level ends with this chunk: its T is complete
+          const long long end = (long long)(g + 1) * 64;
+          if ((end & (rows1 - 1)) == 0) {
+            const long long b = end / rows1 - 1;
+            if (b < a.lnb[l1]) store_fp64(a.T + a.toff[l1] + b * a.r * a.k + qq, a.r, rh, rl, jb, a.k);
+#pragma unroll
+            for (int c = 0; c < kEpiCols; ++c) rh[c] = rl[c] = 0.f;
+          }
+        }
       }
       if (!ok) break;
+      if (MODE == 1) {
+        if (valid && rows1 > a.R) {  // this range's part of a longer block
+          const long long b = it.row0 / rows1, part = (it.row0 & (rows1 - 1)) / a.R;
+          if (b < a.lnb[l1])
+            store_fp64(a.P + a.poff[l1] + (b * a.parts[l1] + part) * a.r * a.k + qq, a.r, rh, rl, jb, a.k);
+        }
+      } else {
 #pragma unroll
-      for (int c = 0; c < kEpiCols; ++c) {
-        const int j = jb + c;
-        if (j >= a.k) continue;
-        const float2 bv = split_bits(a.B[i + (long long)j * a.ldb]);
-        float s, e;
-        two_sum(bv.x, -rh[c], s, e);
-        e += bv.y - rl[c];
-        const float h = s + e;
-        a.R2[i + (long long)j * a.ldr] = make_float2(h, e - (h - s));
+        for (int c = 0; c < kEpiCols; ++c) {
+          const int j = jb + c;
+          if (j >= a.k) continue;
+          const float2 bv = split_bits(a.B[i + (long long)j * a.ldb]);
+          float s, e;
+          two_sum(bv.x, -rh[c], s, e);
+          e += bv.y - rl[c];
+          const float h = s + e;
+          a.R2[i + (long long)j * a.ldr] = make_float2(h, e - (h - s));
+        }
       }
     }
   }
@@ -534,6 +643,34 @@ oz_tc_resid_kernel(const __grid_constant__ CUtensorMap mapD, const __grid_consta
     tc_fence_after();
     tc_dealloc(tmem, kTmemCols);
   }
+}
+
+// out_b = sum over parts of P_b (r k values per block, parts in order).
+__global__ void oz_tc_pass2_kernel(const double *__restrict__ P, int parts, long long blk, double *out,
+                                   const int *skip) {
+  if (skip && *skip) return;
+  const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= blk) return;
+  const double *p = P + (long long)blockIdx.y * parts * blk + e;
+  double s = 0.0;
+  for (int c = 0; c < parts; ++c) s += p[(long long)c * blk];
+  out[(long long)blockIdx.y * blk + e] = s;
+}
+
+static bool is_pow2(long long v) { return v > 0 && (v & (v - 1)) == 0; }
+
+static cudaError_t launch_mode(int mode, const CUtensorMap &a0, const CUtensorMap &b0, const CUtensorMap &a1,
+                               const CUtensorMap &b1, const OzTcArgs &a, cudaStream_t s) {
+  const size_t bytes = (size_t)kStages * kStageBytes + sizeof(Shared) + 1024;
+  auto kern = mode == 0 ? oz_tc_kernel<0> : oz_tc_kernel<1>;
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  if (e != cudaSuccess) return e;
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const long long grid = std::min<long long>(a.items, sms > 0 ? sms : 148);
+  HODLR_LAUNCH(kern, (unsigned)grid, kThreads, bytes, s, a0, b0, a1, b1, a);
+  return cudaGetLastError();
 }
 
 bool oz_tc_supported(int m, int r, int k) {
@@ -583,14 +720,69 @@ cudaError_t launch_oz_tc_resid(const __nv_bfloat16 *Dsl, const int *Dexp, const 
   a.items = (n / kRows) * a.nct;
   a.skip = skip;
   a.st = st;
-  const size_t bytes = (size_t)kStages * kStageBytes + sizeof(Shared) + 1024;
-  cudaError_t e = cudaFuncSetAttribute(oz_tc_resid_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  return launch_mode(0, mD, mX, mU, mT, a, s);
+}
+
+// Rows per reduction range: the largest power of two <= 1024 dividing n.
+static long long reduce_range(long long n) {
+  long long R = 1024;
+  while (R > kRows && n % R) R >>= 1;
+  return R;
+}
+
+size_t oz_tc_reduce_partials(long long n, int L, int r, int k, const int *lev_nb, const long long *lev_rows) {
+  const long long R = reduce_range(n);
+  size_t tot = 0;
+  for (int l = 0; l < L; ++l)
+    if (lev_rows[l] > R) tot += (size_t)lev_nb[l] * (size_t)(lev_rows[l] / R) * r * k;
+  return tot;
+}
+
+cudaError_t launch_oz_tc_reduce(const __nv_bfloat16 *Vsl, const int *Vexp, const __nv_bfloat16 *Xsl,
+                                const int *Xexp, long long n, int L, int r, int k, const int *lev_nb,
+                                const long long *lev_rows, double *T, double *P, const int *skip, DevStatus *st,
+                                cudaStream_t s) {
+  if (k <= 0 || n <= 0 || L <= 0) return cudaSuccess;
+  if (r % 8 || r < 8 || r > 64 || n % kRows || L > kMaxLevels) return cudaErrorInvalidValue;
+  OzTcArgs a{};
+  a.R = reduce_range(n);
+  long long toff = 0, poff = 0;
+  for (int l = 0; l < L; ++l) {
+    if (!is_pow2(lev_rows[l]) || lev_rows[l] % kOzChunk) return cudaErrorInvalidValue;
+    a.lrows[l] = lev_rows[l];
+    a.lnb[l] = lev_nb[l];
+    a.toff[l] = toff;
+    toff += (long long)lev_nb[l] * r * k;
+    a.parts[l] = lev_rows[l] > a.R ? (int)(lev_rows[l] / a.R) : 0;
+    a.poff[l] = poff;
+    poff += (long long)lev_nb[l] * a.parts[l] * r * k;
+  }
+  CUtensorMap mV, mX;
+  if (!make_tensor_map_bf16(&mV, Vsl, n, (long long)kOzSlices * L * r, n, kSlab, kRows, 64) ||
+      !make_tensor_map_bf16(&mX, Xsl, n, (long long)kOzSlices * k, n, kSlab, kCols, 64))
+    return cudaErrorInvalidValue;
+  a.Vexp = Vexp;
+  a.Xexp = Xexp;
+  a.T = T;
+  a.P = P;
+  a.n = n;
+  a.m = 128;
+  a.L = L;
+  a.r = r;
+  a.k = k;
+  a.QL = kRows / r;
+  a.nstack = (L + a.QL - 1) / a.QL;
+  a.nct = (k + kCols - 1) / kCols;
+  a.items = ((n + a.R - 1) / a.R) * a.nstack * a.nct;
+  a.skip = skip;
+  a.st = st;
+  cudaError_t e = launch_mode(1, mV, mX, mV, mX, a, s);
   if (e != cudaSuccess) return e;
-  int dev = 0, sms = 0;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  const long long grid = std::min<long long>(a.items, sms > 0 ? sms : 148);
-  HODLR_LAUNCH(oz_tc_resid_kernel, (unsigned)grid, kThreads, bytes, s, mD, mX, mU, mT, a);
+  const long long blk = (long long)r * k;
+  for (int l = 0; l < L; ++l)
+    if (a.parts[l] > 0)
+      HODLR_LAUNCH(oz_tc_pass2_kernel, dim3((unsigned)ceil_div(blk, 256), (unsigned)lev_nb[l]), 256, 0, s,
+                   P + a.poff[l], a.parts[l], blk, T + a.toff[l], skip);
   return cudaGetLastError();
 }
 

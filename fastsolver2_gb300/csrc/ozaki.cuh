@@ -83,4 +83,13 @@ cudaError_t launch_oz_tc_resid(const __nv_bfloat16 *Dsl, const int *Dexp, const 
                                const double *B, long long ldb, float2 *R2, long long ldr, const int *skip,
                                DevStatus *st, cudaStream_t s);
 
+// T_l = V_l^T X for every level in one pass (oz_tc.cu): level l's blocks at
+// T + sum_{l' < l} nb(l') r k (r x k each, ld r); P: partial sums of blocks
+// longer than a reduction range, oz_tc_reduce_partials doubles.
+size_t oz_tc_reduce_partials(long long n, int L, int r, int k, const int *lev_nb, const long long *lev_rows);
+cudaError_t launch_oz_tc_reduce(const __nv_bfloat16 *Vsl, const int *Vexp, const __nv_bfloat16 *Xsl,
+                                const int *Xexp, long long n, int L, int r, int k, const int *lev_nb,
+                                const long long *lev_rows, double *T, double *P, const int *skip, DevStatus *st,
+                                cudaStream_t s);
+
 }  // namespace hodlr
