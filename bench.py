@@ -414,10 +414,12 @@ def run_ours(args, wl):
     # factor, DRAM bytes per launch from the ncu captures in profiles/, N=2^17 x 8)
     bf16_peak = _measured_peak("bf16_tflops")
     if args.resid == 2:
+        # tcgen05: the residual (leaf term and every level's update in one
+        # pass) and the reductions of every level in one pass
         resid_kernels = {
-            "oz_update_kernel": (("resid_update",), "tensor", bf16_peak, OZ_PAIRS, None),
-            "oz_reduce_kernel": (("resid_reduce",), "tensor", bf16_peak, OZ_PAIRS, None),
-            "oz_leaf_kernel": (("resid_leaf",), "tensor", bf16_peak, OZ_PAIRS, None),
+            "oz_tc_kernel<0>": (("resid_leaf", "resid_update"), "tensor", bf16_peak, OZ_PAIRS,
+                                TRAFFIC.get("oz_tc_kernel<0>")),
+            "oz_tc_kernel<1>": (("resid_reduce",), "tensor", bf16_peak, OZ_PAIRS, TRAFFIC.get("oz_tc_kernel<1>")),
         }
     else:
         resid_kernels = {
@@ -426,8 +428,14 @@ def run_ours(args, wl):
             "dw_reduce_kernel": (("resid_reduce",), "fp32_fma_pipe", dw_tf, 1.0, 8 * (100.69e6 + 3.11e6)),
         }
     kernels = dict(resid_kernels)
-    kernels["reduce_tma_kernel"] = (("reduce",), "fp32_fma_pipe", ffma_tf, 1.0, None)
-    kernels["update_tma_kernel"] = (("update",), "fp32_fma_pipe", ffma_tf, 1.0, None)
+    # the FP32 low-rank GEMMs move 4-8 bytes per 2 r flops: HBM-bound, rated
+    # by their algorithmic bytes (each operand read once, C read and written)
+    hbm_peak = _measured_peak("hbm_gbs")
+    upd_bytes = (sum(n * r * 4 + 2 * n * l * r * 4 for l in range(1, L))
+                 + nsw * sum(n * r * 4 + 2 * n * k * 4 for l in range(L)))
+    red_bytes = sum(n * r * 4 + n * (l + 1) * r * 4 for l in range(L)) + nsw * L * (n * r * 4 + n * k * 4)
+    kernels["reduce_tma_kernel"] = (("reduce",), "hbm", hbm_peak, red_bytes, TRAFFIC.get("reduce_tma_kernel"))
+    kernels["update_tma_kernel"] = (("update",), "hbm", hbm_peak, upd_bytes, TRAFFIC.get("update_tma_kernel"))
     roof = None
     best = None
     for kname, spec in kernels.items():
@@ -436,18 +444,28 @@ def run_ours(args, wl):
             best = (kname, kms, spec)
     if best and best[1] > 0:
         kname, kms, (phs, bound, pk, factor, traffic) = best
-        kwork = factor * sum(work[ph] for ph in phs)
         nl = sum(phase_report[ph]["launches_per_step"] for ph in phs)
-        ach = kwork / (kms * 1e-3) / 1e12
-        roof = {"kernel": kname, "bound": bound, "achieved": ach, "peak": pk, "unit": "TFLOP/s",
-                "frac": ach / pk if pk else None, "traffic": traffic,
-                "avg_launch_ms": kms / max(nl, 1), "launches_per_step": nl}
+        if bound == "hbm":  # factor = algorithmic bytes per step
+            ach = factor / (kms * 1e-3) / 1e9
+            roof = {"kernel": kname, "bound": "hbm", "achieved": ach, "peak": pk, "unit": "GB/s",
+                    "frac": ach / pk if pk else None, "traffic": traffic,
+                    "algorithmic_bytes_per_launch": factor / max(nl, 1),
+                    "avg_launch_ms": kms / max(nl, 1), "launches_per_step": nl}
+        else:
+            kwork = factor * sum(work[ph] for ph in phs)
+            ach = kwork / (kms * 1e-3) / 1e12
+            roof = {"kernel": kname, "bound": bound, "achieved": ach, "peak": pk, "unit": "TFLOP/s",
+                    "frac": ach / pk if pk else None, "traffic": traffic,
+                    "avg_launch_ms": kms / max(nl, 1), "launches_per_step": nl}
         if bound == "tensor":
             roof["note"] = ("bf16 digit-product flops (%d digit pairs per FP64 product) of the kernel's phases / "
                             "their CUDA-event time in the timed graphs; peak = the driver-measured dense bf16 "
-                            "GEMM rate (MEASURED_PEAKS.json); frac_of_mma_sync = against the warp-level bf16 MMA "
-                            "rate measured live (hodlr_probe_mma_bf16)" % OZ_PAIRS)
-            roof["frac_of_mma_sync"] = ach / mma_tf
+                            "GEMM rate (MEASURED_PEAKS.json)" % OZ_PAIRS)
+        elif bound == "hbm":
+            roof["note"] = ("algorithmic bytes of the kernel's launches in one step (FP32 operands read once, the "
+                            "updated columns read and written once) / their CUDA-event time in the timed graphs; "
+                            "peak = the driver-measured HBM copy bandwidth (MEASURED_PEAKS.json); traffic = ncu "
+                            "DRAM bytes (read + write) per launch, averaged over one step's launches")
         else:
             roof["note"] = ("FP64-equivalent algorithmic flops of the kernel's phases / their CUDA-event time in "
                             "the timed graphs; peak = this GPU's FFMA rate measured live (hodlr_probe_fp_peaks), "
@@ -462,7 +480,7 @@ def run_ours(args, wl):
                    **wl, "parallelism": "replicas" if world > 1 else "single GPU",
                    "l2": "inputs larger than L2 (>14 GB resident per step)",
                    "residual": {0: "native fp64", 1: "fp64-accurate double-word (FP32 pipes)",
-                                2: "fp64-accurate bf16 digit products (tensor cores, mma.sync)"}[args.resid]},
+                                2: "fp64-accurate bf16 digit products (tcgen05 tensor cores)"}[args.resid]},
         "ms_per_step_without_phase_events": ms_no_events,
         "fp_peaks_measured_tflops": {"ffma": ffma_tf, "dfma": dfma_tf, "mma_sync_bf16": mma_tf,
                                      "hbm_gbs_measured_peaks_json": _measured_peak("hbm_gbs"),
@@ -610,6 +628,10 @@ def run_ragged(args, fs, torch, stream, colmajor):
 
 
 OZ_PAIRS = 28   # digit pairs (s + t <= 6 of 7 x 7) per FP64 product in the tensor-core residual
+# ncu DRAM bytes (read + write) per launch, averaged over the launches of one
+# mixed step at N=2^20 (profiles/dram_traffic_mixed_n2e20_leaf128_r32_k64.md)
+TRAFFIC = {"update_tma_kernel": 38.804e9 / 155, "reduce_tma_kernel": 25.562e9 / 156,
+           "oz_tc_kernel<0>": 21.104e9 / 11, "oz_tc_kernel<1>": (19.496e9 + 0.303e9) / 110}
 
 
 def _measured_peak(key):
