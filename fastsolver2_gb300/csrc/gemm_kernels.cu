@@ -629,7 +629,7 @@ update_tma_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constan
   if (tid == 0) {
     tma_store_2d(&mapC, sC, (int)rowC, j0);
     tma_store_commit();
-    tma_store_wait_all();
+    tma_store_wait_read_all();
   }
 }
 

@@ -37,18 +37,24 @@ namespace {
 constexpr int kRows = 128;   // tile rows (MMA M)
 constexpr int kCols = 64;    // tile columns (MMA N)
 constexpr int kSlab = 32;    // K per stage: one 64-byte swizzled row
-constexpr int kStages = 16;
+// A stage holds one K-half of a group: the seven A digit slabs (128 x 32
+// each) and, after them, the seven B digit slabs (64 x 32 each) contiguous,
+// so that one MMA of A slab s against B slabs t0 .. t1 (N up to 256) writes
+// each product A_s B_t into the columns of its diagonal s + t.
+constexpr int kStages = 2;
 constexpr int kABytes = kRows * kSlab * 2;
 constexpr int kBBytes = kCols * kSlab * 2;
-constexpr int kStageBytes = kABytes + kBBytes;
+constexpr int kAAll = kOzSlices * kABytes;
+constexpr int kStageBytes = kOzSlices * (kABytes + kBBytes);
 constexpr int kEpiWarps = 16;  // four per SM sub-partition; each thread one row, 16 columns
 constexpr int kThreads = 64 + 32 * kEpiWarps;
 constexpr int kEpiCols = kCols / (kEpiWarps / 4);
 constexpr unsigned kTmemCols = 512;
 // kind::f16 instruction descriptor: D f32 (bits 4-5 = 1), A and B bf16
 // (bits 7-9, 10-12 = 1), both K-major, N >> 3 at bit 17, M >> 4 at bit 24.
-constexpr unsigned kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((unsigned)(kCols >> 3) << 17) |
-                            ((unsigned)(kRows >> 4) << 24);
+constexpr unsigned idesc_n(int n) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((unsigned)(n >> 3) << 17) | ((unsigned)(kRows >> 4) << 24);
+}
 constexpr long long kWaitCycles = 2000000000LL;  // about one second
 
 struct Shared {
@@ -76,12 +82,12 @@ __device__ __forceinline__ void tc_relinquish() {
 __device__ __forceinline__ void tc_dealloc(unsigned taddr, unsigned ncols) {
   asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols) : "memory");
 }
-__device__ __forceinline__ void tc_mma(unsigned d, uint64_t a, uint64_t b, unsigned accumulate) {
+__device__ __forceinline__ void tc_mma(unsigned d, uint64_t a, uint64_t b, unsigned idesc, unsigned accumulate) {
   asm volatile(
       "{\n\t.reg .pred p;\n\t"
       "setp.ne.b32 p, %4, 0;\n\t"
       "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(d),
-      "l"(a), "l"(b), "r"(kIdesc), "r"(accumulate)
+      "l"(a), "l"(b), "r"(idesc), "r"(accumulate)
       : "memory");
 }
 // The barrier receives one arrival when every tcgen05.mma this thread issued has completed.
@@ -91,11 +97,6 @@ __device__ __forceinline__ void tc_commit(uint64_t *bar) {
 }
 __device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
-__device__ __forceinline__ void tc_ld8(unsigned taddr, unsigned (&v)[8]) {
-  asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
-               : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7])
-               : "r"(taddr));
-}
 __device__ __forceinline__ void tc_ld4(unsigned taddr, unsigned (&v)[4]) {
   asm volatile("tcgen05.ld.sync.aligned.32x32b.x4.b32 {%0,%1,%2,%3}, [%4];"
                : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3])
@@ -443,19 +444,21 @@ oz_tc_kernel(const __grid_constant__ CUtensorMap mapA0, const __grid_constant__ 
             by = a.ltrow[l] + (it.row0 / a.lrows[l]) * kOzSlices * a.k + it.j0;
             bs = a.k;
           }
-          for (int kh = 0; ok && kh < nkh; ++kh)
-            for (int sl = 0; sl < kOzSlices; ++sl) {
-              const int slot = (int)(issued % kStages);
-              if (!wait_or_abort(&sh->empty[slot], (unsigned)(((issued / kStages) & 1) ^ 1), sh)) {
-                ok = false;
-                break;
-              }
-              unsigned char *sa = stages + slot * kStageBytes, *sb = sa + kABytes;
-              mbar_arrive_expect_tx(&sh->full[slot], kStageBytes);
-              tma_load_2d(sa, ma, &sh->full[slot], ax + kh * kSlab, (int)(ay + sl * as));
-              tma_load_2d(sb, mb, &sh->full[slot], bx + kh * kSlab, (int)(by + sl * bs));
-              ++issued;
+          for (int kh = 0; ok && kh < nkh; ++kh) {
+            const int slot = (int)(issued % kStages);
+            if (!wait_or_abort(&sh->empty[slot], (unsigned)(((issued / kStages) & 1) ^ 1), sh)) {
+              ok = false;
+              break;
             }
+            unsigned char *st = stages + slot * kStageBytes;
+            mbar_arrive_expect_tx(&sh->full[slot], kStageBytes);
+#pragma unroll 1
+            for (int sl = 0; sl < kOzSlices; ++sl) {
+              tma_load_2d(st + sl * kABytes, ma, &sh->full[slot], ax + kh * kSlab, (int)(ay + sl * as));
+              tma_load_2d(st + kAAll + sl * kBBytes, mb, &sh->full[slot], bx + kh * kSlab, (int)(by + sl * bs));
+            }
+            ++issued;
+          }
         }
       }
     }
@@ -471,45 +474,52 @@ oz_tc_kernel(const __grid_constant__ CUtensorMap mapA0, const __grid_constant__ 
           const int nkh = group_khalves<MODE>(a, g);
           const unsigned par_empty = (unsigned)((gcount & 1) ^ 1);
           ++gcount;
+          // The group's K-halves sit in stages it_s (and it_s + 1).  Each
+          // K-half: diagonals 0-3 (tensor-memory columns 0-255, A_s against
+          // B_0 .. B_{3-s}), then diagonals 4-6 (columns 256-447, A_s
+          // against B_{max(0, 4-s)} .. B_{6-s}); a K-half's stage is released
+          // as soon as its products are issued, so that the next group's
+          // first K-half loads while the second one multiplies.
           for (int kh = 0; ok && kh < nkh; ++kh) {
-            // the K-half's seven stages: descriptors of their A and B slabs
-            const unsigned slot0 = (unsigned)(it_s & (kStages - 1)), ph0 = (unsigned)((it_s / kStages) & 1);
-            uint64_t ad[kOzSlices], bd[kOzSlices];
-#pragma unroll
-            for (int t = 0; t < kOzSlices; ++t) {
-              const unsigned sa = smem_u32(stages + ((slot0 + t) & (kStages - 1)) * kStageBytes);
-              ad[t] = desc_sw64(sa);
-              bd[t] = desc_sw64(sa + kABytes);
+            const long long sidx = it_s + kh;
+            const int slot = (int)(sidx & (kStages - 1));
+            if (!wait_or_abort(&sh->full[slot], (unsigned)((sidx / kStages) & 1), sh)) {
+              ok = false;
+              break;
             }
-            const unsigned first = kh == 0 ? 0u : 1u;  // the K-half that starts each diagonal's sum
-#pragma unroll
-            for (int d = 0; d < kOzSlices; ++d) {
-              const unsigned slot = (slot0 + d) & (kStages - 1);
-              if (!wait_or_abort(&sh->full[slot], ph0 ^ (slot < slot0 ? 1u : 0u), sh)) {
-                ok = false;
-                break;
-              }
-              if (kh == 0 && (d == 0 || d == 4)) {
-                if (!wait_or_abort(&sh->acc_empty[d == 0 ? 0 : 1], par_empty, sh)) {
-                  ok = false;
-                  break;
-                }
-              }
-              tc_fence_after();
-              const unsigned dt = tmem + (unsigned)(d * kCols);
-#pragma unroll
-              for (int s = 0; s <= d; ++s)
-#pragma unroll
-                for (int kk = 0; kk < kSlab / 16; ++kk)  // +32 bytes = +2 in the descriptor's address field
-                  tc_mma(dt, ad[s] + 2 * kk, bd[d - s] + 2 * kk, (s > 0 || kk > 0) ? 1u : first);
-              if (kh == nkh - 1 && d == 3) tc_commit(&sh->acc_full[0]);
-              if (kh == nkh - 1 && d == kOzSlices - 1) tc_commit(&sh->acc_full[1]);
+            const unsigned sa = smem_u32(stages + slot * kStageBytes);
+            const uint64_t adesc = desc_sw64(sa), bdesc = desc_sw64(sa + kAAll);
+            if (kh == 0 && !wait_or_abort(&sh->acc_empty[0], par_empty, sh)) {
+              ok = false;
+              break;
             }
-            if (!ok) break;
+            tc_fence_after();
 #pragma unroll
-            for (int t = 0; t < kOzSlices; ++t) tc_commit(&sh->empty[(slot0 + t) & (kStages - 1)]);
-            it_s += kOzSlices;
+            for (int kk = 0; kk < kSlab / 16; ++kk)  // +32 bytes = +2 in the descriptor's address field
+#pragma unroll
+              for (int s = 0; s < 4; ++s)
+                tc_mma(tmem + (unsigned)(64 * s), adesc + (uint64_t)(kABytes / 16 * s + 2 * kk),
+                       bdesc + (uint64_t)(2 * kk), idesc_n(64 * (4 - s)), (kh > 0 || kk > 0 || s > 0) ? 1u : 0u);
+            if (kh == nkh - 1) tc_commit(&sh->acc_full[0]);
+            if (kh == 0 && !wait_or_abort(&sh->acc_empty[1], par_empty, sh)) {
+              ok = false;
+              break;
+            }
+            tc_fence_after();
+#pragma unroll
+            for (int kk = 0; kk < kSlab / 16; ++kk)
+#pragma unroll
+              for (int s = 0; s < kOzSlices; ++s) {
+                const int t0 = s < 4 ? 4 - s : 0;
+                tc_mma(tmem + (unsigned)(64 * (s + t0)), adesc + (uint64_t)(kABytes / 16 * s + 2 * kk),
+                       bdesc + (uint64_t)(kBBytes / 16 * t0 + 2 * kk), idesc_n(64 * (7 - s - t0)),
+                       (kh > 0 || kk > 0 || s > 0) ? 1u : 0u);
+              }
+            if (kh == nkh - 1) tc_commit(&sh->acc_full[1]);
+            tc_commit(&sh->empty[slot]);
           }
+          if (!ok) break;
+          it_s += nkh;
         }
       }
       sh->consumed = (int)it_s;
@@ -594,19 +604,21 @@ oz_tc_kernel(const __grid_constant__ CUtensorMap mapA0, const __grid_constant__ 
         tc_fence_before();
         __syncwarp();
         if (lane == 0) arrive(&sh->acc_empty[1]);
-        if (MODE == 1 && valid && rows1 <= a.R) {
-          // a block of this level ends with this chunk: its T is complete
-          const long long end = (long long)(g + 1) * 64;
-          if ((end & (rows1 - 1)) == 0) {
-            const long long b = end / rows1 - 1;
-            if (b < a.lnb[l1]) store_fp64(a.T + a.toff[l1] + b * a.r * a.k + qq, a.r, rh, rl, jb, a.k);
+        if constexpr (MODE == 1) {
+          if (valid && rows1 <= a.R) {
+            // a block of this level ends with this chunk: its T is complete
+            const long long end = (long long)(g + 1) * 64;
+            if ((end & (rows1 - 1)) == 0) {
+              const long long b = end / rows1 - 1;
+              if (b < a.lnb[l1]) store_fp64(a.T + a.toff[l1] + b * a.r * a.k + qq, a.r, rh, rl, jb, a.k);
 #pragma unroll
-            for (int c = 0; c < kEpiCols; ++c) rh[c] = rl[c] = 0.f;
+              for (int c = 0; c < kEpiCols; ++c) rh[c] = rl[c] = 0.f;
+            }
           }
         }
       }
       if (!ok) break;
-      if (MODE == 1) {
+      if constexpr (MODE == 1) {
         if (valid && rows1 > a.R) {  // this range's part of a longer block
           const long long b = it.row0 / rows1, part = (it.row0 & (rows1 - 1)) / a.R;
           if (b < a.lnb[l1])

@@ -69,6 +69,11 @@ __device__ __forceinline__ void tma_store_2d(const CUtensorMap *map, const void 
                : "memory");
 }
 __device__ __forceinline__ void tma_store_commit() { asm volatile("cp.async.bulk.commit_group;" ::: "memory"); }
+// Wait until every committed store has finished reading its shared memory
+// (the global writes complete on their own; the CTA may then exit).
+__device__ __forceinline__ void tma_store_wait_read_all() {
+  asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
+}
 // Wait until every committed store has finished reading shared memory and
 // its writes are performed.
 __device__ __forceinline__ void tma_store_wait_all() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
