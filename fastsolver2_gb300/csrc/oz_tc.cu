@@ -549,6 +549,9 @@ oz_tc_kernel(const __grid_constant__ CUtensorMap mapA0, const __grid_constant__ 
       const long long lrow0 = it.row0 - it.row0 % a.m;
       const int l1 = it.stack * a.QL + lq;          // mode 1: the row's level
       const bool valid = MODE == 0 || (lq < a.QL && l1 < a.L);
+      // a warp whose rows are all padding of the last level stack only keeps
+      // the barrier phases (waits for the products, then releases them)
+      const bool idle = MODE == 1 && __all_sync(0xffffffffu, !valid);
       const long long rows1 = (MODE == 1 && valid) ? a.lrows[l1] : 0;
       // the row exponent of this thread's row and the column exponent of
       // column jl in group g (loaded one group ahead of their use)
@@ -591,7 +594,7 @@ oz_tc_kernel(const __grid_constant__ CUtensorMap mapA0, const __grid_constant__ 
           break;
         }
         tc_fence_after();
-        drain_region<4, 0>(tl, rh, rl, er, ec, fast);
+        if (!idle) drain_region<4, 0>(tl, rh, rl, er, ec, fast);
         tc_fence_before();
         __syncwarp();
         if (lane == 0) arrive(&sh->acc_empty[0]);
@@ -600,7 +603,7 @@ oz_tc_kernel(const __grid_constant__ CUtensorMap mapA0, const __grid_constant__ 
           break;
         }
         tc_fence_after();
-        drain_region<3, 4>(tl + (unsigned)(4 * kCols), rh, rl, er, ec, fast);
+        if (!idle) drain_region<3, 4>(tl + (unsigned)(4 * kCols), rh, rl, er, ec, fast);
         tc_fence_before();
         __syncwarp();
         if (lane == 0) arrive(&sh->acc_empty[1]);
@@ -735,9 +738,9 @@ cudaError_t launch_oz_tc_resid(const __nv_bfloat16 *Dsl, const int *Dexp, const 
   return launch_mode(0, mD, mX, mU, mT, a, s);
 }
 
-// Rows per reduction range: the largest power of two <= 1024 dividing n.
+// Rows per reduction range: the largest power of two <= 2048 dividing n.
 static long long reduce_range(long long n) {
-  long long R = 1024;
+  long long R = 2048;
   while (R > kRows && n % R) R >>= 1;
   return R;
 }
