@@ -287,14 +287,31 @@ __global__ void resid_finish_kernel(const float2 *R2, long long n, int P, long l
   if (skip && *skip) return;
   const int j = blockIdx.y, pb = blockIdx.x;
   const long long lo = pb * per, hi = min(n, lo + per);
-  double acc = 0.0;
+  // FP32 arithmetic only (GB300's FP64 pipe runs at 1/64 of the FP32 rate):
+  // hi + lo rounds the normalised double-word value to FP32 correctly; the
+  // squares accumulate per thread in FP32 relative to a running power-of-two
+  // scale sc > max |v| (the scale / sum-of-squares scheme of nrm2, every
+  // rescaling exact), so residuals of any magnitude neither underflow nor
+  // overflow; the block combines ssq sc^2 in FP64
+  float sc = 0.f, isc = 0.f, ssq = 0.f;
   for (long long i = lo + threadIdx.x; i < hi; i += blockDim.x) {
     const float2 rv = R2[i + (long long)j * n];
-    const double v = (double)rv.x + (double)rv.y;
-    X32[i + (long long)j * n] = (float)v;
-    acc += v * v;
+    const float v = rv.x + rv.y;
+    X32[i + (long long)j * n] = v;
+    const float av = fabsf(v);
+    if (av >= sc && av > 0.f && av <= 3.4028235e38f) {
+      const int eb = (int)((__float_as_uint(av) >> 23) & 0xff);  // sc = 2^(e + 1) > |v|, at most 2^127
+      const int es = eb < 254 ? eb + 1 : 254;
+      const float ns = __uint_as_float((unsigned)es << 23), ins = __uint_as_float((unsigned)(254 - es) << 23);
+      const float rr = sc * ins;  // old / new scale (a power of two <= 1)
+      ssq *= rr * rr;
+      sc = ns;
+      isc = ins;
+    }
+    const float t = v * isc;
+    ssq = fmaf(t, t, ssq);
   }
-  block_sumsq_store(acc, work, (long long)j * P + pb);
+  block_sumsq_store((double)ssq * (double)sc * (double)sc, work, (long long)j * P + pb);
 }
 
 cudaError_t launch_resid_finish(const float2 *R2, long long n, int k, int P, float *X32, double *work,
