@@ -682,16 +682,10 @@ static int residual_tensor(hodlr_ctx *h, double *X, long long ldx, const double 
     PHASE(h, HODLR_PHASE_RESID_REDUCE,
           launch_oz_tc_reduce(h->Vsl, h->Vexp, h->Xsl, h->Xexp, n, L, r, k, h->lev_nb.data(), h->lev_rows.data(),
                               h->Tall, h->Tpart, skip, h->dst, s));
-    long long toff = 0, eoff = 0, tboff = 0;
-    for (int l = 0; l < L; ++l) {
-      const int nb = h->nb(l);
-      PHASE(h, HODLR_PHASE_MISC,
-            launch_oz_slice_tprime(h->Tall + tboff, h->slev(l), r, k, nb, h->Tsl + toff * r, h->Texp + eoff, skip,
-                                   s));
-      toff += (long long)nb * kOzSlices * k;
-      eoff += (long long)nb * k;
-      tboff += (long long)nb * r * k;
-    }
+    const double *scales[kOzMaxLevels];
+    for (int l = 0; l < L; ++l) scales[l] = h->slev(l);
+    PHASE(h, HODLR_PHASE_MISC,
+          launch_oz_slice_tprime_all(h->Tall, r, k, L, h->lev_nb.data(), scales, h->Tsl, h->Texp, skip, s));
     PHASE(h, HODLR_PHASE_RESID_UPDATE,
           launch_oz_tc_resid(h->Dsl, h->Dexp, h->Xsl, h->Xexp, h->Usl, h->Uexp, h->Tsl, h->Texp, n, m, L, r, k,
                              h->lev_nb.data(), h->lev_rows.data(), B, ldb, h->R2, n, skip, h->dst, s));

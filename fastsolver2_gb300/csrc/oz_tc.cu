@@ -660,16 +660,33 @@ oz_tc_kernel(const __grid_constant__ CUtensorMap mapA0, const __grid_constant__ 
   }
 }
 
-// out_b = sum over parts of P_b (r k values per block, parts in order).
-__global__ void oz_tc_pass2_kernel(const double *__restrict__ P, int parts, long long blk, double *out,
-                                   const int *skip) {
+// The partial sums of every level with blocks longer than a range, in one
+// launch: thread e of level slot i (e < nb r k) sums its element's parts in
+// a fixed order (four interleaved accumulators, combined pairwise).
+struct Pass2Levels {
+  long long pre[kMaxLevels + 1], toff[kMaxLevels], poff[kMaxLevels];
+  int parts[kMaxLevels], n;
+  long long blk;
+};
+__global__ void oz_tc_pass2_kernel(const double *__restrict__ P, double *T, Pass2Levels a, const int *skip) {
   if (skip && *skip) return;
   const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (e >= blk) return;
-  const double *p = P + (long long)blockIdx.y * parts * blk + e;
-  double s = 0.0;
-  for (int c = 0; c < parts; ++c) s += p[(long long)c * blk];
-  out[(long long)blockIdx.y * blk + e] = s;
+  if (e >= a.pre[a.n]) return;
+  int i = 0;
+  while (e >= a.pre[i + 1]) ++i;
+  const long long le = e - a.pre[i], b = le / a.blk, x = le % a.blk;
+  const int parts = a.parts[i];
+  const double *p = P + a.poff[i] + b * parts * a.blk + x;
+  double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;
+  int c = 0;
+  for (; c + 4 <= parts; c += 4) {
+    s0 += p[(long long)c * a.blk];
+    s1 += p[(long long)(c + 1) * a.blk];
+    s2 += p[(long long)(c + 2) * a.blk];
+    s3 += p[(long long)(c + 3) * a.blk];
+  }
+  for (; c < parts; ++c) s0 += p[(long long)c * a.blk];
+  T[a.toff[i] + b * a.blk + x] = (s0 + s1) + (s2 + s3);
 }
 
 static bool is_pow2(long long v) { return v > 0 && (v & (v - 1)) == 0; }
@@ -793,11 +810,20 @@ cudaError_t launch_oz_tc_reduce(const __nv_bfloat16 *Vsl, const int *Vexp, const
   a.st = st;
   cudaError_t e = launch_mode(1, mV, mX, mV, mX, a, s);
   if (e != cudaSuccess) return e;
-  const long long blk = (long long)r * k;
+  Pass2Levels p2{};
+  p2.blk = (long long)r * k;
+  long long pre = 0;
   for (int l = 0; l < L; ++l)
-    if (a.parts[l] > 0)
-      HODLR_LAUNCH(oz_tc_pass2_kernel, dim3((unsigned)ceil_div(blk, 256), (unsigned)lev_nb[l]), 256, 0, s,
-                   P + a.poff[l], a.parts[l], blk, T + a.toff[l], skip);
+    if (a.parts[l] > 0) {
+      p2.pre[p2.n] = pre;
+      p2.toff[p2.n] = a.toff[l];
+      p2.poff[p2.n] = a.poff[l];
+      p2.parts[p2.n] = a.parts[l];
+      pre += (long long)lev_nb[l] * p2.blk;
+      ++p2.n;
+    }
+  p2.pre[p2.n] = pre;
+  if (pre > 0) HODLR_LAUNCH(oz_tc_pass2_kernel, (unsigned)ceil_div(pre, 256), 256, 0, s, P, T, p2, skip);
   return cudaGetLastError();
 }
 

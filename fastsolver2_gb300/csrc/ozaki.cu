@@ -157,6 +157,64 @@ cudaError_t launch_oz_slice_tprime(const double *T, const double *scale, int r, 
   return cudaGetLastError();
 }
 
+// Every level at once: warp w of level l (w < nb(l) k) slices T'_b(:, j) of
+// that level; levels found from the warp prefix sums.
+__global__ void oz_slice_tprime_all_kernel(const double *T, int r, int k, __nv_bfloat16 *out, int *exps,
+                                           TprimeLevels a, const int *skip) {
+  if (skip && *skip) return;
+  const long long w = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (w >= a.wpre[a.L]) return;
+  int l = 0;
+  while (w >= a.wpre[l + 1]) ++l;
+  const long long wl = w - a.wpre[l];
+  const int b = (int)(wl / k), j = (int)(wl % k);
+  const double *src = T + a.toff[l] + (long long)(b ^ 1) * r * k + (long long)j * r;
+  const double *scale = a.scale[l];
+  double v[2];
+#pragma unroll
+  for (int h = 0; h < 2; ++h) {
+    const int q = lane + 32 * h;
+    v[h] = q < r ? (scale ? scale[q] : 1.0) * src[q] : 0.0;
+  }
+  unsigned long long mb = max(abs_bits(v[0]), abs_bits(v[1]));
+#pragma unroll
+  for (int o = 16; o; o >>= 1) mb = max(mb, __shfl_xor_sync(0xffffffffu, mb, o));
+  const int E = oz_exponent_bits(mb);
+  if (lane == 0) exps[a.eoff[l] + (long long)b * k + j] = E;
+  __nv_bfloat16 *o = out + a.ooff[l];
+#pragma unroll
+  for (int h = 0; h < 2; ++h) {
+    const int q = lane + 32 * h;
+    if (q < r)
+      oz_digits(v[h], E, [&](int s, __nv_bfloat16 d) { o[(((long long)b * kOzSlices + s) * k + j) * r + q] = d; });
+  }
+}
+
+cudaError_t launch_oz_slice_tprime_all(const double *T, int r, int k, int L, const int *lev_nb,
+                                       const double *const *scale, __nv_bfloat16 *out, int *exps, const int *skip,
+                                       cudaStream_t s) {
+  if (L <= 0 || k <= 0) return cudaSuccess;
+  if (r > 64 || L > kOzMaxLevels) return cudaErrorInvalidValue;
+  TprimeLevels a{};
+  a.L = L;
+  long long w = 0, t = 0, o = 0, e = 0;
+  for (int l = 0; l < L; ++l) {
+    a.wpre[l] = w;
+    a.toff[l] = t;
+    a.ooff[l] = o;
+    a.eoff[l] = e;
+    a.scale[l] = scale[l];
+    w += (long long)lev_nb[l] * k;
+    t += (long long)lev_nb[l] * r * k;
+    o += (long long)lev_nb[l] * kOzSlices * k * r;
+    e += (long long)lev_nb[l] * k;
+  }
+  a.wpre[L] = w;
+  HODLR_LAUNCH(oz_slice_tprime_all_kernel, (unsigned)ceil_div(w * 32, 256), 256, 0, s, T, r, k, out, exps, a, skip);
+  return cudaGetLastError();
+}
+
 // --------------------------------------------------------------- MMA core
 __device__ __forceinline__ unsigned ld32(const __nv_bfloat16 *p) { return *reinterpret_cast<const unsigned *>(p); }
 

@@ -71,6 +71,19 @@ cudaError_t launch_oz_update(const __nv_bfloat16 *Usl, long long uslice, const i
                              const __nv_bfloat16 *Tsl, const int *Texp, int k, long long rows, int nb, float2 *R2,
                              long long ldr, const int *skip, cudaStream_t s);
 
+// The T' digits of every level in one launch, from every level's T blocks
+// stored one level after another (level l at sum_{l' < l} nb(l') r k); out
+// and exps laid out as the tcgen05 residual reads them (below).
+constexpr int kOzMaxLevels = 32;
+struct TprimeLevels {
+  long long wpre[kOzMaxLevels + 1], toff[kOzMaxLevels], ooff[kOzMaxLevels], eoff[kOzMaxLevels];
+  const double *scale[kOzMaxLevels];
+  int L;
+};
+cudaError_t launch_oz_slice_tprime_all(const double *T, int r, int k, int L, const int *lev_nb,
+                                       const double *const *scale, __nv_bfloat16 *out, int *exps, const int *skip,
+                                       cudaStream_t s);
+
 // R2 = split(B) - D X - sum_l U_l T'_l in one pass over 128-row tiles on
 // the tcgen05 tensor cores (oz_tc.cu): leaf size 128 or 256, the T' digits
 // of every level stored one level after another (level l's block b at line
