@@ -670,11 +670,15 @@ static bool update_tma_try(const UpdateArgs &a, DevStatus *st, cudaStream_t s, c
   return true;
 }
 
+// update_tc.cu: the tcgen05 path (FP32 operands split into bf16 planes)
+bool update_tc_try(const UpdateArgs &a, DevStatus *st, cudaStream_t s, cudaError_t &err);
+
 template <typename T>
 cudaError_t launch_update_nn(const UpdateArgs &a, cudaStream_t s, DevStatus *st) {
   if (a.M <= 0 || a.N <= 0 || a.nbatch <= 0) return cudaSuccess;
   if constexpr (sizeof(T) == 4) {
     cudaError_t e = cudaSuccess;
+    if (update_tc_try(a, st, s, e)) return e;
     if (update_tma_try(a, st, s, e)) return e;
   }
   const int nrt = ceil_div(a.M, kUpdBM), nct = ceil_div(a.N, kUpdBN);

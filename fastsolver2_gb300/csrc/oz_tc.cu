@@ -28,6 +28,7 @@
 
 #include "kernels.cuh"
 #include "ozaki.cuh"
+#include "tcgen05.cuh"
 #include "tma.cuh"
 
 namespace hodlr {
@@ -64,54 +65,6 @@ struct Shared {
   int abort;
   int consumed;  // stages the MMA thread consumed (for the drain after an abort)
 };
-
-// Shared-memory matrix descriptor: K-major, 64-byte swizzle (rows of 64
-// bytes, 8-row atoms of 512 bytes = stride-dimension offset), version 1.
-__device__ __forceinline__ uint64_t desc_sw64(unsigned saddr) {
-  return (uint64_t)((saddr >> 4) & 0x3FFFu) | ((uint64_t)1 << 16) | ((uint64_t)(512 >> 4) << 32) |
-         ((uint64_t)1 << 46) | ((uint64_t)4 << 61);
-}
-
-__device__ __forceinline__ void tc_alloc(unsigned *dst, unsigned ncols) {
-  asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(dst)), "r"(ncols)
-               : "memory");
-}
-__device__ __forceinline__ void tc_relinquish() {
-  asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
-}
-__device__ __forceinline__ void tc_dealloc(unsigned taddr, unsigned ncols) {
-  asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols) : "memory");
-}
-__device__ __forceinline__ void tc_mma(unsigned d, uint64_t a, uint64_t b, unsigned idesc, unsigned accumulate) {
-  asm volatile(
-      "{\n\t.reg .pred p;\n\t"
-      "setp.ne.b32 p, %4, 0;\n\t"
-      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(d),
-      "l"(a), "l"(b), "r"(idesc), "r"(accumulate)
-      : "memory");
-}
-// The barrier receives one arrival when every tcgen05.mma this thread issued has completed.
-__device__ __forceinline__ void tc_commit(uint64_t *bar) {
-  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
-               : "memory");
-}
-__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
-__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
-__device__ __forceinline__ void tc_ld4(unsigned taddr, unsigned (&v)[4]) {
-  asm volatile("tcgen05.ld.sync.aligned.32x32b.x4.b32 {%0,%1,%2,%3}, [%4];"
-               : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3])
-               : "r"(taddr));
-}
-// Waits for this thread's tensor-memory loads; the registers pass through
-// so that no use of them is scheduled before the wait.
-template <int N, int W>
-__device__ __forceinline__ void tc_wait_ld(unsigned (&v)[N][W]) {
-  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-  for (int a = 0; a < N; ++a)
-#pragma unroll
-    for (int b = 0; b < W; ++b) asm volatile("" : "+r"(v[a][b]));
-}
 
 __device__ __forceinline__ void arrive(uint64_t *bar) {
   asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
