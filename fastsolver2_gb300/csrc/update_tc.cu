@@ -36,7 +36,8 @@ namespace {
 constexpr int kBM = 128, kBN = 64, kKS = 32;
 constexpr int kStages = 3;                     // ring of (U tile, C tile) stages
 constexpr int kABytes32 = kKS * kBM * 4;       // the FP32 U tile: 16 KB
-constexpr int kStageBytes = kABytes32 + kBN * kBM * 4;  // + the FP32 C tile: 48 KB
+constexpr int kCBytes32 = kBN * kBM * 4;       // the FP32 C tile: 32 KB
+constexpr int kStageBytes = kABytes32 + kCBytes32 + kBN * kKS * 4;  // + the FP32 eta tile: 56 KB
 constexpr int kPA = kBM * kKS * 2;  // one bf16 plane of the U tile: 8 KB
 constexpr int kPB = kBN * kKS * 2;  // one bf16 plane of the eta tile: 4 KB
 constexpr size_t kSmem = (size_t)kStages * kStageBytes + 3 * kPA + 3 * kPB + 1024;
@@ -66,8 +67,9 @@ __device__ __forceinline__ void put_planes(unsigned char *p0, int plane_bytes, i
 }  // namespace
 
 __global__ void __launch_bounds__(256, 1)
-update_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapC, UpdateArgs a,
-                 int nrt, int nct, long long ntiles, DevStatus *st) {
+update_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapC,
+                 const __grid_constant__ CUtensorMap mapE, UpdateArgs a, int nrt, int nct, long long ntiles,
+                 DevStatus *st) {
   if (a.skip && *a.skip) return;
   extern __shared__ unsigned char smem_raw[];
   unsigned char *base =
@@ -94,10 +96,14 @@ update_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant
     mbar_arrive_expect_tx(&full[sidx], kStageBytes);
     tma_load_2d(sa, &mapA, &full[sidx], (int)((long long)b * a.a_bstride + rt * kBM), 0);
     tma_load_2d(sa + kABytes32, &mapC, &full[sidx], (int)((long long)b * a.c_bstride + rt * kBM), ct * kBN);
+    // eta of child b: rows ((b & 1) ^ flip) r .. of node b >> 1's block, columns ct * kBN ..
+    tma_load_2d(sa + kABytes32 + kCBytes32, &mapE, &full[sidx], (int)(((b & 1) ^ a.b_flip) * a.b_s2),
+                (int)((long long)(b >> 1) * a.N + ct * kBN));
   };
   if (tid == 0) {
     prefetch_tensormap(&mapA);
     prefetch_tensormap(&mapC);
+    prefetch_tensormap(&mapE);
     for (int q = 0; q < kStages; ++q) mbar_init(&full[q], 1);
     mbar_init(&mma_bar, 1);
     mbar_fence_init();
@@ -127,21 +133,19 @@ update_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant
       tma_store_wait_read_all();
       issue(i + kStages - 1);
     }
-    // eta planes of this tile: row j (a column of C), 8 K values per thread
-    {
-      const long long boff = (long long)(b >> 1) * a.b_s1 + (long long)((b & 1) ^ a.b_flip) * a.b_s2;
-      const float *B = a.B32 + boff;
+    bool got = mbar_wait_bounded(&full[sidx], (unsigned)((i / kStages) & 1));
+    if (got) {
+      // eta planes of this tile: row j (a column of C), 8 K values per thread;
+      // rows beyond the rank and columns beyond the block are zero
+      const float *sE = reinterpret_cast<const float *>(base + sidx * kStageBytes + kABytes32 + kCBytes32);
       const int j = tid >> 2, c = tid & 3, jg = ct * kBN + j;
       float x[8];
 #pragma unroll
       for (int e = 0; e < 8; ++e) {
         const int q = 8 * c + e;
-        x[e] = (q < a.K && jg < a.N) ? B[q + (long long)jg * a.ldb] : 0.f;
+        x[e] = (q < a.K && jg < a.N) ? sE[j * kKS + q] : 0.f;
       }
       put_planes(pb, kPB, swz64(j, c), x);
-    }
-    bool got = mbar_wait_bounded(&full[sidx], (unsigned)((i / kStages) & 1));
-    if (got) {
 #pragma unroll
       for (int t = 0; t < 2; ++t) {  // U planes: row r of the tile, 8 K values per task
         const int task = tid + 256 * t, r = task >> 2, c = task & 3;
@@ -221,12 +225,15 @@ bool update_tc_try(const UpdateArgs &a, DevStatus *st, cudaStream_t s, cudaError
   const char *off = getenv("HODLR_NO_TCGEN05");
   if (off && off[0] == '1') return false;
   if (a.a_trans || !a.B32 || a.b_trans || a.K < 1 || a.K > kKS || a.a_bstride != a.M || a.c_bstride != a.M ||
-      a.M % kBM)
+      a.M % kBM || a.nbatch % 2 || a.b_s1 != (long long)a.ldb * a.N || a.b_s2 % 4 || a.ldb < 2 * a.b_s2)
     return false;
   const long long rows = (long long)a.M * a.nbatch;
   CUtensorMap ma, mc;
   if (!make_tensor_map_f32(&ma, static_cast<const float *>(a.A), rows, a.K, a.lda, kBM, kKS, false)) return false;
   if (!make_tensor_map_f32(&mc, static_cast<const float *>(a.C), rows, a.N, a.ldc, kBM, kBN, false)) return false;
+  // eta of every node as one matrix: ldb rows (both children's blocks), N columns per node
+  CUtensorMap me;
+  if (!make_tensor_map_f32(&me, a.B32, a.ldb, (long long)(a.nbatch / 2) * a.N, a.ldb, kKS, kBN, false)) return false;
   const int nrt = a.M / kBM, nct = (a.N + kBN - 1) / kBN;
   static bool attr = false;
   if (!attr) {
@@ -239,7 +246,7 @@ bool update_tc_try(const UpdateArgs &a, DevStatus *st, cudaStream_t s, cudaError
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   const long long grid = std::min<long long>(ntiles, sms > 0 ? sms : 148);
-  HODLR_LAUNCH(update_tc_kernel, (unsigned)grid, 256, kSmem, s, ma, mc, a, nrt, nct, ntiles, st);
+  HODLR_LAUNCH(update_tc_kernel, (unsigned)grid, 256, kSmem, s, ma, mc, me, a, nrt, nct, ntiles, st);
   err = cudaGetLastError();
   return true;
 }
