@@ -435,7 +435,10 @@ def run_ours(args, wl):
                  + nsw * sum(n * r * 4 + 2 * n * k * 4 for l in range(L)))
     red_bytes = sum(n * r * 4 + n * (l + 1) * r * 4 for l in range(L)) + nsw * L * (n * r * 4 + n * k * 4)
     kernels["reduce_tma_kernel"] = (("reduce",), "hbm", hbm_peak, red_bytes, TRAFFIC.get("reduce_tma_kernel"))
-    kernels["update_tma_kernel"] = (("update",), "hbm", hbm_peak, upd_bytes, TRAFFIC.get("update_tma_kernel"))
+    # the update runs on the tcgen05 tensor cores (exact bf16x3 split) unless
+    # HODLR_NO_TCGEN05=1 selects the FP32-FMA TMA kernel; both are HBM-bound
+    upd_name = "update_tma_kernel" if os.environ.get("HODLR_NO_TCGEN05") == "1" else "update_tc_kernel"
+    kernels[upd_name] = (("update",), "hbm", hbm_peak, upd_bytes, TRAFFIC.get(upd_name))
     roof = None
     best = None
     for kname, spec in kernels.items():
@@ -630,8 +633,9 @@ def run_ragged(args, fs, torch, stream, colmajor):
 OZ_PAIRS = 28   # digit pairs (s + t <= 6 of 7 x 7) per FP64 product in the tensor-core residual
 # ncu DRAM bytes (read + write) per launch, averaged over the launches of one
 # mixed step at N=2^20 (profiles/dram_traffic_mixed_n2e20_leaf128_r32_k64.md)
-TRAFFIC = {"update_tma_kernel": 38.804e9 / 155, "reduce_tma_kernel": 25.562e9 / 156,
-           "oz_tc_kernel<0>": 21.104e9 / 11, "oz_tc_kernel<1>": (19.496e9 + 0.303e9) / 110}
+TRAFFIC = {"update_tc_kernel": 38.768e9 / 155, "update_tma_kernel": 38.804e9 / 155,
+           "reduce_tma_kernel": 25.605e9 / 156,
+           "oz_tc_kernel<0>": 21.139e9 / 11, "oz_tc_kernel<1>": (20.175e9 + 0.134e9) / 11}
 
 
 def _measured_peak(key):

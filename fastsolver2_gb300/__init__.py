@@ -8,6 +8,7 @@ library, and loading fails loudly if the library is missing.
 """
 import ctypes
 import os
+import struct
 
 from . import build as _build
 
@@ -92,6 +93,12 @@ SIGNATURES = {
     "hodlr_adjoint": (_I, [_VP, _VP, _I64, _VP, _I64, _I, ctypes.POINTER(Grads)]),
     "hodlr_get_factors": (_I, [_VP, _VP, _VP, _VP, _VP, _VP]),
     "hodlr_get_inputs": (_I, [_VP, _VP, _I64, _I64, _VP, _VP, _VP]),
+    "hodlr_draw_seeds": (_I, [_I64, _I, _VP]),
+    "hodlr_rand_matrix": (_I, [_VP, _I, _I64, _I, _D, _VP, _I64, _VP]),
+    "hodlr_set_seeded": (_I, [_VP, _VP, _VP, _VP, _D]),
+    "hodlr_checkpoint_size": (_I, [_VP, ctypes.POINTER(_I64)]),
+    "hodlr_checkpoint_save": (_I, [_VP, _VP, _I64]),
+    "hodlr_checkpoint_load": (_I, [_VP, _I64, _VP, ctypes.POINTER(_VP)]),
     "hodlr_set_uvd": (_I, [_VP, _VP, _I64, _VP, _I64, _VP]),
     "hodlr_gemm_reduce": (_I, [_I, _I, _I, _I, _VP, _I64, _VP, _I64, _VP, _I64]),
     "hodlr_gemm_reduce_noalloc": (_I, [_I, _I, _I, _I, _VP, _I64, _VP, _I64, _VP, _I64]),
@@ -230,6 +237,31 @@ class Solver:
         stride = self.leaf * self.leaf if leaf_stride is None else leaf_stride
         check(lib().hodlr_get_inputs(self.h, _ptr(D), ld, stride, _ptr(U), _ptr(V), _ptr(s)))
 
+    def set_seeded(self, useeds, vseeds, dseeds, offset=0.0):
+        """Inputs from per-leaf drand48 seeds, as the reference's HMatrix::init builds them."""
+        a = [_seed_array(x) for x in (useeds, vseeds, dseeds)]
+        check(lib().hodlr_set_seeded(self.h, a[0], a[1], a[2], float(offset)))
+
+    def checkpoint(self):
+        """The factored state as bytes (hodlr_checkpoint_save)."""
+        nb = _I64()
+        check(lib().hodlr_checkpoint_size(self.h, ctypes.byref(nb)))
+        buf = ctypes.create_string_buffer(nb.value)
+        check(lib().hodlr_checkpoint_save(self.h, buf, nb.value))
+        return buf.raw
+
+    @classmethod
+    def from_checkpoint(cls, data, stream=None):
+        """A factored Solver from bytes written by checkpoint() (hodlr_checkpoint_load)."""
+        h = ctypes.c_void_p()
+        check(lib().hodlr_checkpoint_load(data, len(data), stream, ctypes.byref(h)))
+        self = cls.__new__(cls)
+        self.h = h
+        self.desc = None
+        # header: magic[8], version, nbuf (uint32), n (int64), leaf, levels, rank (int32)
+        self.n, self.leaf, self.levels, self.rank = struct.unpack_from("<q3i", data, 16)
+        return self
+
     def profile(self, enable=-1, read=False):
         """Switch per-phase timing on/off; with read=True return {phase: (ms, launches)} and reset."""
         if not read:
@@ -349,6 +381,26 @@ def hsolve(nrow, nrhs, rank, nPart, LD, K, U, V, precision=PREC_FP64, stream=Non
     check(lib().hodlr_hsolve_ex(nrow, nrhs, rank, nPart, LD, p(K), p(U), p(V), precision, stream,
                                 ctypes.byref(info)))
     return info
+
+
+def _seed_array(seeds):
+    seeds = [int(x) for x in seeds]
+    return (ctypes.c_int64 * max(1, len(seeds)))(*seeds)
+
+
+def draw_seeds(master, n):
+    """Matrix::rand's per-partition seeds: srand48(master), n lrand48 draws."""
+    out = (ctypes.c_int64 * max(1, n))()
+    check(lib().hodlr_draw_seeds(int(master), int(n), out))
+    return [out[i] for i in range(n)]
+
+
+def rand_matrix(seeds, rows, A, offset=0.0, stream=None):
+    """Fill A (CUDA float64, column-major) with len(seeds) row partitions of `rows` rows, each from its
+    seed's drand48 stream in row-major order (the reference's PtrMatrix::rand)."""
+    cols = A.shape[1] if A.dim() == 2 else 1
+    check(lib().hodlr_rand_matrix(_seed_array(seeds), len(seeds), rows, cols, float(offset), _ptr(A), _ld(A),
+                                  stream))
 
 
 def probe_fp_peaks():

@@ -117,4 +117,71 @@ cudaError_t launch_chol_inv(const double *G, double *Rinv, int r, int nbatch, De
   return cudaGetLastError();
 }
 
+// ---------------------------------------------------------------------------
+// The reference's own seeded generator, bit for bit.  PtrMatrix::rand(seed,
+// offset) (src/ptr_matrix.cc:62-71) fills a block of a partitioned matrix in
+// row-major order from one drand48 stream per partition (Matrix::rand,
+// src/matrix.cc:250-297; the per-partition seeds travel in the MapSeed
+// argument maps, src/lmatrix.cc:327-360).  drand48 is the POSIX 48-bit
+// linear congruential generator X' = (a X + c) mod 2^48, a = 0x5DEECE66D,
+// c = 0xB, seeded as X0 = (seed mod 2^32) 2^16 + 0x330E; a draw returns the
+// new state times 2^-48 (exact in FP64) and lrand48 its top 31 bits.  A row
+// reaches its first state by jumping ahead -- the affine map raised to the
+// row's draw index by binary powering -- so rows fill in parallel.
+
+__global__ void rand_block_kernel(const long long *seeds, int npart, long long rows, int cols, double offset,
+                                  double *A, long long lda) {
+  const long long total = (long long)npart * rows;
+  for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < total;
+       e += (long long)gridDim.x * blockDim.x) {
+    const long long k = e / rows, i = e % rows;
+    unsigned long long x = lcg_jump(lcg_seed(seeds[k]), (unsigned long long)i * (unsigned long long)cols);
+    double *a = A + k * rows + i;
+    for (int j = 0; j < cols; ++j) {
+      x = lcg_step(x);
+      a[(long long)j * lda] = __dadd_rn((double)x * 0x1.0p-48, offset);
+    }
+  }
+}
+
+cudaError_t launch_rand_block(const long long *seeds, int npart, long long rows, int cols, double offset,
+                              double *A, long long lda, cudaStream_t s) {
+  const long long total = (long long)npart * rows;
+  if (total == 0 || cols == 0) return cudaSuccess;
+  const int grid = (int)std::min<long long>(ceil_div(total, 256), 152 * 16);
+  HODLR_LAUNCH(rand_block_kernel, grid, 256, 0, s, seeds, npart, rows, cols, offset, A, lda);
+  return cudaGetLastError();
+}
+
+// DenseBlockTask (src/tasks/dense_block.cc:63-75) with the reference's BLAS
+// loop order (netlib DGEMM 'N','T' with beta = 0: for each column j, the
+// products U(i,l) V(j,l) added into a zeroed column in the order l = 0 ..
+// r-1), then the diagonal D added: K_leaf = U_leaf V_leaf^T + diag(D_leaf).
+// Separate rounded multiplies and adds (no fused multiply-add), so the
+// blocks equal the reference's bit for bit.
+__global__ void seeded_leaves_kernel(const double *__restrict__ U, const double *__restrict__ V,
+                                     const double *__restrict__ Dg, long long n, int m, int r, int nleaf,
+                                     double *K) {
+  const long long mm = (long long)m * m, total = (long long)nleaf * mm;
+  for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < total;
+       e += (long long)gridDim.x * blockDim.x) {
+    const long long k = e / mm, w = e % mm;
+    const int i = (int)(w % m), j = (int)(w / m);
+    const double *u = U + k * m + i, *v = V + k * m + j;
+    double c = 0.0;
+    for (int l = 0; l < r; ++l) c = __dadd_rn(c, __dmul_rn(v[(long long)l * n], u[(long long)l * n]));
+    if (i == j) c = __dadd_rn(c, Dg[k * m + i]);
+    K[e] = c;
+  }
+}
+
+cudaError_t launch_seeded_leaves(const double *U, const double *V, const double *Dg, long long n, int m, int r,
+                                 int nleaf, double *K, cudaStream_t s) {
+  const long long total = (long long)nleaf * m * m;
+  if (total == 0) return cudaSuccess;
+  const int grid = (int)std::min<long long>(ceil_div(total, 256), 152 * 16);
+  HODLR_LAUNCH(seeded_leaves_kernel, grid, 256, 0, s, U, V, Dg, n, m, r, nleaf, K);
+  return cudaGetLastError();
+}
+
 }  // namespace hodlr

@@ -1500,6 +1500,87 @@ int hodlr_hsolve(int nrow, int nrhs, int rank, int nPart, int LD, double *K, dou
 }
 
 // ------------------------------------------------- reference-structured init
+int hodlr_draw_seeds(int64_t master, int n, int64_t *seeds) {
+  if (n < 0 || (n > 0 && !seeds)) return set_err(HODLR_ERR_INVALID_ARG, "bad seed count or null output");
+  unsigned long long x = lcg_seed(master);
+  for (int i = 0; i < n; ++i) {
+    x = lcg_step(x);
+    seeds[i] = (int64_t)(x >> 17);  // lrand48: the top 31 bits of the state
+  }
+  return HODLR_OK;
+}
+
+// The per-partition seeds (host array) on the device, for the fill kernels.
+static int seeds_to_device(const int64_t *seeds, int npart, long long **out, cudaStream_t s) {
+  *out = nullptr;
+  CK(cudaMallocAsync((void **)out, sizeof(long long) * std::max(1, npart), s));
+  CK(cudaMemcpyAsync(*out, seeds, sizeof(long long) * npart, cudaMemcpyHostToDevice, s));
+  return HODLR_OK;
+}
+
+int hodlr_rand_matrix(const int64_t *seeds, int npart, int64_t rows, int cols, double offset, double *A,
+                      int64_t lda, void *stream) {
+  if (!seeds || !A || npart < 1 || rows < 1 || cols < 0) return set_err(HODLR_ERR_INVALID_ARG, "bad argument");
+  if (lda < (int64_t)npart * rows) return set_err(HODLR_ERR_INVALID_ARG, "lda < npart * rows");
+  cudaStream_t s = (cudaStream_t)stream;
+  long long *dseeds = nullptr;
+  CKS(seeds_to_device(seeds, npart, &dseeds, s));
+  cudaError_t e = launch_rand_block(dseeds, npart, rows, cols, offset, A, lda, s);
+  cudaFreeAsync(dseeds, s);
+  CK(e);
+  CK(cudaStreamSynchronize(s));
+  return HODLR_OK;
+}
+
+int hodlr_set_seeded(hodlr_handle h, const int64_t *useeds, const int64_t *vseeds, const int64_t *dseeds,
+                     double offset) {
+  if (!h || !useeds || !vseeds || !dseeds) return set_err(HODLR_ERR_INVALID_ARG, "null argument");
+  if (h->forest) return set_err(HODLR_ERR_INVALID_ARG, "batch handles take hodlr_batch_set_* inputs");
+  const long long n = h->n;
+  const int m = h->m, L = h->L, r = h->r, nl = h->nleaf;
+  cudaStream_t s = h->st;
+  long long *su = nullptr, *sv = nullptr, *sd = nullptr;
+  double *Dg = nullptr;
+  int rc = seeds_to_device(useeds, nl, &su, s);
+  if (rc == HODLR_OK) rc = seeds_to_device(vseeds, nl, &sv, s);
+  if (rc == HODLR_OK) rc = seeds_to_device(dseeds, nl, &sd, s);
+  if (rc == HODLR_OK && cudaMallocAsync((void **)&Dg, sizeof(double) * n, s) != cudaSuccess)
+    rc = set_err(HODLR_ERR_OUT_OF_MEMORY, "cudaMallocAsync");
+  // U, V: N x r, one m-row partition per leaf; D: N entries (+ offset).
+  // Without levels (one dense block) the leaf block uses scratch U and V.
+  double *Ub = nullptr, *Vb = nullptr;
+  if (rc == HODLR_OK && L == 0 &&
+      (cudaMallocAsync((void **)&Ub, sizeof(double) * n * r, s) != cudaSuccess ||
+       cudaMallocAsync((void **)&Vb, sizeof(double) * n * r, s) != cudaSuccess))
+    rc = set_err(HODLR_ERR_OUT_OF_MEMORY, "cudaMallocAsync");
+  double *U0 = L > 0 ? h->Ulev(0) : Ub, *V0 = L > 0 ? h->Vlev(0) : Vb;
+  cudaError_t e = cudaSuccess;
+  if (rc == HODLR_OK) {
+    e = launch_rand_block(su, nl, m, r, 0.0, U0, n, s);
+    if (e == cudaSuccess) e = launch_rand_block(sv, nl, m, r, 0.0, V0, n, s);
+    if (e == cudaSuccess) e = launch_rand_block(sd, nl, m, 1, offset, Dg, n, s);
+    if (e == cudaSuccess) e = launch_seeded_leaves(U0, V0, Dg, n, m, r, nl, h->D, s);
+    for (int l = 1; l < L && e == cudaSuccess; ++l) {  // every level has the same U and V
+      e = cudaMemcpyAsync(h->Ulev(l), U0, sizeof(double) * n * r, cudaMemcpyDeviceToDevice, s);
+      if (e == cudaSuccess) e = cudaMemcpyAsync(h->Vlev(l), V0, sizeof(double) * n * r, cudaMemcpyDeviceToDevice, s);
+    }
+    if (e == cudaSuccess && L > 0) e = launch_fill(h->s, (long long)L * r, 1.0, s);
+  }
+  for (void *p : {(void *)su, (void *)sv, (void *)sd, (void *)Dg, (void *)Ub, (void *)Vb})
+    if (p) cudaFreeAsync(p, s);
+  CKS(rc);
+  CK(e);
+  for (int l = 0; l < L; ++l) {
+    h->has_level[l] = 1;
+    CKS(prepare_level(h, l));
+  }
+  h->has_D = true;
+  CKS(prepare_leaves(h));
+  h->factored = false;
+  CK(cudaStreamSynchronize(s));
+  return HODLR_OK;
+}
+
 int hodlr_set_uvd(hodlr_handle h, const double *U, int64_t ldu, const double *V, int64_t ldv, const double *Dg) {
   if (!h || !U || !V || !Dg) return set_err(HODLR_ERR_INVALID_ARG, "null argument");
   if (ldu < h->n || ldv < h->n) return set_err(HODLR_ERR_INVALID_ARG, "ld < n");
@@ -2256,6 +2337,179 @@ int hodlr_batch_autotune(hodlr_batch b, hodlr_tuning *per_forest, int capacity) 
   b->factor_runs = b->solve_runs = 0;
   b->factored = false;
   return (int)b->forests.size() > 0 ? HODLR_OK : HODLR_OK;
+}
+
+}  // extern "C"
+
+// ------------------------------------------------------------- checkpoints
+// A factored handle as one host byte stream: a header (descriptor, launch
+// shapes, payload size and checksum), then every input and factor buffer as
+// (uint64 byte count, bytes).  The input-derived copies of the mixed path
+// (FP32 V, double-word and digit splits) are rebuilt from the inputs on load
+// rather than stored; workspaces are not state.  No reference counterpart:
+// the reference refactors on every solve (src/hmatrix.cc:49-96).
+namespace {
+
+constexpr char kCkMagic[8] = {'H', 'O', 'D', 'L', 'R', 'C', 'K', '1'};
+constexpr uint32_t kCkVersion = 1;
+
+struct CkHeader {
+  char magic[8];
+  uint32_t version, nbuf;
+  int64_t n;
+  int32_t leaf, levels, rank, nrhs_max, precision, residual;
+  double refine_tol;
+  int32_t refine_max_iter, flags;
+  int32_t red_ctas_per_sm, update_tile_rows;
+  uint64_t payload, checksum;
+};
+
+struct CkBuf {
+  void *p;
+  size_t bytes;
+};
+
+// The state buffers of a plain handle, in stream order.
+std::vector<CkBuf> ck_buffers(const hodlr_ctx *h) {
+  const size_t n = h->n, m = h->m, L = h->L, r = h->r, nl = h->nleaf, nn = h->nnode;
+  const size_t mm = m * m, nlr = n * L * r, cap = nn * 4 * r * r;
+  const bool x = h->mixed;
+  const size_t w = x ? 4 : 8;  // element size of the factor buffers
+  void *sinv = x ? (void *)h->Sinv32 : (void *)h->Sinv;
+  void *dinv = x ? (void *)h->Dinv32 : (void *)h->Dinv;
+  void *lu = x ? (void *)h->LU32 : (void *)h->LU;
+  void *ut = x ? (void *)h->Ut32 : (void *)h->Ut;
+  return {{h->D, nl * mm * 8},         {h->U, nlr * 8},       {h->V, nlr * 8},
+          {h->s, L * r * 8},           {h->ipiv, n * 4},      {h->capLU, cap * 8},
+          {h->cap_ipiv, nn * 2 * r * 4}, {sinv, cap * w},     {dinv, dinv ? nl * mm * w : 0},
+          {lu, nl * mm * w},           {ut, nlr * w}};
+}
+
+// Fletcher-style sum over 32-bit words (every buffer is a whole number of them).
+void ck_sum(const unsigned char *p, size_t bytes, uint64_t &a, uint64_t &b) {
+  const size_t nw = bytes / 4;
+  for (size_t i = 0; i < nw; ++i) {
+    uint32_t v;
+    memcpy(&v, p + 4 * i, 4);
+    a += v;
+    b += a;
+  }
+}
+
+}  // namespace
+
+extern "C" {
+
+int hodlr_checkpoint_size(hodlr_handle h, int64_t *bytes) {
+  if (!h || !bytes) return set_err(HODLR_ERR_INVALID_ARG, "null argument");
+  if (h->forest) return set_err(HODLR_ERR_INVALID_ARG, "batch handles have no checkpoint");
+  if (!h->factored) return set_err(HODLR_ERR_NOT_FACTORED, "not factored");
+  size_t total = sizeof(CkHeader);
+  for (const CkBuf &b : ck_buffers(h)) total += 8 + b.bytes;
+  *bytes = (int64_t)total;
+  return HODLR_OK;
+}
+
+int hodlr_checkpoint_save(hodlr_handle h, void *buf, int64_t bytes) {
+  int64_t need = 0;
+  CKS(hodlr_checkpoint_size(h, &need));
+  if (!buf) return set_err(HODLR_ERR_INVALID_ARG, "null buffer");
+  if (bytes < need) return set_err(HODLR_ERR_INVALID_ARG, "checkpoint buffer too small");
+  CK(cudaStreamSynchronize(h->st));
+  unsigned char *out = static_cast<unsigned char *>(buf);
+  unsigned char *p = out + sizeof(CkHeader);
+  const std::vector<CkBuf> bufs = ck_buffers(h);
+  for (const CkBuf &b : bufs) {
+    const uint64_t nb = b.bytes;
+    memcpy(p, &nb, 8);
+    p += 8;
+    if (nb) CK(cudaMemcpy(p, b.p, nb, cudaMemcpyDeviceToHost));
+    p += nb;
+  }
+  CkHeader hd{};
+  memcpy(hd.magic, kCkMagic, 8);
+  hd.version = kCkVersion;
+  hd.nbuf = (uint32_t)bufs.size();
+  hd.n = h->d.n;
+  hd.leaf = h->d.leaf;
+  hd.levels = h->d.levels;
+  hd.rank = h->d.rank;
+  hd.nrhs_max = h->d.nrhs_max;
+  hd.precision = h->d.precision;
+  hd.residual = h->d.residual;
+  hd.refine_tol = h->d.refine_tol;
+  hd.refine_max_iter = h->d.refine_max_iter;
+  hd.flags = h->d.flags;
+  hd.red_ctas_per_sm = h->tune.red_ctas_per_sm;
+  hd.update_tile_rows = h->tune.upd_bm;
+  hd.payload = (uint64_t)(p - out) - sizeof(CkHeader);
+  uint64_t a = 1, c = 0;
+  ck_sum(out + sizeof(CkHeader), hd.payload, a, c);
+  hd.checksum = a ^ (c << 1);
+  memcpy(out, &hd, sizeof hd);
+  return HODLR_OK;
+}
+
+int hodlr_checkpoint_load(const void *buf, int64_t bytes, void *stream, hodlr_handle *out) {
+  if (!buf || !out) return set_err(HODLR_ERR_INVALID_ARG, "null argument");
+  *out = nullptr;
+  if (bytes < (int64_t)sizeof(CkHeader)) return set_err(HODLR_ERR_INVALID_ARG, "checkpoint truncated");
+  const unsigned char *in = static_cast<const unsigned char *>(buf);
+  CkHeader hd;
+  memcpy(&hd, in, sizeof hd);
+  if (memcmp(hd.magic, kCkMagic, 8) != 0 || hd.version != kCkVersion)
+    return set_err(HODLR_ERR_INVALID_ARG, "not a checkpoint of this library version");
+  if (hd.payload > (uint64_t)bytes - sizeof(CkHeader)) return set_err(HODLR_ERR_INVALID_ARG, "checkpoint truncated");
+  uint64_t a = 1, c = 0;
+  ck_sum(in + sizeof(CkHeader), hd.payload, a, c);
+  if ((a ^ (c << 1)) != hd.checksum) return set_err(HODLR_ERR_INVALID_ARG, "checkpoint checksum mismatch");
+  hodlr_desc d{};
+  d.n = hd.n;
+  d.leaf = hd.leaf;
+  d.levels = hd.levels;
+  d.rank = hd.rank;
+  d.nrhs_max = hd.nrhs_max;
+  d.precision = hd.precision;
+  d.residual = hd.residual;
+  d.refine_tol = hd.refine_tol;
+  d.refine_max_iter = hd.refine_max_iter;
+  d.flags = hd.flags;
+  d.stream = stream;
+  hodlr_tuning t{hd.red_ctas_per_sm, hd.update_tile_rows, -1.0};
+  if (!valid_tuning(t)) return set_err(HODLR_ERR_INVALID_ARG, "checkpoint holds unknown launch shapes");
+  hodlr_handle h = nullptr;
+  CKS(hodlr_create(&d, &h));
+  auto fail = [&](int code, const char *msg) {
+    hodlr_destroy(h);
+    return set_err(code, msg);
+  };
+  if (hodlr_set_tuning(h, &t) != HODLR_OK) return fail(HODLR_ERR_INVALID_ARG, "checkpoint launch shapes");
+  const std::vector<CkBuf> bufs = ck_buffers(h);
+  if (hd.nbuf != bufs.size()) return fail(HODLR_ERR_INVALID_ARG, "checkpoint does not match its descriptor");
+  const unsigned char *p = in + sizeof(CkHeader), *end = p + hd.payload;
+  for (const CkBuf &b : bufs) {
+    uint64_t nb = 0;
+    if (end - p < 8) return fail(HODLR_ERR_INVALID_ARG, "checkpoint truncated");
+    memcpy(&nb, p, 8);
+    p += 8;
+    if (nb != b.bytes || (uint64_t)(end - p) < nb)
+      return fail(HODLR_ERR_INVALID_ARG, "checkpoint does not match its descriptor");
+    if (nb && cudaMemcpy(b.p, p, nb, cudaMemcpyHostToDevice) != cudaSuccess)
+      return fail(HODLR_ERR_CUDA, "checkpoint copy to the device");
+    p += nb;
+  }
+  h->has_D = true;
+  std::fill(h->has_level.begin(), h->has_level.end(), (char)1);
+  int rc = prepare_leaves(h);
+  for (int l = 0; l < h->L && rc == HODLR_OK; ++l) rc = prepare_level(h, l);
+  if (rc != HODLR_OK) {
+    hodlr_destroy(h);
+    return rc;
+  }
+  if (cudaStreamSynchronize(h->st) != cudaSuccess) return fail(HODLR_ERR_CUDA, "checkpoint preparation");
+  h->factored = true;
+  *out = h;
+  return HODLR_OK;
 }
 
 }  // extern "C"

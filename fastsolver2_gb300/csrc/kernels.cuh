@@ -198,6 +198,38 @@ cudaError_t launch_gaussian(double *X, long long ld, long long n, int c, unsigne
 // Leaf blocks [nleaf][m][m] = G/sqrt(m) + shift*I.
 cudaError_t launch_gen_leaves(double *D, int m, int nleaf, unsigned long long seed, double shift,
                               cudaStream_t s);
+// The reference's drand48 generator (POSIX 48-bit LCG): srand48 seeding,
+// one step, and the state after t steps (the affine map powered by squaring;
+// the maps x -> a^k x + c_k commute, so the order of composition is free).
+constexpr unsigned long long kLcgA = 0x5DEECE66Dull, kLcgC = 0xBull, kLcgMask = (1ull << 48) - 1;
+__host__ __device__ inline unsigned long long lcg_seed(long long seed) {
+  return (((unsigned long long)seed & 0xffffffffull) << 16) | 0x330Eull;
+}
+__host__ __device__ inline unsigned long long lcg_step(unsigned long long x) {
+  return (kLcgA * x + kLcgC) & kLcgMask;
+}
+__host__ __device__ inline unsigned long long lcg_jump(unsigned long long x, unsigned long long t) {
+  unsigned long long a = kLcgA, c = kLcgC, A = 1, C = 0;
+  while (t) {
+    if (t & 1) {
+      A = (a * A) & kLcgMask;
+      C = (a * C + c) & kLcgMask;
+    }
+    c = (a * c + c) & kLcgMask;
+    a = (a * a) & kLcgMask;
+    t >>= 1;
+  }
+  return (A * x + C) & kLcgMask;
+}
+// Partition k (rows [k*rows, (k+1)*rows) of A, cols columns, ld lda) filled
+// in row-major order from the drand48 stream seeded by seeds[k] (device
+// array), each draw plus offset.
+cudaError_t launch_rand_block(const long long *seeds, int npart, long long rows, int cols, double offset,
+                              double *A, long long lda, cudaStream_t s);
+// Leaf blocks [nleaf][m][m] = U_k V_k^T + diag(D_k) in the reference's BLAS
+// order, without fused multiply-adds (U, V: n x r, ld n; Dg: n entries).
+cudaError_t launch_seeded_leaves(const double *U, const double *V, const double *Dg, long long n, int m, int r,
+                                 int nleaf, double *K, cudaStream_t s);
 // Per-block Cholesky of Gram matrices G_b (r x r, ld r) and the inverse of
 // the upper factor: Rinv_b (r x r, ld r), G = R^T R.  Reports failure in st.
 cudaError_t launch_chol_inv(const double *G, double *Rinv, int r, int nbatch, DevStatus *st,

@@ -4,6 +4,8 @@
 // shared-memory matrix descriptor of the K-major 64-byte-swizzled layout
 // that a TMA load with CU_TENSOR_MAP_SWIZZLE_64B produces.
 #pragma once
+#include <cuda_bf16.h>
+
 #include <cstdint>
 
 #include "tma.cuh"
@@ -72,6 +74,31 @@ __device__ __forceinline__ void tc_wait_ld(unsigned (&v)[N][W]) {
   for (int a = 0; a < N; ++a)
 #pragma unroll
     for (int b = 0; b < W; ++b) asm volatile("" : "+r"(v[a][b]));
+}
+
+// Exact three-way bf16 split of an FP32 value, x = h + m + l (24 significant
+// bits; both subtractions are exact), for FP32-class products on the bf16
+// tensor cores from the six partial products down to 2^-16.
+__device__ __forceinline__ void split3(float x, __nv_bfloat16 &h, __nv_bfloat16 &m, __nv_bfloat16 &l) {
+  h = __float2bfloat16_rn(x);
+  const float r1 = x - __bfloat162float(h);
+  m = __float2bfloat16_rn(r1);
+  l = __float2bfloat16_rn(r1 - __bfloat162float(m));
+}
+
+// Byte offset of 16-byte chunk c (of 4) of row i in a K-major tile of 64-byte
+// rows with the 64-byte swizzle (chunk index XOR address bits 7-8; the tile
+// base is 1024-byte aligned).
+__device__ __forceinline__ int swz64(int i, int c) { return i * 64 + ((c ^ ((i >> 1) & 3)) << 4); }
+
+// Writes the three planes of 8 consecutive K values of one row.
+__device__ __forceinline__ void put_planes(unsigned char *p0, int plane_bytes, int off, const float (&x)[8]) {
+  __align__(16) __nv_bfloat16 h[8], m[8], l[8];
+#pragma unroll
+  for (int e = 0; e < 8; ++e) split3(x[e], h[e], m[e], l[e]);
+  *reinterpret_cast<uint4 *>(p0 + off) = *reinterpret_cast<const uint4 *>(h);
+  *reinterpret_cast<uint4 *>(p0 + plane_bytes + off) = *reinterpret_cast<const uint4 *>(m);
+  *reinterpret_cast<uint4 *>(p0 + 2 * plane_bytes + off) = *reinterpret_cast<const uint4 *>(l);
 }
 
 }  // namespace hodlr

@@ -42,28 +42,6 @@ constexpr int kPA = kBM * kKS * 2;  // one bf16 plane of the U tile: 8 KB
 constexpr int kPB = kBN * kKS * 2;  // one bf16 plane of the eta tile: 4 KB
 constexpr size_t kSmem = (size_t)kStages * kStageBytes + 3 * kPA + 3 * kPB + 1024;
 
-__device__ __forceinline__ void split3(float x, __nv_bfloat16 &h, __nv_bfloat16 &m, __nv_bfloat16 &l) {
-  h = __float2bfloat16_rn(x);
-  const float r1 = x - __bfloat162float(h);
-  m = __float2bfloat16_rn(r1);
-  l = __float2bfloat16_rn(r1 - __bfloat162float(m));
-}
-
-// Byte offset of 16-byte chunk c (of 4) of row i in a K-major tile of 64-byte
-// rows with the 64-byte swizzle (chunk index XOR address bits 7-8; the tile
-// base is 1024-byte aligned).
-__device__ __forceinline__ int swz64(int i, int c) { return i * 64 + ((c ^ ((i >> 1) & 3)) << 4); }
-
-// Writes the three planes of 8 consecutive K values of one row.
-__device__ __forceinline__ void put_planes(unsigned char *p0, int plane_bytes, int off, const float (&x)[8]) {
-  __align__(16) __nv_bfloat16 h[8], m[8], l[8];
-#pragma unroll
-  for (int e = 0; e < 8; ++e) split3(x[e], h[e], m[e], l[e]);
-  *reinterpret_cast<uint4 *>(p0 + off) = *reinterpret_cast<const uint4 *>(h);
-  *reinterpret_cast<uint4 *>(p0 + plane_bytes + off) = *reinterpret_cast<const uint4 *>(m);
-  *reinterpret_cast<uint4 *>(p0 + 2 * plane_bytes + off) = *reinterpret_cast<const uint4 *>(l);
-}
-
 }  // namespace
 
 __global__ void __launch_bounds__(256, 1)
@@ -138,17 +116,20 @@ update_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant
       // eta planes of this tile: row j (a column of C), 8 K values per thread;
       // rows beyond the rank and columns beyond the block are zero
       const float *sE = reinterpret_cast<const float *>(base + sidx * kStageBytes + kABytes32 + kCBytes32);
+      // eta planes: 8 consecutive K values of column j (two 16-byte loads;
+      // a quarter warp reads 128 contiguous bytes)
       const int j = tid >> 2, c = tid & 3, jg = ct * kBN + j;
-      float x[8];
+      const float4 e0 = *reinterpret_cast<const float4 *>(sE + j * kKS + 8 * c);
+      const float4 e1 = *reinterpret_cast<const float4 *>(sE + j * kKS + 8 * c + 4);
+      float x[8] = {e0.x, e0.y, e0.z, e0.w, e1.x, e1.y, e1.z, e1.w};
 #pragma unroll
-      for (int e = 0; e < 8; ++e) {
-        const int q = 8 * c + e;
-        x[e] = (q < a.K && jg < a.N) ? sE[j * kKS + q] : 0.f;
-      }
+      for (int e = 0; e < 8; ++e)
+        if (8 * c + e >= a.K || jg >= a.N) x[e] = 0.f;
       put_planes(pb, kPB, swz64(j, c), x);
 #pragma unroll
       for (int t = 0; t < 2; ++t) {  // U planes: row r of the tile, 8 K values per task
-        const int task = tid + 256 * t, r = task >> 2, c = task & 3;
+        // consecutive lanes take consecutive rows: conflict-free column reads
+        const int task = tid + 256 * t, r = task & (kBM - 1), c = task >> 7;
         float x[8];
 #pragma unroll
         for (int e = 0; e < 8; ++e) x[e] = sA[(8 * c + e) * kBM + r];

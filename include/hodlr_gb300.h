@@ -192,6 +192,40 @@ HODLR_API int hodlr_adjoint(hodlr_handle h, const double *x, int64_t ldx,
 HODLR_API int hodlr_get_factors(hodlr_handle h, double *leaf_lu, int32_t *leaf_ipiv,
                       double *utilde, double *cap_lu, int32_t *cap_ipiv);
 
+/* The reference's seeded inputs, bit for bit (Matrix::rand src/matrix.cc:
+ * 250-297, PtrMatrix::rand src/ptr_matrix.cc:62-71, the MapSeed argument maps
+ * src/lmatrix.cc:327-360, DenseBlockTask src/tasks/dense_block.cc:35-76),
+ * generated in device memory.  drand48 is the POSIX 48-bit LCG.
+ * hodlr_draw_seeds: n per-partition seeds as Matrix::rand draws them
+ * (srand48(master), then n lrand48 draws) into host memory; the reference
+ * seeds `master` from the clock, a caller passes it.
+ * hodlr_rand_matrix: A (device, column-major, lda >= npart*rows) gets npart
+ * row partitions of `rows` rows; partition k is filled in row-major order
+ * from the drand48 stream of seeds[k] (host array), each draw + offset.
+ * Runs on `stream` (NULL = legacy default) and returns when done.
+ * hodlr_set_seeded: the handle's inputs as HMatrix::init(U, V, D) builds them
+ * from per-leaf seeds (host arrays of 2^levels): U and V (N x r, the same at
+ * every level), D (N entries, draws + offset), leaf blocks U_k V_k^T +
+ * diag(D_k) in the reference's BLAS order; s = 1. */
+HODLR_API int hodlr_draw_seeds(int64_t master, int n, int64_t *seeds);
+HODLR_API int hodlr_rand_matrix(const int64_t *seeds, int npart, int64_t rows, int cols, double offset, double *A,
+                                int64_t lda, void *stream);
+HODLR_API int hodlr_set_seeded(hodlr_handle h, const int64_t *useeds, const int64_t *vseeds, const int64_t *dseeds,
+                               double offset);
+
+/* Checkpoint of a factored plain handle (no counterpart in the reference,
+ * which refactors on every solve): the descriptor, the launch shapes, the
+ * inputs and every factor buffer in one host byte stream with a checksum.
+ * hodlr_checkpoint_size gives the byte count; hodlr_checkpoint_save writes
+ * it into host memory `buf` of `bytes` bytes; hodlr_checkpoint_load creates a
+ * factored handle from it on `stream` (NULL = a stream of its own) whose
+ * solves give the same bits as the saved handle's.  Batch handles have no
+ * checkpoint (HODLR_ERR_INVALID_ARG); a corrupted or truncated stream is
+ * refused with HODLR_ERR_INVALID_ARG. */
+HODLR_API int hodlr_checkpoint_size(hodlr_handle h, int64_t *bytes);
+HODLR_API int hodlr_checkpoint_save(hodlr_handle h, void *buf, int64_t bytes);
+HODLR_API int hodlr_checkpoint_load(const void *buf, int64_t bytes, void *stream, hodlr_handle *out);
+
 /* ------------------------------------------------- component entry points */
 /* LMatrix::gemmRed('t', 'n', 1.0, V, U, 0.0, W) over nPart row partitions
  * (src/lmatrix.cc:713-761, GemmRedTask src/tasks/gemm_reduce.cc:33-83):

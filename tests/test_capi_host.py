@@ -90,3 +90,24 @@ def test_no_cpu_fallback_when_library_missing(monkeypatch, tmp_path):
     monkeypatch.setattr(fs, "LIB_PATH", str(tmp_path / "missing.so"))
     with pytest.raises(ImportError):
         fs.lib()
+
+
+def test_checkpoint_load_rejects_bad_streams_on_host(fs):
+    L = fs.lib()
+    h = ctypes.c_void_p()
+    # shorter than a header
+    assert L.hodlr_checkpoint_load(b"HODLRCK1", 8, None, ctypes.byref(h)) == fs.HODLR_ERR_INVALID_ARG
+    # a header-sized stream without the magic
+    junk = bytes(256)
+    assert L.hodlr_checkpoint_load(junk, len(junk), None, ctypes.byref(h)) == fs.HODLR_ERR_INVALID_ARG
+    assert b"checkpoint" in L.hodlr_last_error_string()
+    assert not h.value
+    assert L.hodlr_checkpoint_size(None, None) == fs.HODLR_ERR_INVALID_ARG
+    assert L.hodlr_checkpoint_save(None, None, 0) == fs.HODLR_ERR_INVALID_ARG
+
+
+def test_draw_seeds_matches_glibc_lrand48_stream(fs):
+    """hodlr_draw_seeds (host code) against the oracle's srand48_r/lrand48_r calls."""
+    from oracle import oracle as O
+    for master in (0, 1, 20240601, 2**31 - 1, 2**40 + 12345, -7):
+        assert fs.draw_seeds(master, 37) == [int(x) for x in O.seeds(master, 37)]
