@@ -367,3 +367,30 @@ def test_tcgen05_residual_extreme_exponents(hodlr, monkeypatch):
     assert i2.status == hodlr.HODLR_OK and i2.rel_residual <= 1e-12
     assert rel(X2, X1) < 1e-11
     assert P.rel_residual(pr, X2) < 2e-12
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+@pytest.mark.parametrize("rank0,rank1", [(12, 5), (3, 16)])
+def test_unequal_sibling_ranks_by_zero_padding(hodlr, precision, rank0, rank1):
+    """The irregular-rank tree of solver_irregular_ranks.cc / node_solve_region.cc:77-97
+    (K01 = U0 V1^T with rank0 columns, K10 = U1 V0^T with rank1) solved by the uniform
+    path with bases zero-padded to max(rank0, rank1)."""
+    m, L = 64, 4
+    r = max(rank0, rank1)
+    pr = P.gaussian_problem(m, L, r, nrhs=3, seed=44, orthonormal=True, decay=2.0, shift=2.0)
+    for l in range(L):
+        half = pr.n >> (l + 1)
+        for c in range(2 << l):
+            rows = slice(c * half, (c + 1) * half)
+            ru, rv = (rank0, rank1) if c % 2 == 0 else (rank1, rank0)
+            pr.U[l][rows, ru:] = 0.0
+            pr.V[l][rows, rv:] = 0.0
+    s = make_solver(hodlr, pr, precision=precision, refine_tol=1e-12)
+    s.factor()
+    B = to_dev(pr.B)
+    info = s.solve(B)
+    X = to_host(B)
+    Xd = np.linalg.solve(pr.dense(), pr.B)
+    assert rel(X, Xd) < (1e-11 if precision == 0 else 1e-10)
+    if precision == 1:
+        assert info.rel_residual <= 1e-12
