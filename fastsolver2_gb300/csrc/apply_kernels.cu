@@ -135,63 +135,68 @@ leaf_apply_kernel(const T *__restrict__ Dinv, T *X, long long ldx, int ncols, co
 }
 
 // The FP32 leaf-128 case (every mixed-path leaf application but the
-// transposed ones) with float4 operand reads: a thread owns rows
-// 4 ti .. 4 ti + 3 and 64 + 4 ti .. 64 + 4 ti + 3 (two 16-byte loads of the
-// Dinv slab per k) and columns tj + 16 b (four broadcast loads of the X
-// tile) -- 6 shared loads per 32 FMAs instead of 12.  The result goes back
-// through shared memory (16-byte stores) for coalesced global stores.
-__global__ void __launch_bounds__(256)
+// transposed ones) with 8 x 8 register tiles read as float4 runs: 128
+// threads per (leaf, 64-column tile); a thread owns rows 4 ti .. 4 ti + 3 and
+// 64 + 4 ti .. 64 + 4 ti + 3 and columns 8 tj .. 8 tj + 7.  The X tile is
+// staged transposed ([k][column], rows padded to 68 floats) so that both
+// operands come as two 16-byte loads: 4 shared loads per 64 FMAs.  The
+// result goes back through shared memory for coalesced global stores.
+constexpr int kLa128Threads = 128, kLa128CT = 64, kLa128LD = kLa128CT + 4;
+constexpr size_t kLa128Smem = (size_t)(128 * kLa128LD + 32 * 128) * sizeof(float);
+
+__global__ void __launch_bounds__(kLa128Threads, 4)
 leaf_apply128_f32_kernel(const float *__restrict__ Dinv, float *X, long long ldx, int ncols, const int *skip) {
   if (skip && *skip) return;
-  constexpr int M = 128, CT = 64, KC = 32;
+  constexpr int M = 128, CT = kLa128CT, LD = kLa128LD, KC = 32, NT = kLa128Threads;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  float *sX = reinterpret_cast<float *>(smem_raw);  // M x CT, ld M
-  float *sA = sX + M * CT;                           // [KC][M]: sA[q * M + i] = Dinv(i, k0 + q)
+  float *sXt = reinterpret_cast<float *>(smem_raw);  // [M][LD]: sXt[k * LD + j] = X(k, j)
+  float *sA = sXt + M * LD;                           // [KC][M]: sA[q * M + i] = Dinv(i, k0 + q)
   const int leaf = blockIdx.y, c0 = blockIdx.x * CT, nc = min(CT, ncols - c0);
   const float *A = Dinv + (long long)leaf * M * M;
   float *Xg = X + (long long)leaf * M + (long long)c0 * ldx;
   const int tid = threadIdx.x, ti = tid & 15, tj = tid >> 4;
-  for (int e = tid; e < M * CT; e += 256) {
+  for (int e = tid; e < M * CT; e += NT) {  // coalesced along the rows of X
     const int i = e % M, j = e / M;
-    sX[e] = j < nc ? Xg[i + (long long)j * ldx] : 0.f;
+    sXt[i * LD + j] = j < nc ? Xg[i + (long long)j * ldx] : 0.f;
   }
-  float acc[8][4];
+  float acc[8][8];
 #pragma unroll
   for (int a = 0; a < 8; ++a)
 #pragma unroll
-    for (int b = 0; b < 4; ++b) acc[a][b] = 0.f;
+    for (int b = 0; b < 8; ++b) acc[a][b] = 0.f;
   for (int k0 = 0; k0 < M; k0 += KC) {
     __syncthreads();
-    for (int e = tid; e < M * KC / 4; e += 256) {  // the slab, 16-byte copies
+    for (int e = tid; e < M * KC / 4; e += NT) {  // the slab, 16-byte copies
       const int i4 = e % (M / 4), q = e / (M / 4);
       reinterpret_cast<float4 *>(sA + q * M)[i4] = reinterpret_cast<const float4 *>(A + (long long)(k0 + q) * M)[i4];
     }
     __syncthreads();
-#pragma unroll 4
+#pragma unroll 2
     for (int q = 0; q < KC; ++q) {
       const float4 a0 = *reinterpret_cast<const float4 *>(sA + q * M + 4 * ti);
       const float4 a1 = *reinterpret_cast<const float4 *>(sA + q * M + 64 + 4 * ti);
+      const float4 x0 = *reinterpret_cast<const float4 *>(sXt + (k0 + q) * LD + 8 * tj);
+      const float4 x1 = *reinterpret_cast<const float4 *>(sXt + (k0 + q) * LD + 8 * tj + 4);
       const float av[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
-      float xb[4];
-#pragma unroll
-      for (int b = 0; b < 4; ++b) xb[b] = sX[(k0 + q) + (tj + 16 * b) * M];
+      const float xb[8] = {x0.x, x0.y, x0.z, x0.w, x1.x, x1.y, x1.z, x1.w};
 #pragma unroll
       for (int a = 0; a < 8; ++a)
 #pragma unroll
-        for (int b = 0; b < 4; ++b) acc[a][b] = fmaf(av[a], xb[b], acc[a][b]);
+        for (int b = 0; b < 8; ++b) acc[a][b] = fmaf(av[a], xb[b], acc[a][b]);
     }
   }
-  __syncthreads();  // every thread is done with sX: it takes the result
+  __syncthreads();  // every thread is done with sXt: it takes the result, column-major ld M
+  float *sY = sXt;
 #pragma unroll
-  for (int b = 0; b < 4; ++b) {
-    float *col = sX + (tj + 16 * b) * M;
+  for (int b = 0; b < 8; ++b) {
+    float *col = sY + (8 * tj + b) * M;
     *reinterpret_cast<float4 *>(col + 4 * ti) = make_float4(acc[0][b], acc[1][b], acc[2][b], acc[3][b]);
     *reinterpret_cast<float4 *>(col + 64 + 4 * ti) = make_float4(acc[4][b], acc[5][b], acc[6][b], acc[7][b]);
   }
   __syncthreads();
-  for (int e = tid; e < M * CT; e += 256) {
+  for (int e = tid; e < M * CT; e += NT) {
     const int i = e % M, j = e / M;
-    if (j < nc) Xg[i + (long long)j * ldx] = sX[e];
+    if (j < nc) Xg[i + (long long)j * ldx] = sY[e];
   }
 }
 
@@ -204,9 +209,10 @@ static cudaError_t leaf_apply_m(const T *Dinv, int nleaf, T *X, long long ldx, i
   if constexpr (std::is_same<T, float>::value && M == 128) {
     if (!trans) {
       auto k = leaf_apply128_f32_kernel;
-      cudaError_t e = set_smem(k, bytes);
+      cudaError_t e = set_smem(k, kLa128Smem);
       if (e != cudaSuccess) return e;
-      HODLR_LAUNCH(k, grid, 256, bytes, s, Dinv, X, ldx, ncols, skip);
+      HODLR_LAUNCH(k, dim3(ceil_div(ncols, kLa128CT), nleaf), kLa128Threads, kLa128Smem, s, Dinv, X, ldx, ncols,
+                   skip);
       return cudaGetLastError();
     }
   }
