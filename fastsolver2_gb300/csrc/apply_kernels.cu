@@ -144,8 +144,13 @@ leaf_apply_kernel(const T *__restrict__ Dinv, T *X, long long ldx, int ncols, co
 constexpr int kLa128Threads = 128, kLa128CT = 64, kLa128LD = kLa128CT + 4;
 constexpr size_t kLa128Smem = (size_t)(128 * kLa128LD + 32 * 128) * sizeof(float);
 
+// The source tile may be another matrix, of FP32 or FP64 (rounded to FP32
+// as it is staged): the factorisation's first application reads U in FP64
+// and writes Utilde in FP32 with no separate conversion pass.
+template <typename S>
 __global__ void __launch_bounds__(kLa128Threads, 4)
-leaf_apply128_f32_kernel(const float *__restrict__ Dinv, float *X, long long ldx, int ncols, const int *skip) {
+leaf_apply128_f32_kernel(const float *__restrict__ Dinv, const S *Xs, long long lds, float *X, long long ldx,
+                         int ncols, const int *skip) {
   if (skip && *skip) return;
   constexpr int M = 128, CT = kLa128CT, LD = kLa128LD, KC = 32, NT = kLa128Threads;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -154,10 +159,11 @@ leaf_apply128_f32_kernel(const float *__restrict__ Dinv, float *X, long long ldx
   const int leaf = blockIdx.y, c0 = blockIdx.x * CT, nc = min(CT, ncols - c0);
   const float *A = Dinv + (long long)leaf * M * M;
   float *Xg = X + (long long)leaf * M + (long long)c0 * ldx;
+  const S *Xsg = Xs + (long long)leaf * M + (long long)c0 * lds;
   const int tid = threadIdx.x, ti = tid & 15, tj = tid >> 4;
   for (int e = tid; e < M * CT; e += NT) {  // coalesced along the rows of X
     const int i = e % M, j = e / M;
-    sXt[i * LD + j] = j < nc ? Xg[i + (long long)j * ldx] : 0.f;
+    sXt[i * LD + j] = j < nc ? (float)Xsg[i + (long long)j * lds] : 0.f;
   }
   float acc[8][8];
 #pragma unroll
@@ -208,11 +214,11 @@ static cudaError_t leaf_apply_m(const T *Dinv, int nleaf, T *X, long long ldx, i
   dim3 grid(ceil_div(ncols, CT), nleaf);
   if constexpr (std::is_same<T, float>::value && M == 128) {
     if (!trans) {
-      auto k = leaf_apply128_f32_kernel;
+      auto k = leaf_apply128_f32_kernel<float>;
       cudaError_t e = set_smem(k, kLa128Smem);
       if (e != cudaSuccess) return e;
-      HODLR_LAUNCH(k, dim3(ceil_div(ncols, kLa128CT), nleaf), kLa128Threads, kLa128Smem, s, Dinv, X, ldx, ncols,
-                   skip);
+      HODLR_LAUNCH(k, dim3(ceil_div(ncols, kLa128CT), nleaf), kLa128Threads, kLa128Smem, s, Dinv,
+                   (const float *)X, ldx, X, ldx, ncols, skip);
       return cudaGetLastError();
     }
   }
@@ -231,6 +237,18 @@ static cudaError_t leaf_apply_m(const T *Dinv, int nleaf, T *X, long long ldx, i
 }
 
 bool leaf_apply_supported(int m) { return m == 64 || m == 128 || m == 256; }
+
+cudaError_t launch_leaf_apply_f64src(const float *Dinv, int m, int nleaf, const double *Xs, long long lds, float *X,
+                                     long long ldx, int ncols, cudaStream_t s) {
+  if (m != 128) return cudaErrorNotSupported;
+  if (ncols <= 0 || nleaf <= 0) return cudaSuccess;
+  auto k = leaf_apply128_f32_kernel<double>;
+  cudaError_t e = set_smem(k, kLa128Smem);
+  if (e != cudaSuccess) return e;
+  HODLR_LAUNCH(k, dim3(ceil_div(ncols, kLa128CT), nleaf), kLa128Threads, kLa128Smem, s, Dinv, Xs, lds, X, ldx, ncols,
+               (const int *)nullptr);
+  return cudaGetLastError();
+}
 
 template <typename T>
 cudaError_t launch_leaf_apply(const T *Dinv, int m, int nleaf, T *X, long long ldx, int ncols, bool trans,

@@ -443,12 +443,19 @@ template <typename T> static int factor_sweep(hodlr_ctx *h) {
         launch_leaf_getrf<T>(h->D, m, (long long)m * m, LU, h->ipiv, m, h->nleaf, h->dst, fused ? Dinv : nullptr, s));
   if (Dinv && !fused) PHASE(h, HODLR_PHASE_LEAF_LU, launch_leaf_inverse<T>(LU, h->ipiv, m, h->nleaf, Dinv, s));
   if (L == 0) return HODLR_OK;
-  if (sizeof(T) == 8)
-    CK(cudaMemcpyAsync(Ut, h->U, sizeof(double) * n * L * r, cudaMemcpyDeviceToDevice, s));
-  else
-    PHASE(h, HODLR_PHASE_MISC,
-          (launch_convert<double, float>(h->U, n, reinterpret_cast<float *>(Ut), n, n, L * r, s)));
-  CKS(leaf_solve<T>(h, Ut, n, L * r, false, nullptr));
+  if (sizeof(T) == 4 && Dinv && m == 128) {
+    // Utilde = D^{-1} U straight from the FP64 U (rounded as it is staged)
+    PHASE(h, HODLR_PHASE_LEAF_SOLVE,
+          launch_leaf_apply_f64src(reinterpret_cast<const float *>(Dinv), m, h->nleaf, h->U, n,
+                                   reinterpret_cast<float *>(Ut), n, L * r, s));
+  } else {
+    if (sizeof(T) == 8)
+      CK(cudaMemcpyAsync(Ut, h->U, sizeof(double) * n * L * r, cudaMemcpyDeviceToDevice, s));
+    else
+      PHASE(h, HODLR_PHASE_MISC,
+            (launch_convert<double, float>(h->U, n, reinterpret_cast<float *>(Ut), n, n, L * r, s)));
+    CKS(leaf_solve<T>(h, Ut, n, L * r, false, nullptr));
+  }
   for (int l = L - 1; l >= 0; --l) {
     const int nb = h->nb(l);
     const long long rows = h->rows(l);

@@ -84,6 +84,11 @@ bool leaf_apply_supported(int m);
 template <typename T>
 cudaError_t launch_leaf_apply(const T *Dinv, int m, int nleaf, T *X, long long ldx, int ncols, bool trans,
                               const int *skip, cudaStream_t s);
+// X := Dinv X for leaf size 128 with the source read from Xs (FP64, leading
+// dimension lds) and rounded to FP32 as it is staged (the factorisation's
+// U -> Utilde); cudaErrorNotSupported for other leaf sizes.
+cudaError_t launch_leaf_apply_f64src(const float *Dinv, int m, int nleaf, const double *Xs, long long lds, float *X,
+                                     long long ldx, int ncols, cudaStream_t s);
 
 // Capacitance factorisation of the nodes of one depth: S from the T blocks'
 // columns [ucol, ucol + r), FP64 LU (stored in cap_lu / cap_ipiv) and the FP64
