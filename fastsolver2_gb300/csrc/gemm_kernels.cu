@@ -184,7 +184,7 @@ __device__ __forceinline__ void reduce_tma_issue(unsigned char *base, uint64_t *
 }
 
 template <int RT, typename OutT>
-__global__ void __launch_bounds__(256, RT <= 32 ? 3 : 1)
+__global__ void __launch_bounds__(256, RT <= 16 ? 3 : (RT <= 32 ? 2 : 1))
 reduce_tma_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapX,
                   long long nrows, int r, int C, int chunk_rows, int nchunks, int nct, OutT *out,
                   const int *skip, DevStatus *st) {
@@ -216,11 +216,13 @@ reduce_tma_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constan
   if (tid == 0)
     for (int s = 0; s < min(kTmaStages, nst); ++s)
       reduce_tma_issue<A_BYTES, STAGE>(base, bars, &mapA, &mapX, s, row0i, c0);
-  float acc[RPT][CPT];
+  // packed pair accumulators: .x sums the even rows of the chunk, .y the odd
+  // ones (a float4 run holds both), so one packed FMA does two products
+  float2 acc[RPT][CPT];
 #pragma unroll
   for (int a = 0; a < RPT; ++a)
 #pragma unroll
-    for (int c = 0; c < CPT; ++c) acc[a][c] = 0.f;
+    for (int c = 0; c < CPT; ++c) acc[a][c] = make_float2(0.f, 0.f);
   for (int s = 0; s < nst; ++s) {
     const int slot = s % kTmaStages;
     const bool ok = mbar_wait_bounded(&bars[slot], (unsigned)((s / kTmaStages) & 1));
@@ -246,11 +248,9 @@ reduce_tma_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constan
         const float4 xv = *reinterpret_cast<const float4 *>(sx + swz128(tc + 8 * c, kc));
 #pragma unroll
         for (int a = 0; a < RPT; ++a) {
-          float v = acc[a][c];
-          v = fmaf(av[a].x, xv.x, v);
-          v = fmaf(av[a].y, xv.y, v);
-          v = fmaf(av[a].z, xv.z, v);
-          v = fmaf(av[a].w, xv.w, v);
+          float2 v = acc[a][c];
+          v = __ffma2_rn(make_float2(av[a].x, av[a].y), make_float2(xv.x, xv.y), v);
+          v = __ffma2_rn(make_float2(av[a].z, av[a].w), make_float2(xv.z, xv.w), v);
           acc[a][c] = v;
         }
       }
@@ -261,7 +261,7 @@ reduce_tma_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constan
 #pragma unroll
   for (int a = 0; a < RPT; ++a)
 #pragma unroll
-    for (int c = 0; c < CPT; ++c) sRed[(g * RT + tr + 8 * a) * (BN + 1) + tc + 8 * c] = acc[a][c];
+    for (int c = 0; c < CPT; ++c) sRed[(g * RT + tr + 8 * a) * (BN + 1) + tc + 8 * c] = acc[a][c].x + acc[a][c].y;
   __syncthreads();
   OutT *o = out + ((long long)b * nchunks + chunk) * r * C;
   for (int e = tid; e < RT * BN; e += 256) {
