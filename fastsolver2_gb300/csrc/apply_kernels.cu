@@ -165,11 +165,13 @@ leaf_apply128_f32_kernel(const float *__restrict__ Dinv, const S *Xs, long long 
     const int i = e % M, j = e / M;
     sXt[i * LD + j] = j < nc ? (float)Xsg[i + (long long)j * lds] : 0.f;
   }
-  float acc[8][8];
+  // column pairs (8 tj + 2 p, + 1) in packed FP32x2 accumulators: one packed
+  // FMA does the two products of a row with an adjacent column pair
+  float2 acc[8][4];
 #pragma unroll
   for (int a = 0; a < 8; ++a)
 #pragma unroll
-    for (int b = 0; b < 8; ++b) acc[a][b] = 0.f;
+    for (int p = 0; p < 4; ++p) acc[a][p] = make_float2(0.f, 0.f);
   for (int k0 = 0; k0 < M; k0 += KC) {
     __syncthreads();
     for (int e = tid; e < M * KC / 4; e += NT) {  // the slab, 16-byte copies
@@ -184,11 +186,12 @@ leaf_apply128_f32_kernel(const float *__restrict__ Dinv, const S *Xs, long long 
       const float4 x0 = *reinterpret_cast<const float4 *>(sXt + (k0 + q) * LD + 8 * tj);
       const float4 x1 = *reinterpret_cast<const float4 *>(sXt + (k0 + q) * LD + 8 * tj + 4);
       const float av[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
-      const float xb[8] = {x0.x, x0.y, x0.z, x0.w, x1.x, x1.y, x1.z, x1.w};
+      const float2 xp[4] = {make_float2(x0.x, x0.y), make_float2(x0.z, x0.w), make_float2(x1.x, x1.y),
+                            make_float2(x1.z, x1.w)};
 #pragma unroll
       for (int a = 0; a < 8; ++a)
 #pragma unroll
-        for (int b = 0; b < 8; ++b) acc[a][b] = fmaf(av[a], xb[b], acc[a][b]);
+        for (int p = 0; p < 4; ++p) acc[a][p] = __ffma2_rn(make_float2(av[a], av[a]), xp[p], acc[a][p]);
     }
   }
   __syncthreads();  // every thread is done with sXt: it takes the result, column-major ld M
@@ -196,8 +199,11 @@ leaf_apply128_f32_kernel(const float *__restrict__ Dinv, const S *Xs, long long 
 #pragma unroll
   for (int b = 0; b < 8; ++b) {
     float *col = sY + (8 * tj + b) * M;
-    *reinterpret_cast<float4 *>(col + 4 * ti) = make_float4(acc[0][b], acc[1][b], acc[2][b], acc[3][b]);
-    *reinterpret_cast<float4 *>(col + 64 + 4 * ti) = make_float4(acc[4][b], acc[5][b], acc[6][b], acc[7][b]);
+    float y[8];
+#pragma unroll
+    for (int a = 0; a < 8; ++a) y[a] = (b & 1) ? acc[a][b >> 1].y : acc[a][b >> 1].x;
+    *reinterpret_cast<float4 *>(col + 4 * ti) = make_float4(y[0], y[1], y[2], y[3]);
+    *reinterpret_cast<float4 *>(col + 64 + 4 * ti) = make_float4(y[4], y[5], y[6], y[7]);
   }
   __syncthreads();
   for (int e = tid; e < M * CT; e += NT) {
