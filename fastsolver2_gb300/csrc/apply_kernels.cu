@@ -161,9 +161,14 @@ leaf_apply128_f32_kernel(const float *__restrict__ Dinv, const S *Xs, long long 
   float *Xg = X + (long long)leaf * M + (long long)c0 * ldx;
   const S *Xsg = Xs + (long long)leaf * M + (long long)c0 * lds;
   const int tid = threadIdx.x, ti = tid & 15, tj = tid >> 4;
-  for (int e = tid; e < M * CT; e += NT) {  // coalesced along the rows of X
-    const int i = e % M, j = e / M;
-    sXt[i * LD + j] = j < nc ? (float)Xsg[i + (long long)j * lds] : 0.f;
+  // coalesced along the rows of X; four columns per thread land as one
+  // 16-byte store (rows 68 floats apart: a quarter warp covers all banks)
+  for (int e = tid; e < M * CT / 4; e += NT) {
+    const int i = e % M, j = 4 * (e / M);
+    float v[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) v[u] = j + u < nc ? (float)Xsg[i + (long long)(j + u) * lds] : 0.f;
+    *reinterpret_cast<float4 *>(sXt + i * LD + j) = make_float4(v[0], v[1], v[2], v[3]);
   }
   // column pairs (8 tj + 2 p, + 1) in packed FP32x2 accumulators: one packed
   // FMA does the two products of a row with an adjacent column pair

@@ -12,8 +12,10 @@
 #define HODLR_GB300_HPP
 
 #include <cstdint>
+#include <cstring>
 #include <stdexcept>
 #include <string>
+#include <vector>
 
 #include "hodlr_gb300.h"
 
@@ -55,6 +57,34 @@ class HMatrix {
     create(N, rank, nrhs_max, precision);
     check(hodlr_set_uvd(h_, U, N, V, N, D));
     factored_ = false;
+  }
+
+  // HMatrix::init from the per-leaf seeds of the reference's MapSeed
+  // argument maps (src/lmatrix.cc:327-360): U, V, D and the leaf blocks
+  // built on the device bit for bit as the reference's tasks build them.
+  void init_seeded(const int64_t *useeds, const int64_t *vseeds, const int64_t *dseeds, int64_t N, int rank,
+                   double offset, int nrhs_max = 1, int precision = HODLR_PREC_FP64) {
+    create(N, rank, nrhs_max, precision);
+    check(hodlr_set_seeded(h_, useeds, vseeds, dseeds, offset));
+    factored_ = false;
+  }
+
+  // The factored state as bytes, and a factored HMatrix from them.
+  std::vector<char> checkpoint() {
+    if (!factored_) factor();
+    int64_t nb = 0;
+    check(hodlr_checkpoint_size(h_, &nb));
+    std::vector<char> buf((size_t)nb);
+    check(hodlr_checkpoint_save(h_, buf.data(), nb));
+    return buf;
+  }
+  void restore(const std::vector<char> &buf, void *stream = nullptr) {
+    destroy();
+    check(hodlr_checkpoint_load(buf.data(), (int64_t)buf.size(), stream, &h_));
+    int64_t n = 0;
+    std::memcpy(&n, buf.data() + 16, sizeof n);  // the header's N (after magic and two 32-bit fields)
+    n_ = n;
+    factored_ = true;
   }
 
   // General form: leaf blocks in the KTree layout (ld, leaf_stride) and

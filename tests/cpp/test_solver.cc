@@ -3,8 +3,10 @@
 // seed per leaf partition, D + 1e3, one U and V for all levels), then
 // HMatrix(nProc, level).init(U, V, D) and solve(b), and the residual
 // ||b - (U (V^T x) + D.x)|| / ||b|| that the reference leaves disabled
-// (tests/test.cc:651-658).  Prints one JSON line; with a third argument it
-// writes x (raw float64) to that file.
+// (tests/test.cc:651-658); then the same problem built on the device from
+// its seeds (HMatrix::init_seeded) and a checkpoint round trip of that
+// factorisation.  Prints one JSON line; with a fourth argument it writes x
+// (raw float64) to that file.
 //   usage: test_solver <leaf> <levels> <rank> [x.bin]
 #include <cuda_runtime.h>
 #include <stdlib.h>
@@ -72,8 +74,31 @@ int main(int argc, char **argv) {
       bn += b[i] * b[i];
       xs += x[i];
     }
-    printf("{\"n\": %lld, \"leaf\": %d, \"levels\": %d, \"rank\": %d, \"rel_residual\": %.6e, \"x_sum\": %.17g}\n", N,
-           leaf, level, rank, std::sqrt(rn / bn), xs);
+    // the same problem from its seeds on the device (HMatrix::init_seeded),
+    // then a checkpoint of that factorisation restored into a third HMatrix
+    auto to64 = [](const std::vector<long> &v) { return std::vector<int64_t>(v.begin(), v.end()); };
+    const auto vs = to64(seeds(master + 0, nPart)), us = to64(seeds(master + 1, nPart)),
+               ds = to64(seeds(master + 3, nPart));
+    hodlr_gb300::HMatrix H2(/*nProc=*/1, level), H3(/*nProc=*/1, level);
+    H2.init_seeded(us.data(), vs.data(), ds.data(), N, rank, 1000.0);
+    std::vector<double> x2(N), x3(N);
+    cudaMemcpy(dB, b.data(), sizeof(double) * N, cudaMemcpyHostToDevice);
+    H2.solve(dB, N, 1);
+    cudaMemcpy(x2.data(), dB, sizeof(double) * N, cudaMemcpyDeviceToHost);
+    H3.restore(H2.checkpoint());
+    cudaMemcpy(dB, b.data(), sizeof(double) * N, cudaMemcpyHostToDevice);
+    H3.solve(dB, N, 1);
+    cudaMemcpy(x3.data(), dB, sizeof(double) * N, cudaMemcpyDeviceToHost);
+    double dn = 0, xn = 0;
+    bool same = true;
+    for (long long i = 0; i < N; ++i) {
+      dn += (x2[i] - x[i]) * (x2[i] - x[i]);
+      xn += x[i] * x[i];
+      same = same && x3[i] == x2[i];
+    }
+    printf("{\"n\": %lld, \"leaf\": %d, \"levels\": %d, \"rank\": %d, \"rel_residual\": %.6e, \"x_sum\": %.17g, "
+           "\"seeded_rel_diff\": %.6e, \"checkpoint_identical\": %s}\n",
+           N, leaf, level, rank, std::sqrt(rn / bn), xs, std::sqrt(dn / xn), same ? "true" : "false");
     if (argc > 4) {
       FILE *f = fopen(argv[4], "wb");
       if (!f || fwrite(x.data(), sizeof(double), N, f) != (size_t)N) return 3;

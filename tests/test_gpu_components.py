@@ -129,6 +129,8 @@ def test_cpp_hmatrix_driver(hodlr, tmp_path, leaf, levels, rank):
     assert out.returncode == 0, out.stderr
     rep = json.loads(out.stdout.strip().splitlines()[-1])
     assert rep["rel_residual"] < 1e-12
+    assert rep["seeded_rel_diff"] < 1e-12
+    assert rep["checkpoint_identical"] is True
     x = np.fromfile(xfile, dtype=np.float64)
     pr = P.reference_problem(leaf, levels, rank, nrhs=1)
     Xo, _, _ = O.hsolve_general(pr, pr.B)
