@@ -107,11 +107,77 @@ __global__ void oz_slice_cols_kernel(const double *X, long long ldx, long long n
   oz_digits(v1, E, [&](int s, __nv_bfloat16 d) { o[s * sstride + i1] = d; });
 }
 
+// The same slicing with 16-byte accesses: 8 lanes per (64-row chunk,
+// column), 8 consecutive rows per lane -- four 16-byte loads of X, two of the
+// correction, four 16-byte stores of the updated iterate and one per digit
+// slice (8 digits), instead of 2-byte digit stores.  Needs 16-byte aligned
+// rows (checked by the launcher).
+__global__ void oz_slice_cols8_kernel(const double *X, long long ldx, long long nchunk, int c, __nv_bfloat16 *out,
+                                      long long ld_out, long long sstride, int *exps, const int *skip,
+                                      const float *add, double *xout) {
+  static_assert(kOzChunk == 64, "8 lanes x 8 rows per exponent group");
+  if (skip && *skip) return;
+  const long long g = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 3;
+  const int lane = threadIdx.x & 31, sub = lane & 7;
+  if (g >= nchunk * c) return;  // whole 8-lane groups leave together
+  const unsigned gmask = 0xffu << (lane & 24);
+  const long long ch = g / c;
+  const int j = (int)(g % c);
+  const long long i0 = ch * kOzChunk + 8 * sub;
+  double v[8];
+  if (X) {
+    const double2 *xp = reinterpret_cast<const double2 *>(X + i0 + j * ldx);
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const double2 t = xp[u];
+      v[2 * u] = t.x;
+      v[2 * u + 1] = t.y;
+    }
+  } else {
+#pragma unroll
+    for (int u = 0; u < 8; ++u) v[u] = 0.0;
+  }
+  if (add) {
+    const float4 *ap = reinterpret_cast<const float4 *>(add + i0 + j * ldx);
+    const float4 a0 = ap[0], a1 = ap[1];
+    const float av[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
+#pragma unroll
+    for (int u = 0; u < 8; ++u) v[u] += (double)av[u];
+  }
+  if (xout) {
+    double2 *op = reinterpret_cast<double2 *>(xout + i0 + j * ldx);
+#pragma unroll
+    for (int u = 0; u < 4; ++u) op[u] = make_double2(v[2 * u], v[2 * u + 1]);
+  }
+  unsigned long long mb = 0;
+#pragma unroll
+  for (int u = 0; u < 8; ++u) mb = max(mb, abs_bits(v[u]));
+#pragma unroll
+  for (int o = 4; o; o >>= 1) mb = max(mb, __shfl_xor_sync(gmask, mb, o));
+  const int E = oz_exponent_bits(mb);
+  if (sub == 0) exps[ch * c + j] = E;
+  __align__(16) __nv_bfloat16 d[kOzSlices][8];
+#pragma unroll
+  for (int u = 0; u < 8; ++u) oz_digits(v[u], E, [&](int sl, __nv_bfloat16 x) { d[sl][u] = x; });
+  __nv_bfloat16 *o = out + j * ld_out + i0;
+#pragma unroll
+  for (int sl = 0; sl < kOzSlices; ++sl)
+    *reinterpret_cast<uint4 *>(o + sl * sstride) = *reinterpret_cast<const uint4 *>(d[sl]);
+}
+
 cudaError_t launch_oz_slice_cols(const double *X, long long ldx, long long n, int c, __nv_bfloat16 *out,
                                  long long ld_out, long long slice_stride, int *exps, const int *skip,
                                  cudaStream_t s, const float *add, double *xout) {
   if (n <= 0 || c <= 0) return cudaSuccess;
   if (n % kOzChunk) return cudaErrorInvalidValue;
+  const bool a16 = ((uintptr_t)X & 15) == 0 && ((uintptr_t)add & 15) == 0 && ((uintptr_t)xout & 15) == 0 &&
+                   ((uintptr_t)out & 15) == 0 && ldx % 4 == 0 && ld_out % 8 == 0 && slice_stride % 8 == 0;
+  if (a16) {
+    const long long groups = (n / kOzChunk) * c;
+    HODLR_LAUNCH(oz_slice_cols8_kernel, ceil_div(groups * 8, 256), 256, 0, s, X, ldx, n / kOzChunk, c, out,
+                 ld_out, slice_stride, exps, skip, add, xout);
+    return cudaGetLastError();
+  }
   const long long warps = (n / kOzChunk) * c;
   HODLR_LAUNCH(oz_slice_cols_kernel, ceil_div(warps * 32, 256), 256, 0, s, X, ldx, n / kOzChunk, c, out, ld_out,
                slice_stride, exps, skip, add, xout);
