@@ -257,6 +257,62 @@ __global__ void oz_slice_tprime_all_kernel(const double *T, int r, int k, __nv_b
   }
 }
 
+// The same with G = r / 8 lanes per (block, column), 8 consecutive ranks per
+// lane: 16-byte loads of T (and of the scales) and one 16-byte store per
+// digit slice (r a multiple of 8 up to 64; G = 4 or 8).
+template <int G>
+__global__ void oz_slice_tprime_all8_kernel(const double *T, int r, int k, __nv_bfloat16 *out, int *exps,
+                                            TprimeLevels a, const int *skip) {
+  if (skip && *skip) return;
+  const long long w = ((long long)blockIdx.x * blockDim.x + threadIdx.x) / G;
+  const int lane = threadIdx.x & 31, sub = lane % G;
+  if (w >= a.wpre[a.L]) return;  // whole groups leave together
+  const unsigned gmask = (G == 8 ? 0xffu : 0xfu) << (lane & ~(G - 1));
+  int l = 0;
+  while (w >= a.wpre[l + 1]) ++l;
+  const long long wl = w - a.wpre[l];
+  const int b = (int)(wl / k), j = (int)(wl % k);
+  const int q0 = 8 * sub;
+  const double *src = T + a.toff[l] + (long long)(b ^ 1) * r * k + (long long)j * r + q0;
+  const double *scale = a.scale[l];
+  double v[8];
+  if (q0 < r) {
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const double2 t = reinterpret_cast<const double2 *>(src)[u];
+      v[2 * u] = t.x;
+      v[2 * u + 1] = t.y;
+    }
+    if (scale) {
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const double2 sc = reinterpret_cast<const double2 *>(scale + q0)[u];
+        v[2 * u] *= sc.x;
+        v[2 * u + 1] *= sc.y;
+      }
+    }
+  } else {
+#pragma unroll
+    for (int u = 0; u < 8; ++u) v[u] = 0.0;
+  }
+  unsigned long long mb = 0;
+#pragma unroll
+  for (int u = 0; u < 8; ++u) mb = max(mb, abs_bits(v[u]));
+#pragma unroll
+  for (int o = G / 2; o; o >>= 1) mb = max(mb, __shfl_xor_sync(gmask, mb, o));
+  const int E = oz_exponent_bits(mb);
+  if (sub == 0) exps[a.eoff[l] + (long long)b * k + j] = E;
+  if (q0 >= r) return;
+  __align__(16) __nv_bfloat16 d[kOzSlices][8];
+#pragma unroll
+  for (int u = 0; u < 8; ++u) oz_digits(v[u], E, [&](int sl, __nv_bfloat16 x) { d[sl][u] = x; });
+  __nv_bfloat16 *o = out + a.ooff[l];
+#pragma unroll
+  for (int sl = 0; sl < kOzSlices; ++sl)
+    *reinterpret_cast<uint4 *>(o + (((long long)b * kOzSlices + sl) * k + j) * r + q0) =
+        *reinterpret_cast<const uint4 *>(d[sl]);
+}
+
 cudaError_t launch_oz_slice_tprime_all(const double *T, int r, int k, int L, const int *lev_nb,
                                        const double *const *scale, __nv_bfloat16 *out, int *exps, const int *skip,
                                        cudaStream_t s) {
@@ -277,7 +333,18 @@ cudaError_t launch_oz_slice_tprime_all(const double *T, int r, int k, int L, con
     e += (long long)lev_nb[l] * k;
   }
   a.wpre[L] = w;
-  HODLR_LAUNCH(oz_slice_tprime_all_kernel, (unsigned)ceil_div(w * 32, 256), 256, 0, s, T, r, k, out, exps, a, skip);
+  bool a16 = r % 8 == 0 && ((uintptr_t)T & 15) == 0 && ((uintptr_t)out & 15) == 0;
+  for (int l = 0; l < L && a16; ++l) a16 = ((uintptr_t)scale[l] & 15) == 0;
+  if (a16 && r <= 32) {
+    HODLR_LAUNCH(oz_slice_tprime_all8_kernel<4>, (unsigned)ceil_div(w * 4, 256), 256, 0, s, T, r, k, out, exps, a,
+                 skip);
+  } else if (a16) {
+    HODLR_LAUNCH(oz_slice_tprime_all8_kernel<8>, (unsigned)ceil_div(w * 8, 256), 256, 0, s, T, r, k, out, exps, a,
+                 skip);
+  } else {
+    HODLR_LAUNCH(oz_slice_tprime_all_kernel, (unsigned)ceil_div(w * 32, 256), 256, 0, s, T, r, k, out, exps, a,
+                 skip);
+  }
   return cudaGetLastError();
 }
 
