@@ -405,7 +405,7 @@ __device__ __forceinline__ V row_entry(const V (&v)[RS], int p) {
 }
 
 template <int M>
-__global__ void __launch_bounds__(256, 2) cap_factor_cols_kernel(CapFactorArgs a) {
+__global__ void __launch_bounds__(256, 3) cap_factor_cols_kernel(CapFactorArgs a) {
   constexpr int RS = M / 32, CW = M / 8;
   __shared__ double s_l[2][M];   // multipliers by physical row
   __shared__ float s_l32[2][M];
