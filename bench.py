@@ -633,9 +633,9 @@ def run_ragged(args, fs, torch, stream, colmajor):
 OZ_PAIRS = 28   # digit pairs (s + t <= 6 of 7 x 7) per FP64 product in the tensor-core residual
 # ncu DRAM bytes (read + write) per launch, averaged over the launches of one
 # mixed step at N=2^20 (profiles/dram_traffic_mixed_n2e20_leaf128_r32_k64.md)
-TRAFFIC = {"update_tc_kernel": 38.768e9 / 155, "update_tma_kernel": 38.804e9 / 155,
-           "reduce_tma_kernel": 25.605e9 / 156,
-           "oz_tc_kernel<0>": 21.139e9 / 11, "oz_tc_kernel<1>": (20.175e9 + 0.134e9) / 11}
+TRAFFIC = {"update_tc_kernel": 38.775e9 / 155, "update_tma_kernel": 38.804e9 / 155,
+           "reduce_tma_kernel": 25.553e9 / 156,
+           "oz_tc_kernel<0>": 21.130e9 / 11, "oz_tc_kernel<1>": (20.116e9 + 0.134e9) / 11}
 
 
 def _measured_peak(key):
