@@ -93,6 +93,9 @@ SIGNATURES = {
     "hodlr_adjoint": (_I, [_VP, _VP, _I64, _VP, _I64, _I, ctypes.POINTER(Grads)]),
     "hodlr_get_factors": (_I, [_VP, _VP, _VP, _VP, _VP, _VP]),
     "hodlr_get_inputs": (_I, [_VP, _VP, _I64, _I64, _VP, _VP, _VP]),
+    "hodlr_pad_rows": (_I, [_I, _VP, _I, _I, _VP, _I64, _VP, _I64, _VP]),
+    "hodlr_unpad_rows": (_I, [_I, _VP, _I, _I, _VP, _I64, _VP, _I64, _VP]),
+    "hodlr_pad_leaf_blocks": (_I, [_I, _VP, _I, _VP, _VP, _VP]),
     "hodlr_draw_seeds": (_I, [_I64, _I, _VP]),
     "hodlr_rand_matrix": (_I, [_VP, _I, _I64, _I, _D, _VP, _I64, _VP]),
     "hodlr_set_seeded": (_I, [_VP, _VP, _VP, _VP, _D]),
@@ -386,6 +389,31 @@ def hsolve(nrow, nrhs, rank, nPart, LD, K, U, V, precision=PREC_FP64, stream=Non
 def _seed_array(seeds):
     seeds = [int(x) for x in seeds]
     return (ctypes.c_int64 * max(1, len(seeds)))(*seeds)
+
+
+def _sizes(sz):
+    sz = [int(x) for x in sz]
+    return (ctypes.c_int32 * max(1, len(sz)))(*sz), len(sz)
+
+
+def pad_rows(sizes, m_max, src, dst, stream=None):
+    """Rows of leaf i of src (packed, CUDA float64 column-major) to rows i*m_max.. of dst, zero padding."""
+    a, n = _sizes(sizes)
+    cols = src.shape[1] if src.dim() == 2 else 1
+    check(lib().hodlr_pad_rows(n, a, int(m_max), cols, _ptr(src), _ld(src), _ptr(dst), _ld(dst), stream))
+
+
+def unpad_rows(sizes, m_max, src, dst, stream=None):
+    """The inverse of pad_rows: padded src to packed dst."""
+    a, n = _sizes(sizes)
+    cols = src.shape[1] if src.dim() == 2 else 1
+    check(lib().hodlr_unpad_rows(n, a, int(m_max), cols, _ptr(src), _ld(src), _ptr(dst), _ld(dst), stream))
+
+
+def pad_leaf_blocks(sizes, m_max, src, dst, stream=None):
+    """Leaf blocks packed one after another (sz_i x sz_i, column-major) to [nleaf][m_max][m_max]."""
+    a, n = _sizes(sizes)
+    check(lib().hodlr_pad_leaf_blocks(n, a, int(m_max), _ptr(src), _ptr(dst), stream))
 
 
 def draw_seeds(master, n):

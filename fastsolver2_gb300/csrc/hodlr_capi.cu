@@ -1507,6 +1507,86 @@ int hodlr_hsolve(int nrow, int nrhs, int rank, int nPart, int LD, double *K, dou
 }
 
 // ------------------------------------------------- reference-structured init
+// Device copies of the leaf sizes and their prefix offsets (rows, or block
+// elements with squares) for the padding kernels.
+static int irregular_tables(int nleaf, const int32_t *sz, int m_max, bool squares, int **dsz, long long **doff,
+                            long long *total, cudaStream_t s) {
+  if (nleaf < 1 || !sz || m_max < 1) return set_err(HODLR_ERR_INVALID_ARG, "bad leaf sizes");
+  std::vector<int> h_sz(nleaf);
+  std::vector<long long> h_off(nleaf);
+  long long acc = 0;
+  for (int i = 0; i < nleaf; ++i) {
+    if (sz[i] < 1 || sz[i] > m_max) return set_err(HODLR_ERR_INVALID_ARG, "leaf size outside [1, m_max]");
+    h_sz[i] = sz[i];
+    h_off[i] = acc;
+    acc += squares ? (long long)sz[i] * sz[i] : sz[i];
+  }
+  *total = acc;
+  *dsz = nullptr;
+  *doff = nullptr;
+  CK(cudaMallocAsync((void **)dsz, sizeof(int) * nleaf, s));
+  CK(cudaMallocAsync((void **)doff, sizeof(long long) * nleaf, s));
+  CK(cudaMemcpyAsync(*dsz, h_sz.data(), sizeof(int) * nleaf, cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(*doff, h_off.data(), sizeof(long long) * nleaf, cudaMemcpyHostToDevice, s));
+  CK(cudaStreamSynchronize(s));  // the host vectors go out of scope
+  return HODLR_OK;
+}
+
+static int pad_rows_impl(int nleaf, const int32_t *sz, int m_max, int cols, const double *src, int64_t lds,
+                         double *dst, int64_t ldd, void *stream, bool unpad) {
+  if (!src || !dst || cols < 0) return set_err(HODLR_ERR_INVALID_ARG, "bad argument");
+  cudaStream_t s = (cudaStream_t)stream;
+  int *dsz = nullptr;
+  long long *doff = nullptr, packed = 0;
+  const int rc = irregular_tables(nleaf, sz, m_max, false, &dsz, &doff, &packed, s);
+  if (rc != HODLR_OK) {
+    if (dsz) cudaFreeAsync(dsz, s);
+    if (doff) cudaFreeAsync(doff, s);
+    return rc;
+  }
+  const long long padded = (long long)nleaf * m_max;
+  cudaError_t e = cudaSuccess;
+  if ((unpad ? lds < padded || ldd < packed : lds < packed || ldd < padded))
+    e = cudaErrorInvalidValue;
+  else
+    e = launch_pad_rows(doff, dsz, nleaf, m_max, cols, src, lds, dst, ldd, unpad, s);
+  cudaFreeAsync(dsz, s);
+  cudaFreeAsync(doff, s);
+  if (e == cudaErrorInvalidValue) return set_err(HODLR_ERR_INVALID_ARG, "leading dimension too small");
+  CK(e);
+  CK(cudaStreamSynchronize(s));
+  return HODLR_OK;
+}
+
+int hodlr_pad_rows(int nleaf, const int32_t *sz, int m_max, int cols, const double *src, int64_t lds, double *dst,
+                   int64_t ldd, void *stream) {
+  return pad_rows_impl(nleaf, sz, m_max, cols, src, lds, dst, ldd, stream, false);
+}
+
+int hodlr_unpad_rows(int nleaf, const int32_t *sz, int m_max, int cols, const double *src, int64_t lds, double *dst,
+                     int64_t ldd, void *stream) {
+  return pad_rows_impl(nleaf, sz, m_max, cols, src, lds, dst, ldd, stream, true);
+}
+
+int hodlr_pad_leaf_blocks(int nleaf, const int32_t *sz, int m_max, const double *src, double *dst, void *stream) {
+  if (!src || !dst) return set_err(HODLR_ERR_INVALID_ARG, "null argument");
+  cudaStream_t s = (cudaStream_t)stream;
+  int *dsz = nullptr;
+  long long *doff = nullptr, total = 0;
+  const int rc = irregular_tables(nleaf, sz, m_max, true, &dsz, &doff, &total, s);
+  if (rc != HODLR_OK) {
+    if (dsz) cudaFreeAsync(dsz, s);
+    if (doff) cudaFreeAsync(doff, s);
+    return rc;
+  }
+  const cudaError_t e = launch_pad_leaf_blocks(doff, dsz, nleaf, m_max, src, dst, s);
+  cudaFreeAsync(dsz, s);
+  cudaFreeAsync(doff, s);
+  CK(e);
+  CK(cudaStreamSynchronize(s));
+  return HODLR_OK;
+}
+
 int hodlr_draw_seeds(int64_t master, int n, int64_t *seeds) {
   if (n < 0 || (n > 0 && !seeds)) return set_err(HODLR_ERR_INVALID_ARG, "bad seed count or null output");
   unsigned long long x = lcg_seed(master);

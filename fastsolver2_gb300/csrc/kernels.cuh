@@ -203,6 +203,15 @@ cudaError_t launch_gaussian(double *X, long long ld, long long n, int c, unsigne
 // Leaf blocks [nleaf][m][m] = G/sqrt(m) + shift*I.
 cudaError_t launch_gen_leaves(double *D, int m, int nleaf, unsigned long long seed, double shift,
                               cudaStream_t s);
+// Unequal leaf sizes embedded in the uniform tree: rows of leaf i (packed at
+// off[i], sz[i] rows) to rows i*mp.. of the padded matrix (zero padding), or
+// back (unpad); leaf blocks packed one after another (block i at boff[i],
+// sz[i] x sz[i]) into [nleaf][mp][mp] with an identity on the padding.
+// off, sz, boff are device arrays.
+cudaError_t launch_pad_rows(const long long *off, const int *sz, int nleaf, int mp, int cols, const double *src,
+                            long long lds, double *dst, long long ldd, bool unpad, cudaStream_t s);
+cudaError_t launch_pad_leaf_blocks(const long long *boff, const int *sz, int nleaf, int mp, const double *src,
+                                   double *dst, cudaStream_t s);
 // The reference's drand48 generator (POSIX 48-bit LCG): srand48 seeding,
 // one step, and the state after t steps (the affine map powered by squaring;
 // the maps x -> a^k x + c_k commute, so the order of composition is free).

@@ -434,4 +434,54 @@ cudaError_t launch_scale_grad(const double *W, const double *T, int r, int k, in
   return cudaGetLastError();
 }
 
+// ------------------------------------------------- unequal leaf sizes
+// Rows of leaf i (rows off[i] .. off[i] + sz[i] of a packed matrix) to or
+// from rows i * mp .. of the padded one; padded rows are zero.
+__global__ void pad_rows_kernel(const long long *off, const int *sz, int nleaf, int mp, int cols, const double *src,
+                                long long lds, double *dst, long long ldd, int unpad) {
+  const long long total = (long long)nleaf * mp;
+  for (long long j = blockIdx.y; j < cols; j += gridDim.y)
+    for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < total;
+         e += (long long)gridDim.x * blockDim.x) {
+      const int i = (int)(e / mp), q = (int)(e % mp);
+      const bool real = q < sz[i];
+      const long long pr = e, rr = off[i] + q;  // padded row, packed row
+      if (!unpad)
+        dst[pr + j * ldd] = real ? src[rr + j * lds] : 0.0;
+      else if (real)
+        dst[rr + j * ldd] = src[pr + j * lds];
+    }
+}
+
+cudaError_t launch_pad_rows(const long long *off, const int *sz, int nleaf, int mp, int cols, const double *src,
+                            long long lds, double *dst, long long ldd, bool unpad, cudaStream_t s) {
+  const long long total = (long long)nleaf * mp;
+  if (total == 0 || cols == 0) return cudaSuccess;
+  dim3 grid((unsigned)std::min<long long>(ceil_div(total, 256), 152 * 8), (unsigned)std::min(cols, 65535));
+  HODLR_LAUNCH(pad_rows_kernel, grid, 256, 0, s, off, sz, nleaf, mp, cols, src, lds, dst, ldd, unpad ? 1 : 0);
+  return cudaGetLastError();
+}
+
+// Leaf blocks packed one after another (block i: sz[i] x sz[i], column-major,
+// starting at boff[i]) into [nleaf][mp][mp] with an identity on the padding.
+__global__ void pad_leaf_blocks_kernel(const long long *boff, const int *sz, int nleaf, int mp, const double *src,
+                                       double *dst) {
+  const long long mm = (long long)mp * mp, total = (long long)nleaf * mm;
+  for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < total;
+       e += (long long)gridDim.x * blockDim.x) {
+    const int i = (int)(e / mm);
+    const int w = (int)(e % mm), r = w % mp, c = w / mp, m = sz[i];
+    dst[e] = (r < m && c < m) ? src[boff[i] + r + (long long)c * m] : (r == c ? 1.0 : 0.0);
+  }
+}
+
+cudaError_t launch_pad_leaf_blocks(const long long *boff, const int *sz, int nleaf, int mp, const double *src,
+                                   double *dst, cudaStream_t s) {
+  const long long total = (long long)nleaf * mp * mp;
+  if (total == 0) return cudaSuccess;
+  HODLR_LAUNCH(pad_leaf_blocks_kernel, (unsigned)std::min<long long>(ceil_div(total, 256), 152 * 16), 256, 0, s,
+               boff, sz, nleaf, mp, src, dst);
+  return cudaGetLastError();
+}
+
 }  // namespace hodlr

@@ -213,6 +213,30 @@ HODLR_API int hodlr_rand_matrix(const int64_t *seeds, int npart, int64_t rows, i
 HODLR_API int hodlr_set_seeded(hodlr_handle h, const int64_t *useeds, const int64_t *vseeds, const int64_t *dseeds,
                                double offset);
 
+/* Trees whose leaves have unequal sizes (the reference's
+ * spmd_driver/solver_irregular_part.cc: subtrees with different leaf sizes)
+ * embed exactly in the uniform tree: every leaf is padded to m_max rows with
+ * an identity diagonal block, and the padded rows of U, V and of the
+ * right-hand sides are zero.  After a permutation the padded matrix is
+ * block diagonal in (real rows, padded rows), so its solution on the real
+ * rows is the unequal-leaf system's and its padded rows stay zero.  Create
+ * the handle with n = nleaf * m_max and leaf = m_max.
+ * hodlr_pad_rows: rows of leaf i of src (packed: rows sz[0] + .. + sz[i-1]
+ *   onwards, cols columns, leading dimension lds) to rows i * m_max .. of
+ *   dst (leading dimension ldd), zeros in the padding.
+ * hodlr_unpad_rows: the inverse, padded src to packed dst.
+ * hodlr_pad_leaf_blocks: leaf blocks packed one after another (block i:
+ *   sz[i] x sz[i], column-major) to [nleaf][m_max][m_max], ready for
+ *   hodlr_set_leaf_blocks(h, dst, m_max, m_max * m_max).
+ * sz: host array of nleaf sizes in [1, m_max]; src and dst device memory;
+ * run on `stream` (NULL = legacy default) and return when done. */
+HODLR_API int hodlr_pad_rows(int nleaf, const int32_t *sz, int m_max, int cols, const double *src, int64_t lds,
+                             double *dst, int64_t ldd, void *stream);
+HODLR_API int hodlr_unpad_rows(int nleaf, const int32_t *sz, int m_max, int cols, const double *src, int64_t lds,
+                               double *dst, int64_t ldd, void *stream);
+HODLR_API int hodlr_pad_leaf_blocks(int nleaf, const int32_t *sz, int m_max, const double *src, double *dst,
+                                    void *stream);
+
 /* Checkpoint of a factored plain handle (no counterpart in the reference,
  * which refactors on every solve): the descriptor, the launch shapes, the
  * inputs and every factor buffer in one host byte stream with a checksum.

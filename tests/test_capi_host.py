@@ -111,3 +111,14 @@ def test_draw_seeds_matches_glibc_lrand48_stream(fs):
     from oracle import oracle as O
     for master in (0, 1, 20240601, 2**31 - 1, 2**40 + 12345, -7):
         assert fs.draw_seeds(master, 37) == [int(x) for x in O.seeds(master, 37)]
+
+
+def test_padding_calls_reject_bad_sizes_on_host(fs):
+    L = fs.lib()
+    buf = (ctypes.c_double * 16)()
+    bad = (ctypes.c_int32 * 2)(3, 9)  # 9 > m_max
+    assert L.hodlr_pad_rows(2, bad, 8, 1, buf, 16, buf, 16, None) == fs.HODLR_ERR_INVALID_ARG
+    zero = (ctypes.c_int32 * 2)(0, 4)
+    assert L.hodlr_unpad_rows(2, zero, 8, 1, buf, 16, buf, 16, None) == fs.HODLR_ERR_INVALID_ARG
+    assert L.hodlr_pad_leaf_blocks(0, zero, 8, buf, buf, None) == fs.HODLR_ERR_INVALID_ARG
+    assert L.hodlr_pad_leaf_blocks(2, bad, 8, None, buf, None) == fs.HODLR_ERR_INVALID_ARG
