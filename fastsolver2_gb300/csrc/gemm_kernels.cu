@@ -321,14 +321,28 @@ static bool reduce_tma_try(const float *A, long long lda, const float *X, long l
 template <typename OutT>
 __global__ void reduce_pass2_kernel(const double *__restrict__ partial, int nchunks, long long blk,
                                     OutT *out, const int *skip) {
+  // 32 elements per CTA, the chunks split over 8 thread rows (row y sums
+  // chunks y, y + 8, ...), the 8 row sums combined in a fixed order: the
+  // long serial sums of the top levels (hundreds of chunks, few elements)
+  // spread over 8x the threads and SMs.
   if (skip && *skip) return;
-  const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  __shared__ double part[8][33];
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+  const long long e = (long long)blockIdx.x * 32 + tx;
   const int b = blockIdx.y;
-  if (e >= blk) return;
-  const double *p = partial + (long long)b * nchunks * blk + e;
-  double s = 0.0;
-  for (int c = 0; c < nchunks; ++c) s += p[(long long)c * blk];
-  out[(long long)b * blk + e] = s;
+  double acc = 0.0;
+  if (e < blk) {
+    const double *p = partial + (long long)b * nchunks * blk + e;
+    for (int c = ty; c < nchunks; c += 8) acc += p[(long long)c * blk];
+  }
+  part[ty][tx] = acc;
+  __syncthreads();
+  if (ty == 0 && e < blk) {
+    double sum = part[0][tx];
+#pragma unroll
+    for (int y = 1; y < 8; ++y) sum += part[y][tx];
+    out[(long long)b * blk + e] = sum;
+  }
 }
 
 // Row chunks per child so that about `target` CTAs run (at least 256 rows each).
@@ -400,7 +414,7 @@ static cudaError_t reduce_dispatch(const T *A, long long lda, const T *X, long l
     e = run(work);
     if (e != cudaSuccess) return e;
     const long long blk = (long long)r * C;
-    dim3 grid(ceil_div(blk, 256), nbatch);
+    dim3 grid(ceil_div(blk, 32), nbatch);
     HODLR_LAUNCH(reduce_pass2_kernel<OutT>, grid, 256, 0, s, work, nchunks, blk, out, skip);
   } else {
     e = run(out);
