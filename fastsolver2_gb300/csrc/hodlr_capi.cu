@@ -128,6 +128,9 @@ struct hodlr_ctx {
   // double-word (hi, lo) copies for the emulated FP64 residual (mixed mode)
   float2 *D2 = nullptr, *U2 = nullptr, *V2 = nullptr, *X2 = nullptr, *R2 = nullptr, *T2 = nullptr;
   bool emulated = false;
+  // tensor-core mode: D2 / U2 / V2 serve only the transposed solves, so they
+  // are made by the first transposed solve after the inputs change
+  bool dw_stale = false;
   // tensor-core residual (HODLR_RESID_FP64_TENSOR): digit slices of D (row
   // scaled), U (row scaled), V (64-row chunks), the iterate X and the
   // coupling blocks T', with their power-of-two exponents
@@ -793,7 +796,10 @@ static int prepare_leaves(hodlr_ctx *h, long long leaf0 = 0, long long count = -
   if (count < 0) count = h->nleaf;
   if (h->emulated && count > 0) {
     const long long mm = (long long)h->m * h->m, dm = count * mm;
-    CK(launch_split(h->D + leaf0 * mm, dm, h->D2 + leaf0 * mm, dm, dm, 1, nullptr, h->st));
+    if (h->oz)
+      h->dw_stale = true;
+    else
+      CK(launch_split(h->D + leaf0 * mm, dm, h->D2 + leaf0 * mm, dm, dm, 1, nullptr, h->st));
   }
   if (h->oz && count > 0) {  // rows of the leaf blocks, each scaled by its own exponent
     const long long m = h->m, mm = m * m;
@@ -809,7 +815,9 @@ static int prepare_level(hodlr_ctx *h, int l, long long row0 = 0, long long coun
   const long long n = h->n, off = (long long)l * n * h->r + row0;
   if (count < 0) count = n;
   CK((launch_convert<double, float>(h->Vlev(l) + row0, n, h->V32 + off, n, count, h->r, h->st)));
-  if (h->emulated) {
+  if (h->emulated && h->oz) {
+    h->dw_stale = true;
+  } else if (h->emulated) {
     CK(launch_split(h->Ulev(l) + row0, n, h->U2 + off, n, count, h->r, nullptr, h->st));
     CK(launch_split(h->Vlev(l) + row0, n, h->V2 + off, n, count, h->r, nullptr, h->st));
   }
@@ -822,6 +830,25 @@ static int prepare_level(hodlr_ctx *h, int l, long long row0 = 0, long long coun
     CK(launch_oz_slice_cols(h->Vlev(l) + row0, n, count, (int)r, h->Vsl + l * r * n + row0, n, L * r * n,
                             h->Vexp + l * (n / kOzChunk) * r + (row0 / kOzChunk) * r, nullptr, h->st));
   }
+  return HODLR_OK;
+}
+
+// The double-word copies of every leaf block and level (tensor-core mode),
+// made when a transposed solve first needs them after the inputs changed.
+// Rows a forest's shorter trees lack are zero in U and V, so whole-level
+// splits equal the per-system ones.  Inside a caller's stream capture the
+// copies are recorded into that graph and stay marked out of date.
+static int ensure_dw_splits(hodlr_ctx *h) {
+  if (!h->dw_stale) return HODLR_OK;
+  const long long n = h->n, r = h->r, dm = (long long)h->nleaf * h->m * h->m;
+  CK(launch_split(h->D, dm, h->D2, dm, dm, 1, nullptr, h->st));
+  for (int l = 0; l < h->L; ++l) {
+    CK(launch_split(h->Ulev(l), n, h->U2 + (long long)l * n * r, n, n, (int)r, nullptr, h->st));
+    CK(launch_split(h->Vlev(l), n, h->V2 + (long long)l * n * r, n, n, (int)r, nullptr, h->st));
+  }
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  CK(cudaStreamIsCapturing(h->st, &cs));
+  if (cs == cudaStreamCaptureStatusNone) h->dw_stale = false;
   return HODLR_OK;
 }
 
@@ -1133,6 +1160,7 @@ static int solve_impl(hodlr_handle h, double *B, int64_t ldb, int nrhs, hodlr_so
   if (nrhs < 1 || nrhs > h->kmax) return set_err(HODLR_ERR_INVALID_ARG, "nrhs out of range");
   if (ldb < h->n) return set_err(HODLR_ERR_INVALID_ARG, "ldb < n");
   CKS(reset_status(h));
+  if (trans && h->mixed) CKS(ensure_dw_splits(h));
   CK(cudaEventRecord(h->ev[2], h->st));
   auto key = std::make_tuple((const double *)B, (long long)ldb, nrhs, trans ? 1 : 0);
   if (h->solve_graphs.size() > 32 && !h->solve_graphs.count(key)) {  // bound the graph cache

@@ -67,10 +67,45 @@ __global__ void oz_slice_rows_kernel(const double *A, long long rpb, long long b
     oz_digits(row[q * sq], E, [&](int s, __nv_bfloat16 d) { o[s * sstride + q] = d; });
 }
 
+// The same slicing with 16-byte digit stores: a thread packs the digits of 8
+// consecutive columns of its row into one 16-byte store per slice (7 stores
+// per 8 columns instead of 56 two-byte stores, each of which made the warp
+// touch 32 separate sectors).  Needs cols, ld_out and the slice stride to be
+// multiples of 8 and a 16-byte aligned output (checked by the launcher).
+__global__ void oz_slice_rows8_kernel(const double *A, long long rpb, long long bstride, long long si, long long sq,
+                                      long long rows, int cols, __nv_bfloat16 *out, long long ld_out,
+                                      long long sstride, int *exps) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= rows) return;
+  const double *row = A + (i / rpb) * bstride + (i % rpb) * si;
+  unsigned long long mb = 0;
+  for (int q = 0; q < cols; ++q) mb = max(mb, abs_bits(row[q * sq]));
+  const int E = oz_exponent_bits(mb);
+  exps[i] = E;
+  __nv_bfloat16 *o = out + i * ld_out;
+  for (int q0 = 0; q0 < cols; q0 += 8) {
+    double v[8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) v[u] = row[(q0 + u) * sq];
+    __align__(16) __nv_bfloat16 d[kOzSlices][8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) oz_digits(v[u], E, [&](int sl, __nv_bfloat16 x) { d[sl][u] = x; });
+#pragma unroll
+    for (int sl = 0; sl < kOzSlices; ++sl)
+      *reinterpret_cast<uint4 *>(o + sl * sstride + q0) = *reinterpret_cast<const uint4 *>(d[sl]);
+  }
+}
+
 cudaError_t launch_oz_slice_rows(const double *A, long long rpb, long long bstride, long long si, long long sq,
                                  long long rows, int cols, __nv_bfloat16 *out, long long ld_out,
                                  long long slice_stride, int *exps, cudaStream_t s) {
   if (rows <= 0) return cudaSuccess;
+  const bool a16 = ((uintptr_t)out & 15) == 0 && cols % 8 == 0 && ld_out % 8 == 0 && slice_stride % 8 == 0;
+  if (a16) {
+    HODLR_LAUNCH(oz_slice_rows8_kernel, ceil_div(rows, 128), 128, 0, s, A, rpb, bstride, si, sq, rows, cols, out,
+                 ld_out, slice_stride, exps);
+    return cudaGetLastError();
+  }
   HODLR_LAUNCH(oz_slice_rows_kernel, ceil_div(rows, 128), 128, 0, s, A, rpb, bstride, si, sq, rows, cols, out,
                ld_out, slice_stride, exps);
   return cudaGetLastError();

@@ -197,6 +197,32 @@ def test_transpose_solve(hodlr, precision):
     assert rel(to_host(B), Xd) < 1e-11
 
 
+def test_mixed_transpose_solve_follows_new_inputs(hodlr):
+    """In the tensor-core residual mode the double-word copies that transposed
+    solves use are made by the first transposed solve after the inputs change.
+    A second problem set into the same handle (every leaf block and level)
+    must be the one solved, before and after forward solves."""
+    p1 = P.gaussian_problem(128, 5, 16, nrhs=2, seed=31, orthonormal=True, decay=3.0, shift=2.0)
+    p2 = P.gaussian_problem(128, 5, 16, nrhs=2, seed=32, orthonormal=True, decay=3.0, shift=2.0)
+    s = make_solver(hodlr, p1, precision=hodlr.PREC_MIXED, residual=hodlr.RESID_FP64_TENSOR, refine_tol=1e-12)
+    for pr in (p1, p2):
+        if pr is p2:
+            keep = [to_dev(pr.K)]
+            s.set_leaf_blocks(keep[0])
+            for l in range(pr.levels):
+                keep += [to_dev(pr.U[l]), to_dev(pr.V[l]), to_dev(pr.s[l])]
+                s.set_lowrank(l, *keep[-3:])
+            torch.cuda.synchronize()
+        s.factor()
+        for trans in (True, False, True):
+            B = to_dev(pr.B)
+            info = s.solve(B, transpose=trans)
+            assert info.rel_residual <= 1e-12
+            A = pr.dense()
+            Xd = np.linalg.solve(A.T if trans else A, pr.B)
+            assert rel(to_host(B), Xd) < 1e-11, (pr is p2, trans)
+
+
 @pytest.mark.parametrize("trans", [False, True])
 def test_matvec_fp64(hodlr, trans):
     pr = P.gaussian_problem(64, 5, 8, nrhs=3, seed=4, orthonormal=True, decay=2.0)
