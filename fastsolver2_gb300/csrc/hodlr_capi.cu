@@ -145,6 +145,12 @@ struct hodlr_ctx {
   DevStatus *dst = nullptr, *hst = nullptr;
   // timing
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+  // set-time preparation on a side stream (hodlr_set_leaf_blocks /
+  // hodlr_set_lowrank): pst, the copy-done event, one prepared event per input
+  // (leaf blocks, then level l at 1 + l), and the last one enqueued
+  cudaStream_t pst = nullptr;
+  cudaEvent_t pcopy = nullptr, plast = nullptr;
+  std::vector<cudaEvent_t> pready;
   float factor_ms = 0.f, solve_ms = 0.f;
   // graphs
   bool use_graphs = true;
@@ -272,6 +278,11 @@ static void free_ctx(hodlr_ctx *h) {
   if (h->hst) cudaFreeHost(h->hst);
   for (auto &e : h->ev)
     if (e) cudaEventDestroy(e);
+  if (h->pst) cudaStreamSynchronize(h->pst);
+  for (auto &e : h->pready)
+    if (e) cudaEventDestroy(e);
+  if (h->pcopy) cudaEventDestroy(h->pcopy);
+  if (h->pst) cudaStreamDestroy(h->pst);
   if (h->own_stream && h->st) cudaStreamDestroy(h->st);
   delete h;
 }
@@ -329,7 +340,19 @@ static int sync_status(hodlr_ctx *h, hodlr_solve_info *info) {
   return HODLR_OK;
 }
 
+// The handle's stream waits for the set-time preparation still running on the
+// side stream (every call that reads the prepared copies, or writes the
+// inputs by another route, comes through here first).
+static int join_prep(hodlr_ctx *h) {
+  if (h->plast) {
+    CK(cudaStreamWaitEvent(h->st, h->plast, 0));
+    h->plast = nullptr;
+  }
+  return HODLR_OK;
+}
+
 static int reset_status(hodlr_ctx *h) {
+  CKS(join_prep(h));
   CK(cudaMemsetAsync(h->dst, 0, sizeof(DevStatus), h->st));
   return HODLR_OK;
 }
@@ -792,43 +815,45 @@ static int mixed_solve(hodlr_ctx *h, double *B, long long ldb, int k, bool trans
 // Input-derived copies of the mixed path, made when the inputs are set (so a
 // factorisation only reads them): FP32 V for the sweeps and the double-word
 // splits of D, U, V for the emulated residual.
-static int prepare_leaves(hodlr_ctx *h, long long leaf0 = 0, long long count = -1) {
+static int prepare_leaves(hodlr_ctx *h, long long leaf0 = 0, long long count = -1, cudaStream_t ps = nullptr) {
+  const cudaStream_t st = ps ? ps : h->st;
   if (count < 0) count = h->nleaf;
   if (h->emulated && count > 0) {
     const long long mm = (long long)h->m * h->m, dm = count * mm;
     if (h->oz)
       h->dw_stale = true;
     else
-      CK(launch_split(h->D + leaf0 * mm, dm, h->D2 + leaf0 * mm, dm, dm, 1, nullptr, h->st));
+      CK(launch_split(h->D + leaf0 * mm, dm, h->D2 + leaf0 * mm, dm, dm, 1, nullptr, st));
   }
   if (h->oz && count > 0) {  // rows of the leaf blocks, each scaled by its own exponent
     const long long m = h->m, mm = m * m;
     CK(launch_oz_slice_rows(h->D + leaf0 * mm, m, mm, 1, m, count * m, (int)m, h->Dsl + leaf0 * mm, m,
-                            h->n * m, h->Dexp + leaf0 * m, h->st));
+                            h->n * m, h->Dexp + leaf0 * m, st));
   }
   return HODLR_OK;
 }
 
 // Level l, rows [row0, row0 + count) (default: all rows).
-static int prepare_level(hodlr_ctx *h, int l, long long row0 = 0, long long count = -1) {
+static int prepare_level(hodlr_ctx *h, int l, long long row0 = 0, long long count = -1, cudaStream_t ps = nullptr) {
   if (!h->mixed) return HODLR_OK;
+  const cudaStream_t st = ps ? ps : h->st;
   const long long n = h->n, off = (long long)l * n * h->r + row0;
   if (count < 0) count = n;
-  CK((launch_convert<double, float>(h->Vlev(l) + row0, n, h->V32 + off, n, count, h->r, h->st)));
+  CK((launch_convert<double, float>(h->Vlev(l) + row0, n, h->V32 + off, n, count, h->r, st)));
   if (h->emulated && h->oz) {
     h->dw_stale = true;
   } else if (h->emulated) {
-    CK(launch_split(h->Ulev(l) + row0, n, h->U2 + off, n, count, h->r, nullptr, h->st));
-    CK(launch_split(h->Vlev(l) + row0, n, h->V2 + off, n, count, h->r, nullptr, h->st));
+    CK(launch_split(h->Ulev(l) + row0, n, h->U2 + off, n, count, h->r, nullptr, st));
+    CK(launch_split(h->Vlev(l) + row0, n, h->V2 + off, n, count, h->r, nullptr, st));
   }
   if (h->oz) {
     const long long r = h->r, L = h->L;
     // U: row-scaled digits, rows of r contiguous entries
     CK(launch_oz_slice_rows(h->Ulev(l) + row0, count, 0, 1, n, count, (int)r, h->Usl + l * n * r + row0 * r, r,
-                            L * n * r, h->Uexp + l * n + row0, h->st));
+                            L * n * r, h->Uexp + l * n + row0, st));
     // V: digits scaled per 64-row chunk of each column, column-major
     CK(launch_oz_slice_cols(h->Vlev(l) + row0, n, count, (int)r, h->Vsl + l * r * n + row0, n, L * r * n,
-                            h->Vexp + l * (n / kOzChunk) * r + (row0 / kOzChunk) * r, nullptr, h->st));
+                            h->Vexp + l * (n / kOzChunk) * r + (row0 / kOzChunk) * r, nullptr, st));
   }
   return HODLR_OK;
 }
@@ -849,6 +874,56 @@ static int ensure_dw_splits(hodlr_ctx *h) {
   cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
   CK(cudaStreamIsCapturing(h->st, &cs));
   if (cs == cudaStreamCaptureStatusNone) h->dw_stale = false;
+  return HODLR_OK;
+}
+
+// Set-time preparation of the copies derived from one input (input 0: the
+// leaf blocks, 1 + l: level l) on a side stream, so that it overlaps the copy
+// of the next input when the hodlr_set_* calls follow one another (from host
+// memory the copies run at the host link's rate, the preparation on the SMs).
+// Order: before the copy into an input, the handle's stream waits for that
+// input's previous preparation (wait_prepared); the side stream waits for the
+// copy; calls that read prepared copies join the side stream first
+// (join_prep).  Inside a caller's stream capture it all stays on the
+// handle's stream.
+static bool side_prep_ok(hodlr_ctx *h) {
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing(h->st, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone) return false;
+  if (!h->pst) {
+    if (cudaStreamCreateWithFlags(&h->pst, cudaStreamNonBlocking) != cudaSuccess) {
+      h->pst = nullptr;
+      return false;
+    }
+    if (cudaEventCreateWithFlags(&h->pcopy, cudaEventDisableTiming) != cudaSuccess) {
+      h->pcopy = nullptr;
+      return false;
+    }
+    h->pready.assign(1 + h->L, nullptr);
+    for (auto &e : h->pready)
+      if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) {
+        e = nullptr;
+        return false;
+      }
+  }
+  return h->pcopy != nullptr;
+}
+
+static int wait_prepared(hodlr_ctx *h, int input) {
+  if (h->pst && !h->pready.empty() && h->pready[input]) CK(cudaStreamWaitEvent(h->st, h->pready[input], 0));
+  return HODLR_OK;
+}
+
+template <typename F>
+static int prepare_input(hodlr_ctx *h, int input, F prep) {
+  if (!h->mixed || !side_prep_ok(h)) {
+    CKS(join_prep(h));
+    return prep(h->st);
+  }
+  CK(cudaEventRecord(h->pcopy, h->st));
+  CK(cudaStreamWaitEvent(h->pst, h->pcopy, 0));
+  CKS(prep(h->pst));
+  CK(cudaEventRecord(h->pready[input], h->pst));
+  h->plast = h->pready[input];
   return HODLR_OK;
 }
 
@@ -1073,6 +1148,7 @@ int hodlr_create(const hodlr_desc *desc, hodlr_handle *out) {
 
 int hodlr_destroy(hodlr_handle h) {
   if (!h) return HODLR_OK;
+  if (h->pst) cudaStreamSynchronize(h->pst);
   cudaStreamSynchronize(h->st);
   free_ctx(h);
   return HODLR_OK;
@@ -1080,6 +1156,8 @@ int hodlr_destroy(hodlr_handle h) {
 
 int hodlr_set_stream(hodlr_handle h, void *stream) {
   if (!h) return set_err(HODLR_ERR_INVALID_ARG, "null handle");
+  if (h->pst) CK(cudaStreamSynchronize(h->pst));
+  h->plast = nullptr;
   CK(cudaStreamSynchronize(h->st));
   if (h->own_stream) cudaStreamDestroy(h->st);
   h->own_stream = false;
@@ -1097,6 +1175,7 @@ int hodlr_set_leaf_blocks(hodlr_handle h, const double *D, int64_t ld, int64_t l
   if (ld < h->m) return set_err(HODLR_ERR_INVALID_ARG, "ld < leaf size");
   const int m = h->m;
   const long long mm = (long long)m * m;
+  CKS(wait_prepared(h, 0));
   if (ld == m && leaf_stride == mm) {
     CK(cudaMemcpyAsync(h->D, D, sizeof(double) * mm * h->nleaf, cudaMemcpyDefault, h->st));
   } else {
@@ -1108,7 +1187,7 @@ int hodlr_set_leaf_blocks(hodlr_handle h, const double *D, int64_t ld, int64_t l
   }
   h->has_D = true;
   h->factored = false;
-  return prepare_leaves(h);
+  return prepare_input(h, 0, [&](cudaStream_t ps) { return prepare_leaves(h, 0, -1, ps); });
 }
 
 int hodlr_set_lowrank(hodlr_handle h, int level, const double *U, int64_t ldu, const double *V, int64_t ldv,
@@ -1116,6 +1195,7 @@ int hodlr_set_lowrank(hodlr_handle h, int level, const double *U, int64_t ldu, c
   if (!h || !U || !V) return set_err(HODLR_ERR_INVALID_ARG, "null argument");
   if (level < 0 || level >= h->L) return set_err(HODLR_ERR_INVALID_ARG, "level out of range");
   if (ldu < h->n || ldv < h->n) return set_err(HODLR_ERR_INVALID_ARG, "ld < n");
+  CKS(wait_prepared(h, 1 + level));
   // plain (2-D) copies: the sources may be device or host memory
   CK(cudaMemcpy2DAsync(h->Ulev(level), sizeof(double) * h->n, U, sizeof(double) * ldu, sizeof(double) * h->n,
                        h->r, cudaMemcpyDefault, h->st));
@@ -1127,7 +1207,7 @@ int hodlr_set_lowrank(hodlr_handle h, int level, const double *U, int64_t ldu, c
     CK(launch_fill(h->slev(level), h->r, 1.0, h->st));
   h->has_level[level] = 1;
   h->factored = false;
-  return prepare_level(h, level);
+  return prepare_input(h, 1 + level, [&](cudaStream_t ps) { return prepare_level(h, level, 0, -1, ps); });
 }
 
 int hodlr_factor(hodlr_handle h) {
@@ -1650,6 +1730,7 @@ int hodlr_rand_matrix(const int64_t *seeds, int npart, int64_t rows, int cols, d
 int hodlr_set_seeded(hodlr_handle h, const int64_t *useeds, const int64_t *vseeds, const int64_t *dseeds,
                      double offset) {
   if (!h || !useeds || !vseeds || !dseeds) return set_err(HODLR_ERR_INVALID_ARG, "null argument");
+  CKS(join_prep(h));  // the inputs are rewritten: set-time preparation still reading them ends first
   if (h->forest) return set_err(HODLR_ERR_INVALID_ARG, "batch handles take hodlr_batch_set_* inputs");
   const long long n = h->n;
   const int m = h->m, L = h->L, r = h->r, nl = h->nleaf;
@@ -1698,6 +1779,7 @@ int hodlr_set_seeded(hodlr_handle h, const int64_t *useeds, const int64_t *vseed
 
 int hodlr_set_uvd(hodlr_handle h, const double *U, int64_t ldu, const double *V, int64_t ldv, const double *Dg) {
   if (!h || !U || !V || !Dg) return set_err(HODLR_ERR_INVALID_ARG, "null argument");
+  CKS(join_prep(h));  // the inputs are rewritten: set-time preparation still reading them ends first
   if (ldu < h->n || ldv < h->n) return set_err(HODLR_ERR_INVALID_ARG, "ld < n");
   const long long n = h->n;
   const int m = h->m, L = h->L, r = h->r;

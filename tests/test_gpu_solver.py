@@ -223,6 +223,44 @@ def test_mixed_transpose_solve_follows_new_inputs(hodlr):
             assert rel(to_host(B), Xd) < 1e-11, (pr is p2, trans)
 
 
+def _to_pinned(a):
+    """A column-major copy in pinned host memory."""
+    a = np.asarray(a, dtype=np.float64)
+    if a.ndim == 1:
+        return torch.from_numpy(a.copy()).pin_memory()
+    return torch.from_numpy(np.ascontiguousarray(a.T)).pin_memory().t()
+
+
+def test_set_from_pinned_host_matches_device_set(hodlr):
+    """The mixed mode prepares the copies derived from each input on a side
+    stream while the next input is copied.  Inputs set from pinned host memory
+    -- one level first set to other values and overwritten straight away --
+    solve to the same bits as the same inputs set from device memory."""
+    pr = P.gaussian_problem(128, 5, 16, nrhs=3, seed=41, orthonormal=True, decay=3.0, shift=2.0)
+    other = P.gaussian_problem(128, 5, 16, nrhs=3, seed=42, orthonormal=True, decay=3.0, shift=2.0)
+    a = make_solver(hodlr, pr, precision=hodlr.PREC_MIXED, refine_tol=1e-12)
+    b = hodlr.Solver(pr.n, pr.leaf, pr.levels, pr.rank, nrhs_max=pr.nrhs, precision=hodlr.PREC_MIXED,
+                     refine_tol=1e-12)
+    keep = [_to_pinned(pr.K)]
+    b.set_leaf_blocks(keep[0])
+    for l in range(pr.levels):
+        if l == 2:
+            keep += [_to_pinned(other.U[l]), _to_pinned(other.V[l]), _to_pinned(other.s[l])]
+            b.set_lowrank(l, *keep[-3:])
+        keep += [_to_pinned(pr.U[l]), _to_pinned(pr.V[l]), _to_pinned(pr.s[l])]
+        b.set_lowrank(l, *keep[-3:])
+    xs = []
+    for s in (a, b):
+        s.factor()
+        B = to_dev(pr.B)
+        torch.cuda.synchronize()
+        info = s.solve(B)
+        assert info.rel_residual <= 1e-12
+        xs.append(to_host(B))
+    assert np.array_equal(xs[0], xs[1])
+    assert rel(xs[1], np.linalg.solve(pr.dense(), pr.B)) < 1e-11
+
+
 @pytest.mark.parametrize("trans", [False, True])
 def test_matvec_fp64(hodlr, trans):
     pr = P.gaussian_problem(64, 5, 8, nrhs=3, seed=4, orthonormal=True, decay=2.0)
