@@ -320,29 +320,47 @@ def run_ours(args, wl):
             lib = fs.lib()
             Be = colmajor(n, k)
 
-            def e2e_step():
+            # events between the parts of each step: inputs set (host copies
+            # + preparation), factor, solve, read-back
+            pev = [[torch.cuda.Event(enable_timing=True) for _ in range(4)] for _ in range(args.e2e_steps)]
+
+            def e2e_step(ev=None):
                 fs.check(lib.hodlr_set_leaf_blocks(mixed.h, hD.data_ptr(), m, m * m))
                 for l in range(L):
                     off = l * n * r * 8
                     fs.check(lib.hodlr_set_lowrank(mixed.h, l, hU.data_ptr() + off, n, hV.data_ptr() + off, n,
                                                    hs.data_ptr() + l * r * 8))
                 Be.copy_(hB, non_blocking=True)
+                if ev:
+                    ev[0].record(stream)
                 mixed.factor()
+                if ev:
+                    ev[1].record(stream)
                 mixed.solve(Be)
+                if ev:
+                    ev[2].record(stream)
                 hX.copy_(Be, non_blocking=True)
+                if ev:
+                    ev[3].record(stream)
                 stream.synchronize()
 
             e2e_step()
             torch.cuda.synchronize()
             g0, g1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             g0.record(stream)
-            for _ in range(args.e2e_steps):
-                e2e_step()
+            for i in range(args.e2e_steps):
+                e2e_step(pev[i])
             g1.record(stream)
             torch.cuda.synchronize()
             h2d = (hD.numel() + hU.numel() + hV.numel() + L * r + n * k) * 8
             e2e = {"value": g0.elapsed_time(g1) / args.e2e_steps, "unit": "ms", "h2d_bytes_per_step": h2d,
                    "d2h_bytes_per_step": n * k * 8}
+            # per step (medians): inputs set (host copies + preparation, from the
+            # previous step's end), factor, solve, read-back of the solution
+            starts = [g0] + [ev[3] for ev in pev[:-1]]
+            parts = [[a.elapsed_time(b) for a, b in zip([st] + ev[:3], ev)] for st, ev in zip(starts, pev)]
+            e2e["parts_ms"] = {name: float(np.median([p[i] for p in parts]))
+                               for i, name in enumerate(("set_inputs", "factor", "solve", "readback"))}
 
         # the same tree with the plain Gaussian generators (leaf shift 4): FP64 and mixed
         gauss = None
