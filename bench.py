@@ -764,7 +764,7 @@ def main():
     ap.add_argument("--resid", type=int, default=2,
                     help="0 native FP64 residual, 1 double-word FP32 pipes, 2 tensor-core digit products")
     ap.add_argument("--fp64-steps", type=int, default=3)
-    ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--e2e-steps", type=int, default=5)
     ap.add_argument("--small", action="store_true", help="N=2^14 smoke-sized workload")
     ap.add_argument("--levels", type=int, default=None, help="override the tree depth (N = 128 * 2^levels)")
     ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 comparator")

@@ -151,11 +151,18 @@ struct hodlr_ctx {
   cudaStream_t pst = nullptr;
   cudaEvent_t pcopy = nullptr, plast = nullptr;
   std::vector<cudaEvent_t> pready;
+  // mixed mode: the leaf LU (+ inverses) started on the side stream as soon
+  // as the leaf blocks are set, its status in dst_leaf; the next factorisation
+  // skips its own leaf LU and takes over that status
+  DevStatus *dst_leaf = nullptr;
+  bool leaves_prefactored = false;
   float factor_ms = 0.f, solve_ms = 0.f;
   // graphs
   bool use_graphs = true;
   int factor_runs = 0;
   GraphEntry factor_graph;
+  int factor_nl_runs = 0;  // the factorisation without its leaf LU (leaves_prefactored)
+  GraphEntry factor_nl_graph;
   std::map<std::tuple<const double *, long long, int, int>, GraphEntry> solve_graphs;
   std::map<std::tuple<const double *, long long, int, int>, int> solve_runs;
   std::vector<void *> allocs;
@@ -213,6 +220,10 @@ static void clear_graphs(hodlr_ctx *h) {
   destroy_recs(h->factor_graph.recs);
   h->factor_graph = GraphEntry();
   h->factor_runs = 0;
+  if (h->factor_nl_graph.exec) cudaGraphExecDestroy(h->factor_nl_graph.exec);
+  destroy_recs(h->factor_nl_graph.recs);
+  h->factor_nl_graph = GraphEntry();
+  h->factor_nl_runs = 0;
   h->last_recs = nullptr;
 }
 
@@ -456,7 +467,7 @@ static int cap_apply(hodlr_ctx *h, int l, int C, long long tb_stride, bool trans
 // Factorisation sweep: leaf LU (+ explicit leaf inverses), Ut = D^{-1} U
 // (all levels at once), then for depth L-1 .. 0: T = V^T [Ut_d | Ut_u],
 // capacitance LU + inverse, eta = Sinv [s.T1d; s.T0d], Ut_d -= Ut_u eta.
-template <typename T> static int factor_sweep(hodlr_ctx *h) {
+template <typename T> static int factor_sweep(hodlr_ctx *h, bool leaves_done = false) {
   const long long n = h->n;
   const int m = h->m, L = h->L, r = h->r;
   cudaStream_t s = h->st;
@@ -465,9 +476,11 @@ template <typename T> static int factor_sweep(hodlr_ctx *h) {
   const T *Vt = Vptr<T>(h);
   T *Dinv = Dinvptr<T>(h);
   const bool fused = Dinv && leaf_getrf_fused_inverse(m, sizeof(T));
-  PHASE(h, HODLR_PHASE_LEAF_LU,
-        launch_leaf_getrf<T>(h->D, m, (long long)m * m, LU, h->ipiv, m, h->nleaf, h->dst, fused ? Dinv : nullptr, s));
-  if (Dinv && !fused) PHASE(h, HODLR_PHASE_LEAF_LU, launch_leaf_inverse<T>(LU, h->ipiv, m, h->nleaf, Dinv, s));
+  if (!leaves_done) {
+    PHASE(h, HODLR_PHASE_LEAF_LU,
+          launch_leaf_getrf<T>(h->D, m, (long long)m * m, LU, h->ipiv, m, h->nleaf, h->dst, fused ? Dinv : nullptr, s));
+    if (Dinv && !fused) PHASE(h, HODLR_PHASE_LEAF_LU, launch_leaf_inverse<T>(LU, h->ipiv, m, h->nleaf, Dinv, s));
+  }
   if (L == 0) return HODLR_OK;
   if (sizeof(T) == 4 && Dinv && m == 128) {
     // Utilde = D^{-1} U straight from the FP64 U (rounded as it is staged)
@@ -1080,6 +1093,7 @@ static int create_ctx(const hodlr_desc &d, const std::vector<int> &sys_levels, h
     ALLOC(h->sfold, double, (size_t)r);
   }
   ALLOC(h->dst, DevStatus, 1);
+  ALLOC(h->dst_leaf, DevStatus, 1);
 #undef ALLOC
   if (cudaMallocHost(&h->hst, sizeof(DevStatus)) != cudaSuccess) {
     free_ctx(h);
@@ -1187,7 +1201,22 @@ int hodlr_set_leaf_blocks(hodlr_handle h, const double *D, int64_t ld, int64_t l
   }
   h->has_D = true;
   h->factored = false;
-  return prepare_input(h, 0, [&](cudaStream_t ps) { return prepare_leaves(h, 0, -1, ps); });
+  h->leaves_prefactored = false;
+  return prepare_input(h, 0, [&](cudaStream_t ps) -> int {
+    CKS(prepare_leaves(h, 0, -1, ps));
+    if (h->mixed && ps != h->st) {
+      // the leaf LU (+ inverses) depends on the leaf blocks alone: it runs on
+      // the side stream while the low-rank inputs are still being copied
+      float *Dinv = h->Dinv32;
+      const bool fused = Dinv && leaf_getrf_fused_inverse(m, sizeof(float));
+      CK(cudaMemsetAsync(h->dst_leaf, 0, sizeof(DevStatus), ps));
+      CK(launch_leaf_getrf<float>(h->D, m, mm, h->LU32, h->ipiv, m, h->nleaf, h->dst_leaf, fused ? Dinv : nullptr,
+                                  ps));
+      if (Dinv && !fused) CK(launch_leaf_inverse<float>(h->LU32, h->ipiv, m, h->nleaf, Dinv, ps));
+      h->leaves_prefactored = true;
+    }
+    return HODLR_OK;
+  });
 }
 
 int hodlr_set_lowrank(hodlr_handle h, int level, const double *U, int64_t ldu, const double *V, int64_t ldv,
@@ -1218,11 +1247,17 @@ int hodlr_factor(hodlr_handle h) {
     if (!h->has_level[l]) return set_err(HODLR_ERR_NOT_FACTORED, "low-rank level not set");
   h->factored = false;
   CKS(reset_status(h));
+  // leaf LU already run on the side stream since the leaf blocks were set:
+  // its status becomes the factorisation's, and the sweep starts after it
+  const bool nl = h->leaves_prefactored;
+  h->leaves_prefactored = false;
+  if (nl) CK(cudaMemcpyAsync(h->dst, h->dst_leaf, sizeof(DevStatus), cudaMemcpyDeviceToDevice, h->st));
   CK(cudaEventRecord(h->ev[0], h->st));
-  int rc = run_graphed(h, h->factor_graph, h->factor_runs, [&]() -> int {
-    if (h->mixed) return factor_sweep<float>(h);
-    return factor_sweep<double>(h);
-  });
+  int rc = run_graphed(h, nl ? h->factor_nl_graph : h->factor_graph, nl ? h->factor_nl_runs : h->factor_runs,
+                       [&]() -> int {
+                         if (h->mixed) return factor_sweep<float>(h, nl);
+                         return factor_sweep<double>(h, nl);
+                       });
   CKS(rc);
   CK(cudaEventRecord(h->ev[1], h->st));
   int fst = sync_status(h, nullptr);
@@ -1465,6 +1500,7 @@ int hodlr_generate(hodlr_handle h, uint64_t seed, double shift, int orthonormal,
   CKS(reset_status(h));
   CK(launch_gen_leaves(h->D, m, h->nleaf, seed, shift, s));
   h->has_D = true;
+  h->leaves_prefactored = false;
   CKS(prepare_leaves(h));
   double *tmp = nullptr;
   if (orthonormal && L > 0) CK(cudaMallocAsync(&tmp, sizeof(double) * n * r, s));
@@ -1771,6 +1807,7 @@ int hodlr_set_seeded(hodlr_handle h, const int64_t *useeds, const int64_t *vseed
     CKS(prepare_level(h, l));
   }
   h->has_D = true;
+  h->leaves_prefactored = false;
   CKS(prepare_leaves(h));
   h->factored = false;
   CK(cudaStreamSynchronize(s));
@@ -1825,6 +1862,7 @@ int hodlr_set_uvd(hodlr_handle h, const double *U, int64_t ldu, const double *V,
     CKS(prepare_level(h, l));
   }
   h->has_D = true;
+  h->leaves_prefactored = false;
   CKS(prepare_leaves(h));
   h->factored = false;
   CK(cudaStreamSynchronize(s));
@@ -2611,6 +2649,7 @@ int hodlr_checkpoint_save(hodlr_handle h, void *buf, int64_t bytes) {
   int64_t need = 0;
   CKS(hodlr_checkpoint_size(h, &need));
   if (!buf) return set_err(HODLR_ERR_INVALID_ARG, "null buffer");
+  CKS(join_prep(h));  // the side stream may still be writing the leaf factors
   if (bytes < need) return set_err(HODLR_ERR_INVALID_ARG, "checkpoint buffer too small");
   CK(cudaStreamSynchronize(h->st));
   unsigned char *out = static_cast<unsigned char *>(buf);
@@ -2696,6 +2735,7 @@ int hodlr_checkpoint_load(const void *buf, int64_t bytes, void *stream, hodlr_ha
     p += nb;
   }
   h->has_D = true;
+  h->leaves_prefactored = false;
   std::fill(h->has_level.begin(), h->has_level.end(), (char)1);
   int rc = prepare_leaves(h);
   for (int l = 0; l < h->L && rc == HODLR_OK; ++l) rc = prepare_level(h, l);

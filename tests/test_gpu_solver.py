@@ -333,13 +333,29 @@ def test_generated_problem_solves(hodlr):
     assert res.item() < 1e-12
 
 
-def test_singular_leaf_reports_status(hodlr):
+@pytest.mark.parametrize("precision", [0, 1])
+def test_singular_leaf_reports_status(hodlr, precision):
+    """A zero leaf block is reported by the factorisation.  In the mixed mode
+    the leaf LU starts on the handle's side stream when the leaf blocks are
+    set, and the next factorisation takes over its status; a second
+    factorisation runs its own leaf LU.  Good leaf blocks set afterwards
+    factor and solve."""
     pr = P.gaussian_problem(32, 2, 4, nrhs=1, seed=2)
+    good = pr.K.copy()
     pr.K[2 * 32:3 * 32, :] = 0.0  # leaf 2 all zeros
-    s = make_solver(hodlr, pr)
-    with pytest.raises(hodlr.HodlrError) as e:
-        s.factor()
-    assert e.value.code == hodlr.HODLR_ERR_SINGULAR_LEAF
+    s = make_solver(hodlr, pr, precision=precision)
+    for _ in range(2):
+        with pytest.raises(hodlr.HodlrError) as e:
+            s.factor()
+        assert e.value.code == hodlr.HODLR_ERR_SINGULAR_LEAF
+    K = to_dev(good)
+    s.set_leaf_blocks(K)
+    torch.cuda.synchronize()
+    s.factor()
+    pr.K = good
+    B = to_dev(pr.B)
+    s.solve(B)
+    assert rel(to_host(B), np.linalg.solve(pr.dense(), pr.B)) < 1e-11
 
 
 def test_nonfinite_rhs_reports_status(hodlr):
