@@ -918,7 +918,10 @@ static bool side_prep_ok(hodlr_ctx *h) {
         return false;
       }
   }
-  return h->pcopy != nullptr;
+  if (!h->pcopy) return false;
+  for (cudaEvent_t e : h->pready)
+    if (!e) return false;  // a failed event creation keeps the preparation on the handle's stream
+  return true;
 }
 
 static int wait_prepared(hodlr_ctx *h, int input) {
