@@ -9,10 +9,10 @@ relative residual of 1e-12) on the ill-conditioned Gaussian workload
 step = factor + solve with inputs resident in HBM.  The plain FP64 GPU path is
 timed on the same inputs beside it.  One JSON line on stdout.
 
---impl reference: the reference's own CPU algorithm (the oracle's C
-restatement of fastSolver2's hsolve with netlib LU, threaded the way its
-Legion index launch splits subtrees) on the host cores, on a bounded subtree
-sample scaled to the full N by the algorithmic flop count.
+--impl reference: the reference's own CPU algorithm on the host cores --
+fastSolver2's hsolve with its dgemm_/dgesv_ calls on single-threaded OpenBLAS,
+threaded the way its Legion index launch splits subtrees -- solving the whole
+N = 2^20 system in every one of the K + W steps.
 
 Multi-GPU (torchrun): the solve does not shard in this build, so each rank
 solves its own independent system (replicas); the line reports the max over
@@ -129,55 +129,98 @@ class ClockSampler:
 
 
 # ---------------------------------------------------------------- CPU leg
-def cpu_sample_run(wl, levels_sample, threads):
-    """One run of the oracle port on a subtree sample; returns (seconds, flops, info)."""
+def workload_config(wl, world):
+    """The config dict both arms print (the workload, not the implementation)."""
+    return {"workload": "HODLR N=%d leaf %d L=%d rank %d nrhs %d, orthonormal-class factors s_i=10^(-6i/%d), "
+                        "leaf shift 1.5; factor+solve to rel. resid <=1e-12"
+                        % (wl["n"], wl["leaf"], wl["levels"], wl["rank"], wl["nrhs"], wl["rank"]),
+            **wl, "parallelism": "replicas" if world > 1 else "one system per device",
+            "l2": "inputs larger than L2 (>4 GB touched per step)"}
+
+
+def cpu_problem(wl, seed, threads):
+    """Host inputs of the workload for the CPU leg: leaf blocks G/sqrt(m) + 1.5 I,
+    per-level U, V Gaussian / sqrt(block rows) (the scale of orthonormal
+    blocks; the solve's flops do not depend on the values), s_i = 10^(-6 i/r)
+    folded into V, b Gaussian.  Returns (K0, W0 = [b | U^(0) | ...], Vs)."""
     from oracle import oracle as O
-    from oracle import problems as P
-    pr = P.gaussian_problem(wl["leaf"], levels_sample, wl["rank"], nrhs=wl["nrhs"], seed=SEED,
-                            orthonormal=False, shift=4.0)
-    t0 = time.perf_counter()
-    _, _, info = O.hsolve_general(pr, pr.B, nthreads=threads)
-    dt = time.perf_counter() - t0
-    F, S = algo_flops(pr.n, wl["leaf"], levels_sample, wl["rank"], wl["nrhs"])
-    return dt, F + S, info
+    n, m, L, r, k = wl["n"], wl["leaf"], wl["levels"], wl["rank"], wl["nrhs"]
+    K0 = np.empty((n, m), order="F")
+    O.fill_gaussian(K0, seed, 1.0 / np.sqrt(m), 1.5, m, threads)
+    W0 = np.empty((n, k + L * r), order="F")
+    O.fill_gaussian(W0[:, :k], seed + 1, 1.0, 0.0, 0, threads)
+    sv = 10.0 ** (-6.0 * np.arange(r) / r)
+    Vs = []
+    for l in range(L):
+        nb = n >> (l + 1)
+        O.fill_gaussian(W0[:, k + l * r:k + (l + 1) * r], seed + 2 + 2 * l, 1.0 / np.sqrt(nb), 0.0, 0, threads)
+        V = np.empty((n, r), order="F")
+        O.fill_gaussian(V, seed + 3 + 2 * l, 1.0 / np.sqrt(nb), 0.0, 0, threads)
+        V *= sv[None, :]
+        Vs.append(V)
+    return K0, W0, Vs
 
 
-def cpu_baseline(wl, small, repeats=1):
-    threads = os.cpu_count() or 1
-    Ls = 4 if small else 10
-    F, S = algo_flops(wl["n"], wl["leaf"], wl["levels"], wl["rank"], wl["nrhs"])
-    vals = []
-    for _ in range(repeats):
-        dt, fl, info = cpu_sample_run(wl, Ls, threads)
-        assert info == 0
-        vals.append(dt * (F + S) / fl * 1e3)
-    sample = ("oracle C port of hsolve (netlib LU) on a %d-row subtree (leaf %d, %d levels, rank %d, %d rhs), "
-              "%d threads; scaled to N=%d by the algorithmic flop ratio"
-              % (wl["leaf"] << Ls, wl["leaf"], Ls, wl["rank"], wl["nrhs"], threads, wl["n"]))
-    return float(np.median(vals)), threads, sample
+def cpu_solve_runs(wl, steps, warmup, threads=None, seed=SEED):
+    """Full-size solves of the reference algorithm on the host cores: fastSolver2's
+    hsolve (src/tasks/leaf_solve.cc:73-154) with its dgemm_/dgesv_ calls on
+    single-threaded OpenBLAS (bitwise the reference's own build on the same BLAS),
+    the 2^p subtrees under depth p on P = 2^p threads and the top p levels as
+    row-chunked reduce / capacitance / update steps (the reference's index
+    launch).  Every step solves the whole N; the in-place inputs are restored
+    between steps outside the timing.  Returns (ms per step list, threads
+    used, relative residual of the last solution, kind, sample text)."""
+    from oracle import oracle as O
+    threads = threads or (os.cpu_count() or 1)
+    P = 1
+    while P * 2 <= threads and P * 2 <= (1 << wl["levels"]):
+        P *= 2
+    n, m, L, r, k = wl["n"], wl["leaf"], wl["levels"], wl["rank"], wl["nrhs"]
+    if O.blas_lib() is None:
+        raise RuntimeError("scipy's OpenBLAS is not available for the CPU leg")
+    K0, W0, Vs = cpu_problem(wl, seed, threads)
+    K, W = np.empty_like(K0, order="F"), np.empty_like(W0, order="F")
+    times = []
+    for i in range(warmup + steps):
+        O.copy_mt(K, K0, threads)
+        O.copy_mt(W, W0, threads)
+        t0 = time.perf_counter()
+        info = O.blas_hsolve_mt(m, L, r, K, Vs, W, k, P)
+        dt = time.perf_counter() - t0
+        if info != 0:
+            raise RuntimeError("reference hsolve failed: info %d" % info)
+        if i >= warmup:
+            times.append(dt * 1e3)
+    X = np.asfortranarray(W[:, :k])
+    Us = [W0[:, k + l * r:k + (l + 1) * r] for l in range(L)]
+    Y = O.blas_matvec(m, L, r, K0, Us, Vs, None, X, threads)
+    B = W0[:, :k]
+    resid = float((np.linalg.norm(B - Y, axis=0) / np.linalg.norm(B, axis=0)).max())
+    sample = ("fastSolver2's hsolve restated with its dgemm_/dgesv_ calls on single-threaded OpenBLAS (bitwise the "
+              "reference's own build on that BLAS), whole N=%d system every step, %d subtrees on %d threads + the "
+              "top %d levels row-chunked over them; %d steps after %d warm-up" %
+              (n, P, P, P.bit_length() - 1, steps, warmup))
+    return times, P, resid, "port", sample
 
 
 def run_reference(args, wl):
     rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
     if rank != 0:
         return 0
-    for _ in range(args.warmup):
-        cpu_baseline(wl, args.small)
-    vals = []
     t_wall = time.perf_counter()
-    for _ in range(args.steps):
-        v, threads, sample = cpu_baseline(wl, args.small)
-        vals.append(v)
+    times, threads, resid, kind, sample = cpu_solve_runs(wl, args.steps, args.warmup)
     wall = time.perf_counter() - t_wall
-    value = float(np.mean(vals))
+    value = float(np.mean(times))
     line = {"metric": METRIC, "value": value, "unit": "ms", "impl": "reference", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": value, "higher_is_better": False,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded Gaussian)",
-            "config": {"workload": "HODLR N=2^20 leaf 128 L=13 rank 32 nrhs 64 (factor+solve, one-shot hsolve)",
-                       **wl},
-            "cpu_baseline": {"value": value, "unit": "ms", "cores": threads, "kind": "port", "sample": sample},
+            "config": workload_config(wl, world),
+            "cpu_baseline": {"value": value, "unit": "ms", "cores": threads, "kind": kind, "sample": sample},
             "e2e": {"value": value, "unit": "ms", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-            "wall_s": wall}
+            "step_ms": {"median": float(np.median(times)), "min": float(np.min(times)),
+                        "max": float(np.max(times))},
+            "rel_resid": resid, "host_cores": os.cpu_count(), "wall_s": wall}
     print(json.dumps(line), flush=True)
     return 0
 
@@ -199,7 +242,9 @@ def run_ours(args, wl):
     # CPU baseline first (rank 0, N = 1), before the GPU work starts
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
-        cpu = cpu_baseline(wl, args.small)
+        ctimes, cthreads, cresid, ckind, csample = cpu_solve_runs(wl, steps=args.cpu_steps, warmup=1)
+        cpu = {"value": float(np.median(ctimes)), "unit": "ms", "cores": cthreads, "kind": ckind,
+               "sample": csample, "step_ms": ctimes, "rel_resid": cresid}
 
     n, m, L, r, k = wl["n"], wl["leaf"], wl["levels"], wl["rank"], wl["nrhs"]
     stream = torch.cuda.Stream()
@@ -210,8 +255,7 @@ def run_ours(args, wl):
         return torch.empty((cols, rows), dtype=torch.float64, device=dev).t()
 
     launches0 = fs.kernel_launches()
-    ffma_tf, dfma_tf = fs.probe_fp_peaks()   # live FMA-pipe rates of this GPU
-    mma_tf = fs.probe_mma_bf16()              # live warp-level bf16 MMA rate
+    ffma_tf, dfma_tf, mma_tf = probe_peaks()   # live FMA-pipe and warp-level bf16 MMA rates
     with torch.cuda.stream(stream):
         mixed = fs.Solver(n, m, L, r, nrhs_max=k, precision=fs.PREC_MIXED, residual=args.resid,
                           refine_tol=1e-12, refine_max_iter=10, stream=sp)
@@ -307,6 +351,9 @@ def run_ours(args, wl):
         e2e = None
         if not args.no_e2e:
             nleaf = 1 << L
+            # pinned host buffers on the GPU's NUMA node: cudaHostAlloc touches
+            # the pages from the calling thread, so it runs on that node's CPUs
+            numa = host_numa_binding(local)
             pin = dict(dtype=torch.float64, pin_memory=True)
             hD = torch.empty(nleaf * m * m, **pin)
             hU = torch.empty(L * n * r, **pin)
@@ -314,6 +361,8 @@ def run_ours(args, wl):
             hs = torch.empty(max(L, 1) * r, **pin)
             hB = torch.empty((k, n), **pin).t()
             hX = torch.empty((k, n), **pin).t()
+            numa["host_buffer_nodes"] = numa_nodes_of([hD, hU, hV, hB, hX])
+            restore_affinity(numa)
             mixed.get_inputs(D=hD, U=hU, V=hV, s=hs)
             hB.copy_(B0)
             torch.cuda.synchronize()
@@ -357,19 +406,43 @@ def run_ours(args, wl):
             torch.cuda.synchronize()
             h2d = (hD.numel() + hU.numel() + hV.numel() + L * r + n * k) * 8
             e2e = {"value": g0.elapsed_time(g1) / args.e2e_steps, "unit": "ms", "h2d_bytes_per_step": h2d,
-                   "d2h_bytes_per_step": n * k * 8}
+                   "d2h_bytes_per_step": n * k * 8, "steps": args.e2e_steps}
             # per step (medians): inputs set (host copies + preparation, from the
             # previous step's end), factor, solve, read-back of the solution
             starts = [g0] + [ev[3] for ev in pev[:-1]]
             parts = [[a.elapsed_time(b) for a, b in zip([st] + ev[:3], ev)] for st, ev in zip(starts, pev)]
-            e2e["parts_ms"] = {name: float(np.median([p[i] for p in parts]))
-                               for i, name in enumerate(("set_inputs", "factor", "solve", "readback"))}
-            e2e["per_step_ms"] = [float(sum(p)) for p in parts]
+            names = ("set_inputs", "factor", "solve", "readback")
+            e2e["parts_ms"] = {name: {"median": float(np.median([p[i] for p in parts])),
+                                      "min": float(np.min([p[i] for p in parts])),
+                                      "max": float(np.max([p[i] for p in parts]))}
+                               for i, name in enumerate(names)}
+            per_step = [float(sum(p)) for p in parts]
+            e2e["per_step_ms"] = per_step
+            e2e["step_ms"] = {"mean": float(np.mean(per_step)), "median": float(np.median(per_step)),
+                              "min": float(np.min(per_step)), "max": float(np.max(per_step))}
+            # the bare host-to-device copies of the same buffers, in the same
+            # run: the host link's share of the set_inputs part
+            dD, dU, dV = torch.empty_like(hD, device=dev), torch.empty_like(hU, device=dev), \
+                torch.empty_like(hV, device=dev)
+            bare = []
+            for _ in range(5):
+                c0, c1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                c0.record(stream)
+                dD.copy_(hD, non_blocking=True)
+                dU.copy_(hU, non_blocking=True)
+                dV.copy_(hV, non_blocking=True)
+                Be.copy_(hB, non_blocking=True)
+                c1.record(stream)
+                stream.synchronize()
+                bare.append(c0.elapsed_time(c1))
+            e2e["bare_h2d_ms"] = {"median": float(np.median(bare)), "min": float(np.min(bare)),
+                                  "max": float(np.max(bare)),
+                                  "gb_per_s": h2d / (float(np.median(bare)) * 1e-3) / 1e9}
+            e2e["numa"] = numa
             # the same set calls from device buffers: device copies plus the
             # preparation of the derived copies (FP32 V, digit slices), which
             # runs on the handle's side stream -- timed on the host around a
             # device-wide synchronisation
-            dD, dU, dV = hD.to(dev), hU.to(dev), hV.to(dev)
             torch.cuda.synchronize()
 
             def set_from_device():
@@ -463,7 +536,7 @@ def run_ours(args, wl):
             ent.update(tflops=ach, peak=peak_of[name], frac=ach / peak_of[name])
         phase_report[name] = ent
     # the kernels of the dominant phases: (phases, bound, peak, native work
-    # factor, DRAM bytes per launch from the ncu captures in profiles/, N=2^17 x 8)
+    # factor, ncu DRAM bytes per launch)
     bf16_peak = _measured_peak("bf16_tflops")
     if args.resid == 2:
         # tcgen05: the residual (leaf term and every level's update in one
@@ -523,19 +596,18 @@ def run_ours(args, wl):
                             "DRAM bytes (read + write) per launch, averaged over one step's launches")
         else:
             roof["note"] = ("FP64-equivalent algorithmic flops of the kernel's phases / their CUDA-event time in "
-                            "the timed graphs; peak = this GPU's FFMA rate measured live (hodlr_probe_fp_peaks), "
+                            "the timed graphs; peak = this GPU's FFMA rate measured live (bench_peaks.cu), "
                             "/12 for double-word arithmetic; traffic = ncu DRAM bytes per launch of the N=2^17 "
                             "capture x 8")
     line = {
         "metric": METRIC, "value": ms, "unit": "ms", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": ms, "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
         "data": "synthetic (device counter-based Gaussian generator, seeded)",
-        "config": {"workload": "HODLR N=2^20 leaf 128 L=13 rank 32 nrhs 64, mixed precision + FP64 refinement; "
-                               "orthonormal factors s_i=10^(-6i/32), leaf shift 1.5",
-                   **wl, "parallelism": "replicas" if world > 1 else "single GPU",
-                   "l2": "inputs larger than L2 (>14 GB resident per step)",
-                   "residual": {0: "native fp64", 1: "fp64-accurate double-word (FP32 pipes)",
-                                2: "fp64-accurate bf16 digit products (tcgen05 tensor cores)"}[args.resid]},
+        "config": workload_config(wl, world),
+        "method": "mixed precision (FP32 leaf LU / low-rank GEMMs, FP64 capacitance LU) + FP64 iterative "
+                  "refinement; orthonormal factors (CholeskyQR2 on the device)",
+        "residual": {0: "native fp64", 1: "fp64-accurate double-word (FP32 pipes)",
+                     2: "fp64-accurate bf16 digit products (tcgen05 tensor cores)"}[args.resid],
         "ms_per_step_with_phase_events": ms_events,
         "fp_peaks_measured_tflops": {"ffma": ffma_tf, "dfma": dfma_tf, "mma_sync_bf16": mma_tf,
                                      "hbm_gbs_measured_peaks_json": _measured_peak("hbm_gbs"),
@@ -562,7 +634,7 @@ def run_ours(args, wl):
     if ragged is not None:
         line["ragged_batch"] = ragged
     if cpu is not None:
-        line["cpu_baseline"] = {"value": cpu[0], "unit": "ms", "cores": cpu[1], "kind": "port", "sample": cpu[2]}
+        line["cpu_baseline"] = cpu
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:
@@ -678,6 +750,23 @@ def run_ragged(args, fs, torch, stream, colmajor):
         return vs
 
     V0, V = views(big0), views(big)
+    # the same systems as separate FP64 handles: the comparison loop below and
+    # the FP64 products that check the batch's solutions
+    handles = []
+    for i, (n, m, L, r, k) in enumerate(systems):
+        h = fs.Solver(n, m, L, r, nrhs_max=k, precision=fs.PREC_FP64, stream=sp)
+        h.generate(SEED + i, shift=4.0, B=None)
+        handles.append(h)
+
+    def max_residual():
+        worst = 0.0
+        with torch.cuda.stream(stream):
+            for h, x, b in zip(handles, V, V0):
+                y = torch.empty_like(x.t()).t()
+                h.matvec(x, y)
+                worst = max(worst, ((b - y).norm(dim=0) / b.norm(dim=0)).max().item())
+        return worst
+
     for prec, name in ((fs.PREC_FP64, "fp64"), (fs.PREC_MIXED, "mixed")):
         b = fs.Batch(systems, precision=prec, residual=args.resid, refine_tol=1e-12, stream=sp)
         b.generate(SEED, shift=4.0, Bs=V0)
@@ -704,15 +793,14 @@ def run_ragged(args, fs, torch, stream, colmajor):
         nf, fms, sms = b.stats()
         out[name] = {"ms_per_step": ms, "steps": nsteps, "factor_ms": fms, "solve_ms": sms, "forests": nf,
                      "tuning": tunes,
-                     "max_rel_residual": max(i.rel_residual for i in infos) if prec == fs.PREC_MIXED else None,
+                     "max_rel_residual": max_residual(),
+                     "max_rel_residual_device": (max(i.rel_residual for i in infos)
+                                                 if prec == fs.PREC_MIXED else None),
                      "max_iterations": max(i.iterations for i in infos)}
         b.close()
+    out["residual_note"] = ("max over systems and columns of ||b - A x|| / ||b||, A x by each system's own FP64 "
+                            "handle (hodlr_matvec, native FP64)")
     # the same systems as separate handles, one after another (FP64)
-    handles = []
-    for i, (n, m, L, r, k) in enumerate(systems):
-        h = fs.Solver(n, m, L, r, nrhs_max=k, precision=fs.PREC_FP64, stream=sp)
-        h.generate(SEED + i, shift=4.0, B=None)
-        handles.append(h)
     for rep in range(2):   # the first pass loads and captures, the second is timed
         torch.cuda.synchronize()
         t0 = time.perf_counter()
@@ -729,10 +817,78 @@ def run_ragged(args, fs, torch, stream, colmajor):
 
 OZ_PAIRS = 28   # digit pairs (s + t <= 6 of 7 x 7) per FP64 product in the tensor-core residual
 # ncu DRAM bytes (read + write) per launch, averaged over the launches of one
-# mixed step at N=2^20 (profiles/dram_traffic_mixed_n2e20_leaf128_r32_k64.md)
+# mixed step at N=2^20 (a dram__bytes capture of this benchmark's kernels)
 TRAFFIC = {"update_tc_kernel": 38.775e9 / 155, "update_tma_kernel": 38.804e9 / 155,
            "reduce_tma_kernel": 25.553e9 / 156,
            "oz_tc_kernel<0>": 21.130e9 / 11, "oz_tc_kernel<1>": (20.116e9 + 0.134e9) / 11}
+
+
+def host_numa_binding(local):
+    """Pin the calling thread to the CPUs of the GPU's NUMA node (when the
+    node is known and those CPUs are ours), so pinned buffers allocated next
+    land there.  Returns a record (node, CPUs, the previous affinity)."""
+    rec = {"gpu_numa_node": None, "bound_cpus": None}
+    try:
+        bus = subprocess.run(["nvidia-smi", "-i", str(local), "--query-gpu=pci.bus_id", "--format=csv,noheader"],
+                             capture_output=True, text=True, timeout=20).stdout.strip()
+        dom, rest = bus.split(":", 1)
+        path = "/sys/bus/pci/devices/%04x:%s/numa_node" % (int(dom, 16), rest.lower())
+        with open(path) as f:
+            node = int(f.read().strip())
+        rec["gpu_numa_node"] = node
+        rec["pci_bus_id"] = bus
+        if node >= 0 and hasattr(os, "sched_setaffinity"):
+            with open("/sys/devices/system/node/node%d/cpulist" % node) as f:
+                cpus = set()
+                for part in f.read().strip().split(","):
+                    if "-" in part:
+                        a, b = part.split("-")
+                        cpus.update(range(int(a), int(b) + 1))
+                    elif part:
+                        cpus.add(int(part))
+            old = os.sched_getaffinity(0)
+            use = cpus & old
+            if use:
+                os.sched_setaffinity(0, use)
+                rec["bound_cpus"] = len(use)
+                rec["_old"] = sorted(old)
+    except (OSError, ValueError, subprocess.SubprocessError):
+        pass
+    return rec
+
+
+def restore_affinity(rec):
+    old = rec.pop("_old", None)
+    if old:
+        os.sched_setaffinity(0, set(old))
+
+
+def numa_nodes_of(tensors):
+    """Pages per NUMA node of the mappings that overlap the given host
+    tensors (/proc/self/maps for the extents, /proc/self/numa_maps for the
+    per-node page counts)."""
+    spans = [(t.data_ptr(), t.data_ptr() + t.numel() * t.element_size()) for t in tensors]
+    out = {}
+    try:
+        ends = {}
+        with open("/proc/self/maps") as f:
+            for line in f:
+                a, b = line.split()[0].split("-")
+                ends[int(a, 16)] = int(b, 16)
+        with open("/proc/self/numa_maps") as f:
+            for line in f:
+                fields = line.split()
+                start = int(fields[0], 16)
+                end = ends.get(start, start)
+                if not any(start < hi and lo < end for lo, hi in spans):
+                    continue
+                for fld in fields[1:]:
+                    if fld.startswith("N") and "=" in fld:
+                        nd, cnt = fld[1:].split("=")
+                        out["node" + nd] = out.get("node" + nd, 0) + int(cnt)
+    except (OSError, ValueError, IndexError):
+        return None
+    return out
 
 
 def max_over_ranks(value, device):
@@ -745,6 +901,32 @@ def max_over_ranks(value, device):
     t = torch.tensor([float(value)], dtype=torch.float64, device=device)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return t.item()
+
+
+PEAKS_SO = os.path.join(ROOT, "bench_peaks.so")
+
+
+def build_peak_probe():
+    """Compile bench_peaks.cu (the FMA / MMA rate probe of this benchmark,
+    not part of the solver library) into bench_peaks.so for sm_103a."""
+    src = os.path.join(ROOT, "bench_peaks.cu")
+    if os.path.exists(PEAKS_SO) and os.path.getmtime(PEAKS_SO) >= os.path.getmtime(src):
+        return PEAKS_SO
+    nvcc = "/usr/local/cuda/bin/nvcc" if os.path.exists("/usr/local/cuda/bin/nvcc") else "nvcc"
+    subprocess.check_call([nvcc, "-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-lineinfo", "-shared",
+                           "-Xcompiler", "-fPIC", src, "-o", PEAKS_SO + ".tmp"])
+    os.replace(PEAKS_SO + ".tmp", PEAKS_SO)
+    return PEAKS_SO
+
+
+def probe_peaks():
+    """(FFMA, DFMA, mma.sync bf16) TFLOP/s of the current GPU, measured live."""
+    import ctypes
+    lib = ctypes.CDLL(build_peak_probe())
+    f, d, t = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
+    if lib.bench_probe_fp_peaks(ctypes.byref(f), ctypes.byref(d)) or lib.bench_probe_mma_bf16(ctypes.byref(t)):
+        raise RuntimeError("peak probe failed")
+    return f.value, d.value, t.value
 
 
 def _measured_peak(key):
@@ -764,7 +946,8 @@ def main():
     ap.add_argument("--resid", type=int, default=2,
                     help="0 native FP64 residual, 1 double-word FP32 pipes, 2 tensor-core digit products")
     ap.add_argument("--fp64-steps", type=int, default=3)
-    ap.add_argument("--e2e-steps", type=int, default=5)
+    ap.add_argument("--e2e-steps", type=int, default=20)
+    ap.add_argument("--cpu-steps", type=int, default=3, help="full-size CPU solves timed for cpu_baseline")
     ap.add_argument("--small", action="store_true", help="N=2^14 smoke-sized workload")
     ap.add_argument("--levels", type=int, default=None, help="override the tree depth (N = 128 * 2^levels)")
     ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 comparator")

@@ -1,13 +1,13 @@
-// Throughput probe: the FP32 and FP64 FMA issue rates of the current GPU,
-// the denominators of the roofline fractions of the CUDA-core kernels (the
-// FP32 GEMMs and double-word residual on the FMA pipe, the FP64 capacitance
-// factorisation on the FP64 pipe).  Each thread runs eight independent FMA
-// chains; every index is the thread's own output slot.
+// Benchmark helper (not part of the solver library): the FP32 and FP64 FMA
+// issue rates and the warp-level bf16 MMA rate of the current GPU, the
+// denominators bench.py uses for the roofline fractions of the CUDA-core
+// kernels (the FP32 GEMMs on the FMA pipe, the FP64 capacitance
+// factorisation on the FP64 pipe).  Each thread runs eight independent
+// chains; every index is the thread's own output slot.  Built by bench.py
+// (build_peak_probe) into bench_peaks.so next to this file.
 #include <cuda_runtime.h>
 
-#include "kernels.cuh"
-
-namespace hodlr {
+namespace probe {
 
 template <typename T>
 __global__ void __launch_bounds__(256) fma_chain_kernel(T *out, int iters, T a, T b) {
@@ -42,7 +42,7 @@ static cudaError_t time_chain(int iters, double *tflops) {
   float best = 0.f;
   for (int rep = 0; rep < 3; ++rep) {  // the first run loads the module
     cudaEventRecord(e0, 0);
-    HODLR_LAUNCH(fma_chain_kernel<T>, blocks, threads, 0, 0, out, iters, (T)0.999999, (T)1e-7);
+    fma_chain_kernel<T><<<blocks, threads>>>(out, iters, (T)0.999999, (T)1e-7);
     cudaEventRecord(e1, 0);
     e = cudaEventSynchronize(e1);
     if (e == cudaSuccess) e = cudaGetLastError();
@@ -99,7 +99,7 @@ static cudaError_t time_mma(int iters, double *tflops) {
   float best = 0.f;
   for (int rep = 0; rep < 3; ++rep) {
     cudaEventRecord(e0, 0);
-    HODLR_LAUNCH(mma_chain_kernel, blocks, threads, 0, 0, out, iters);
+    mma_chain_kernel<<<blocks, threads>>>(out, iters);
     cudaEventRecord(e1, 0);
     e = cudaEventSynchronize(e1);
     if (e == cudaSuccess) e = cudaGetLastError();
@@ -116,21 +116,18 @@ static cudaError_t time_mma(int iters, double *tflops) {
   return cudaSuccess;
 }
 
-}  // namespace hodlr
+}  // namespace probe
 
-using namespace hodlr;
-
-extern "C" int hodlr_probe_mma_bf16(double *tflops) {
-  if (!tflops) return set_last_error(HODLR_ERR_INVALID_ARG, "probe: null argument");
-  cudaError_t e = time_mma(4096, tflops);
-  if (e != cudaSuccess) return set_last_error(HODLR_ERR_CUDA, cudaGetErrorString(e));
-  return HODLR_OK;
+// Both return 0 or the CUDA error code.
+extern "C" __attribute__((visibility("default"))) int bench_probe_mma_bf16(double *tflops) {
+  if (!tflops) return (int)cudaErrorInvalidValue;
+  return (int)probe::time_mma(4096, tflops);
 }
 
-extern "C" int hodlr_probe_fp_peaks(double *ffma_tflops, double *dfma_tflops) {
-  if (!ffma_tflops || !dfma_tflops) return set_last_error(HODLR_ERR_INVALID_ARG, "probe: null argument");
-  cudaError_t e = time_chain<float>(65536, ffma_tflops);
-  if (e == cudaSuccess) e = time_chain<double>(4096, dfma_tflops);
-  if (e != cudaSuccess) return set_last_error(HODLR_ERR_CUDA, cudaGetErrorString(e));
-  return HODLR_OK;
+extern "C" __attribute__((visibility("default"))) int bench_probe_fp_peaks(double *ffma_tflops,
+                                                                           double *dfma_tflops) {
+  if (!ffma_tflops || !dfma_tflops) return (int)cudaErrorInvalidValue;
+  cudaError_t e = probe::time_chain<float>(65536, ffma_tflops);
+  if (e == cudaSuccess) e = probe::time_chain<double>(4096, dfma_tflops);
+  return (int)e;
 }

@@ -105,6 +105,7 @@ SIGNATURES = {
     "hodlr_set_uvd": (_I, [_VP, _VP, _I64, _VP, _I64, _VP]),
     "hodlr_gemm_reduce": (_I, [_I, _I, _I, _I, _VP, _I64, _VP, _I64, _VP, _I64]),
     "hodlr_gemm_reduce_noalloc": (_I, [_I, _I, _I, _I, _VP, _I64, _VP, _I64, _VP, _I64]),
+    "hodlr_debug_wait_fault": (_I, [_I, _I, _I64]),
     "hodlr_gemm_broadcast": (_I, [_I, _I, _I, _I, _I, _D, _VP, _I64, _VP, _I64, _D, _VP, _I64]),
     "hodlr_node_solve": (_I, [_I, _I, _I, _VP, _I64, _VP, _I64]),
     "hodlr_generate": (_I, [_VP, ctypes.c_uint64, _D, _I, _D, _VP, _I64, _I]),
@@ -122,8 +123,6 @@ SIGNATURES = {
     "hodlr_set_tuning": (_I, [_VP, ctypes.POINTER(Tuning)]),
     "hodlr_get_tuning": (_I, [_VP, ctypes.POINTER(Tuning)]),
     "hodlr_batch_autotune": (_I, [_VP, ctypes.POINTER(Tuning), _I]),
-    "hodlr_probe_fp_peaks": (_I, [ctypes.POINTER(_D), ctypes.POINTER(_D)]),
-    "hodlr_probe_mma_bf16": (_I, [ctypes.POINTER(_D)]),
     "hodlr_kernel_launches": (_I64, []),
     "hodlr_last_error_string": (ctypes.c_char_p, []),
 }
@@ -431,18 +430,10 @@ def rand_matrix(seeds, rows, A, offset=0.0, stream=None):
                                   stream))
 
 
-def probe_fp_peaks():
-    """Measured (FFMA, DFMA) TFLOP/s of the current GPU."""
-    f, d = _D(), _D()
-    check(lib().hodlr_probe_fp_peaks(ctypes.byref(f), ctypes.byref(d)))
-    return f.value, d.value
-
-
-def probe_mma_bf16():
-    """Measured warp-level bf16 MMA TFLOP/s of the current GPU."""
-    t = _D()
-    check(lib().hodlr_probe_mma_bf16(ctypes.byref(t)))
-    return t.value
+def debug_wait_fault(cta=-1, stage=0, budget_cycles=0):
+    """Test hook of the bounded device waits (see hodlr_debug_wait_fault);
+    cta=-1 switches it off."""
+    check(lib().hodlr_debug_wait_fault(cta, stage, budget_cycles))
 
 
 def kernel_launches():

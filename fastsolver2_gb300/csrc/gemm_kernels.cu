@@ -171,6 +171,18 @@ reduce_tn_kernel(const T *__restrict__ A, long long lda, const T *__restrict__ X
 // of 32, 16-byte aligned bases and leading dimensions.
 static constexpr int kTmaStages = 4;
 
+// Test hook of the bounded waits (set by hodlr_debug_wait_fault, off in
+// normal use): CTA `cta` of every reduce_tma_kernel launch does not issue the
+// copies of its stage `stage`, so nothing ever completes that stage's
+// mbarrier phase and the CTA's wait on it can only end by its clock budget,
+// `budget` cycles for that CTA (0 = the default budget; every other CTA keeps
+// the default).
+struct WaitFault {
+  int cta, stage;
+  long long budget;
+};
+__device__ WaitFault g_wait_fault = {-1, -1, 0};
+
 // Stage s of a reduce CTA: rows [row0 + 32 s, +32) of A (all ranks) and of
 // the X column tile at c0, into ring slot s % kTmaStages.
 template <int A_BYTES, int STAGE>
@@ -213,9 +225,12 @@ reduce_tma_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constan
   }
   __syncthreads();
   const int row0i = (int)row0;  // tensor coordinates are 32-bit
+  const WaitFault wf = g_wait_fault;
+  const int skip_stage = wf.cta == (int)blockIdx.x ? wf.stage : -1;
+  const long long budget = skip_stage >= 0 && wf.budget > 0 ? wf.budget : 1000000000LL;
   if (tid == 0)
     for (int s = 0; s < min(kTmaStages, nst); ++s)
-      reduce_tma_issue<A_BYTES, STAGE>(base, bars, &mapA, &mapX, s, row0i, c0);
+      if (s != skip_stage) reduce_tma_issue<A_BYTES, STAGE>(base, bars, &mapA, &mapX, s, row0i, c0);
   // packed pair accumulators: .x sums the even rows of the chunk, .y the odd
   // ones (a float4 run holds both), so one packed FMA does two products
   float2 acc[RPT][CPT];
@@ -225,17 +240,20 @@ reduce_tma_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constan
     for (int c = 0; c < CPT; ++c) acc[a][c] = make_float2(0.f, 0.f);
   for (int s = 0; s < nst; ++s) {
     const int slot = s % kTmaStages;
-    const bool ok = mbar_wait_bounded(&bars[slot], (unsigned)((s / kTmaStages) & 1));
+    const bool ok = mbar_wait_bounded(&bars[slot], (unsigned)((s / kTmaStages) & 1), budget);
     if (__syncthreads_or(!ok)) {  // every thread leaves together
       if (tid == 0) {
         report_error(st, HODLR_ERR_TIMEOUT, blockIdx.x);
-        for (int q = s; q < min(nst, s + kTmaStages); ++q)  // copies still in flight
-          (void)mbar_wait_bounded(&bars[q % kTmaStages], (unsigned)((q / kTmaStages) & 1));
+        // copies still in flight: stages s .. max(kTmaStages, s + kTmaStages - 1) - 1
+        // were issued (stage s + kTmaStages - 1 is issued only after stage s's wait)
+        const int issued_end = min(nst, max(kTmaStages, s + kTmaStages - 1));
+        for (int q = s; q < issued_end; ++q)
+          (void)mbar_wait_bounded(&bars[q % kTmaStages], (unsigned)((q / kTmaStages) & 1), budget);
       }
       return;
     }
     // every thread has finished stage s-1: its slot can be refilled
-    if (tid == 0 && s >= 1 && s - 1 + kTmaStages < nst)
+    if (tid == 0 && s >= 1 && s - 1 + kTmaStages < nst && s - 1 + kTmaStages != skip_stage)
       reduce_tma_issue<A_BYTES, STAGE>(base, bars, &mapA, &mapX, s - 1 + kTmaStages, row0i, c0);
     const unsigned char *sa = base + slot * STAGE, *sx = sa + A_BYTES;
 #pragma unroll
@@ -707,3 +725,12 @@ template cudaError_t launch_update_nn<double>(const UpdateArgs &, cudaStream_t, 
 template cudaError_t launch_update_nn<float>(const UpdateArgs &, cudaStream_t, DevStatus *);
 
 }  // namespace hodlr
+
+extern "C" int hodlr_debug_wait_fault(int cta, int stage, long long budget_cycles) {
+  if (cta < -1 || (cta >= 0 && stage < 0) || budget_cycles < 0 || budget_cycles > 1000000000LL)
+    return hodlr::set_last_error(HODLR_ERR_INVALID_ARG, "debug_wait_fault: bad arguments");
+  const hodlr::WaitFault wf = {cta, cta < 0 ? -1 : stage, cta < 0 ? 0 : budget_cycles};
+  cudaError_t e = cudaMemcpyToSymbol(hodlr::g_wait_fault, &wf, sizeof wf);
+  if (e != cudaSuccess) return hodlr::set_last_error(HODLR_ERR_CUDA, cudaGetErrorString(e));
+  return HODLR_OK;
+}

@@ -2,28 +2,28 @@
 // hodlr_gemm_reduce, for callers that are not allowed to allocate device
 // memory.
 //
-// Who cannot allocate: code that runs while a CUDA stream is being captured
-// into a graph (cudaMalloc is not a stream operation and breaks or
-// serialises the capture), callers whose framework owns the whole device
-// through its own caching allocator and forbids side allocations, and
-// latency-critical loops that cannot afford the implicit device-wide
-// synchronisation cudaMalloc / cudaFree can cause.  hodlr_gemm_reduce needs
-// scratch for its split-K partial sums and per-partition blocks and takes it
-// with cudaMalloc; this variant takes the same scratch from one fixed device
-// array instead.
+// Who cannot allocate: callers whose framework owns the whole device through
+// its own caching allocator and forbids side allocations, and latency-critical
+// loops that cannot afford the implicit device-wide synchronisation
+// cudaMalloc / cudaFree can cause.  hodlr_gemm_reduce needs scratch for its
+// split-K partial sums and per-partition blocks and takes it with cudaMalloc;
+// this variant takes the same scratch from one fixed device array instead.
+// It runs on the legacy default stream and synchronises with it before it
+// returns, so it is a call for ordinary (uncaptured) host code.
 //
 // The scratch is a file-scope __device__ array of kNoAllocDoubles doubles
 // (16 MiB): every GPU that loads this library holds it until the process
 // exits.  Host code cannot use the array's name as a device address (on the
 // host it names a host-side shadow), so the first call on each device looks
 // the address up with cudaGetSymbolAddress while that device is current and
-// caches it; that first call should therefore be made before any stream
-// capture.  Every call on a device shares the one array: calls whose work
-// overlaps on the GPU (concurrent streams, other host threads) race on it.
-// The kernels write every scratch entry they later read (partial sums and
-// blocks are stored, never accumulated), so the contents left by a previous
-// call need no clearing.  Sizes whose scratch would exceed the array are
-// rejected with HODLR_ERR_INVALID_ARG.
+// caches it.  cudaDeviceReset unloads the library's device code, which makes
+// the cached address stale: a process that resets a device must not call this
+// function on that device afterwards.  Every call on a device shares the one
+// array: calls whose work overlaps on the GPU (concurrent streams, other host
+// threads) race on it.  The kernels write every scratch entry they later read
+// (partial sums and blocks are stored, never accumulated), so the contents
+// left by a previous call need no clearing.  Sizes whose scratch would exceed
+// the array are rejected with HODLR_ERR_INVALID_ARG.
 #include <mutex>
 
 #include "kernels.cuh"

@@ -259,17 +259,17 @@ HODLR_API int hodlr_checkpoint_load(const void *buf, int64_t bytes, void *stream
 HODLR_API int hodlr_gemm_reduce(int nrow, int nPart, int ncolV, int ncolU, const double *V, int64_t ldv,
                                 const double *U, int64_t ldu, double *W, int64_t ldw);
 
-/* hodlr_gemm_reduce for callers that may not allocate device memory (code
- * running inside stream capture, frameworks that own the device through
- * their own allocator, loops that cannot absorb cudaMalloc's
- * synchronisation).  No counterpart in the reference.  Same arguments and
- * result; its scratch is a fixed 16 MiB device array inside the library
- * (2^21 doubles, held on every GPU that loads the library) instead of
- * cudaMalloc.  nPart*ncolV*ncolU plus the split-K partial sums must fit that
- * array, else HODLR_ERR_INVALID_ARG.  The first call on a device looks up the
- * array's address (make it before any stream capture); calls that overlap
- * on the GPU share the array and race.  Legacy default stream, returns when
- * W is written. */
+/* hodlr_gemm_reduce for callers that may not allocate device memory
+ * (frameworks that own the device through their own allocator, loops that
+ * cannot absorb cudaMalloc's synchronisation).  No counterpart in the
+ * reference.  Same arguments and result; its scratch is a fixed 16 MiB device
+ * array inside the library (2^21 doubles, held on every GPU that loads the
+ * library) instead of cudaMalloc.  nPart*ncolV*ncolU plus the split-K partial
+ * sums must fit that array, else HODLR_ERR_INVALID_ARG.  The first call on a
+ * device looks up the array's address and caches it (not valid after
+ * cudaDeviceReset on that device); calls that overlap on the GPU share the
+ * array and race.  Runs on the legacy default stream and returns when W is
+ * written. */
 HODLR_API int hodlr_gemm_reduce_noalloc(int nrow, int nPart, int ncolV, int ncolU, const double *V,
                                         int64_t ldv, const double *U, int64_t ldu, double *W, int64_t ldw);
 
@@ -411,14 +411,16 @@ HODLR_API int hodlr_set_tuning(hodlr_handle h, const hodlr_tuning *t);
 HODLR_API int hodlr_get_tuning(hodlr_handle h, hodlr_tuning *t);
 HODLR_API int hodlr_batch_autotune(hodlr_batch b, hodlr_tuning *per_forest, int capacity);
 
-/* Measured FP32 and FP64 FMA throughput of the current GPU (TFLOP/s, eight
- * independent FMA chains per thread, best of two timed runs) -- the
- * denominators of the roofline fractions of the CUDA-core kernels.  No
- * counterpart in the reference.  Legacy default stream; synchronous. */
-HODLR_API int hodlr_probe_fp_peaks(double *ffma_tflops, double *dfma_tflops);
-/* Measured rate of the warp-level bf16 MMA (mma.sync m16n8k16, FP32
- * accumulate) that the tensor-core residual runs on (TFLOP/s). */
-HODLR_API int hodlr_probe_mma_bf16(double *tflops);
+/* Test hook of the bounded device waits (no counterpart in the reference,
+ * whose CPU tasks have no device waits).  While set (cta >= 0), CTA `cta` of
+ * every launch of the FP32 row-reduction kernel (the TMA-fed V^T X of the
+ * mixed path) does not issue the copies of its stage `stage`, so its wait on
+ * that stage ends only by a clock budget of `budget_cycles` SM cycles
+ * (1 .. 1e9; 0 = the default of 1e9): the CTA records HODLR_ERR_TIMEOUT with
+ * its index in the handle's status word, waits (bounded) for its copies in
+ * flight and returns, and the call reports the error.  cta = -1 switches the
+ * hook off.  Affects the current device; no allocation, synchronous. */
+HODLR_API int hodlr_debug_wait_fault(int cta, int stage, long long budget_cycles);
 
 /* Kernels launched by this library since load (for launch accounting). */
 HODLR_API int64_t hodlr_kernel_launches(void);

@@ -1,7 +1,10 @@
 """Build recipe for the oracle (TEST INFRASTRUCTURE ONLY).
 
 * ``libhodlr_oracle.so`` -- the C restatement in ``hodlr_oracle.c``; built on
-  any machine with gcc (x86_64 here, aarch64 on the GPU host).
+  any machine with gcc (x86_64 or aarch64).
+* ``libhsolve_blas.so`` -- ``hsolve_blas.c``: hsolve restated with the BLAS
+  calls it makes, bound at run time to scipy's bundled OpenBLAS, and its
+  threaded form (the CPU baseline); built on any machine with gcc.
 * ``_ref/libhsolve_ref.so`` -- fastSolver2's own ``hsolve``
   (src/tasks/leaf_solve.cc:73-154) compiled verbatim.  The lines are streamed
   out of the read-only reference checkout with ``sed`` straight into g++
@@ -17,11 +20,13 @@ import subprocess
 import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF_ROOT = "/root/reference"
+# where the fastSolver2 checkout lives (read only); FASTSOLVER2_REFERENCE overrides
+REF_ROOT = os.environ.get("FASTSOLVER2_REFERENCE", "/root/reference")
 REF_FILE = os.path.join(REF_ROOT, "src", "tasks", "leaf_solve.cc")
 HSOLVE_LINES = (73, 154)
 
 ORACLE_SO = os.path.join(HERE, "libhodlr_oracle.so")
+BLAS_SO = os.path.join(HERE, "libhsolve_blas.so")
 REF_SO = os.path.join(HERE, "_ref", "libhsolve_ref.so")
 
 
@@ -40,6 +45,21 @@ def build_oracle(force=False):
         subprocess.check_call(cmd)
         os.replace(ORACLE_SO + ".tmp", ORACLE_SO)
     return ORACLE_SO
+
+
+def build_blas_port(force=False):
+    src = os.path.join(HERE, "hsolve_blas.c")
+    if force or _stale(BLAS_SO, [src, __file__]):
+        cmd = ["gcc", "-O2", "-ffp-contract=off", "-fPIC", "-shared", "-pthread",
+               "-fvisibility=hidden", src, "-o", BLAS_SO + ".tmp", "-ldl", "-lm"]
+        subprocess.check_call(cmd)
+        os.replace(BLAS_SO + ".tmp", BLAS_SO)
+    return BLAS_SO
+
+
+def scipy_openblas():
+    """Path of scipy's bundled OpenBLAS, or None."""
+    return _scipy_openblas()
 
 
 def _scipy_openblas():
@@ -83,6 +103,7 @@ def build_reference(force=False):
 
 def build(force=False):
     build_oracle(force)
+    build_blas_port(force)
     try:
         build_reference(force)
     except (subprocess.CalledProcessError, OSError) as e:  # reference is optional

@@ -15,6 +15,7 @@ from . import build as _build
 
 _lib = None
 _ref = None
+_blas = None
 
 _dp = ctypes.POINTER(ctypes.c_double)
 _ip = ctypes.POINTER(ctypes.c_int)
@@ -80,6 +81,38 @@ def ref_lib():
                                  _dp, _dp, _dp]
         _ref = R
     return _ref
+
+
+def blas_lib():
+    """libhsolve_blas.so bound to scipy's OpenBLAS (single-threaded BLAS), or
+    None where that BLAS is absent."""
+    global _blas
+    if _blas is None:
+        path = _build.BLAS_SO
+        if not os.path.exists(path):
+            _build.build_blas_port()
+        blas = _build.scipy_openblas()
+        if blas is None:
+            return None
+        B = ctypes.CDLL(path)
+        B.hb_init.argtypes = [ctypes.c_char_p]
+        B.hb_init.restype = ctypes.c_int
+        if B.hb_init(blas.encode()) != 0:
+            return None
+        B.hb_hsolve.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                _dp, _dp, _dp]
+        B.hb_hsolve.restype = ctypes.c_int
+        B.hb_hsolve_mt.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, _dp, _i64, ctypes.POINTER(_dp),
+                                   _i64, ctypes.c_int, _dp, _i64, ctypes.c_int]
+        B.hb_hsolve_mt.restype = ctypes.c_int
+        B.hb_matvec_mt.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, _dp, _i64, ctypes.POINTER(_dp),
+                                   _i64, ctypes.POINTER(_dp), _i64, ctypes.POINTER(_dp), ctypes.c_int, _dp, _i64,
+                                   _dp, _i64, ctypes.c_int]
+        B.hb_copy_mt.argtypes = [ctypes.c_void_p, ctypes.c_void_p, _i64, ctypes.c_int]
+        B.hb_fill_gaussian.argtypes = [_dp, _i64, _i64, _i64, ctypes.c_uint64, ctypes.c_double, ctypes.c_double,
+                                       _i64, ctypes.c_int]
+        _blas = B
+    return _blas
 
 
 def _p(a):
@@ -231,3 +264,60 @@ def hodlr_matvec(prob, X):
     lib().orc_hodlr_matvec(m, L, r, _p(K), _ld(K), _ptr_array(Us), ld, _ptr_array(Vs), ld, sp,
                            X.shape[1], _p(X), _ld(X), _p(Y), _ld(Y))
     return Y
+
+
+# ---------------------------------------------------------------- BLAS-backed restatement
+
+def blas_hsolve(nrow, nrhs, rank, nPart, K, U, V):
+    """In-place hsolve (src/tasks/leaf_solve.cc:73-154) with its dgemm_/dgesv_
+    calls on scipy's OpenBLAS.  Returns INFO, or None without that BLAS."""
+    B = blas_lib()
+    if B is None:
+        return None
+    LD = _ld(K)
+    assert _ld(U) == LD and _ld(V) == LD
+    return B.hb_hsolve(nrow, nrhs, rank, nPart, LD, _p(K), _p(U), _p(V))
+
+
+def blas_hsolve_mt(leaf, levels, rank, K, Vs, W, nrhs, nthreads):
+    """In-place threaded hsolve with per-level V (hb_hsolve_mt): K (N x m
+    stacked leaf blocks) becomes the leaf LU, W = [B | U^(0) | ...] becomes
+    [X | Utilde^(0) | ...].  Returns 0, 1 (singular leaf) or 2 (singular
+    capacitance system)."""
+    B = blas_lib()
+    assert B is not None, "scipy's OpenBLAS is not available"
+    ldv = _ld(Vs[0]) if levels else K.shape[0]
+    return B.hb_hsolve_mt(leaf, levels, rank, _p(K), _ld(K), _ptr_array(Vs), ldv, nrhs, _p(W), _ld(W), nthreads)
+
+
+def blas_matvec(leaf, levels, rank, K, Us, Vs, ss, X, nthreads=None):
+    """Y = A X in FP64 from the exact representation, threaded (hb_matvec_mt)."""
+    B = blas_lib()
+    assert B is not None, "scipy's OpenBLAS is not available"
+    X = np.asfortranarray(X)
+    Y = np.empty_like(X, order="F")
+    ld = _ld(Us[0]) if levels else X.shape[0]
+    sp = _ptr_array(ss) if ss is not None else None
+    B.hb_matvec_mt(leaf, levels, rank, _p(K), _ld(K), _ptr_array(Us), ld, _ptr_array(Vs), ld, sp, X.shape[1],
+                   _p(X), _ld(X), _p(Y), _ld(Y), nthreads or (os.cpu_count() or 1))
+    return Y
+
+
+def copy_mt(dst, src, nthreads=None):
+    """dst[...] = src for two contiguous arrays of the same size, threaded."""
+    assert dst.nbytes == src.nbytes
+    B = blas_lib()
+    if B is None:
+        np.copyto(dst, src)
+        return
+    B.hb_copy_mt(dst.ctypes.data, src.ctypes.data, dst.nbytes, nthreads or (os.cpu_count() or 1))
+
+
+def fill_gaussian(A, seed, scale=1.0, diag=0.0, diag_block=0, nthreads=None):
+    """Fill the Fortran-ordered 2-D array A in place with seeded N(0, scale^2)
+    values, plus `diag` on the diagonal of each diag_block x diag_block square
+    of rows (the leaf blocks of a KTree region); threaded (hb_fill_gaussian)."""
+    B = blas_lib()
+    assert B is not None, "scipy's OpenBLAS is not available"
+    B.hb_fill_gaussian(_p(A), A.shape[0], A.shape[1], _ld(A), seed, scale, diag, diag_block,
+                       nthreads or (os.cpu_count() or 1))

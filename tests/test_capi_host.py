@@ -122,3 +122,12 @@ def test_padding_calls_reject_bad_sizes_on_host(fs):
     assert L.hodlr_unpad_rows(2, zero, 8, 1, buf, 16, buf, 16, None) == fs.HODLR_ERR_INVALID_ARG
     assert L.hodlr_pad_leaf_blocks(0, zero, 8, buf, buf, None) == fs.HODLR_ERR_INVALID_ARG
     assert L.hodlr_pad_leaf_blocks(2, bad, 8, None, buf, None) == fs.HODLR_ERR_INVALID_ARG
+
+
+def test_wait_fault_hook_rejects_bad_arguments_on_host(fs):
+    L = fs.lib()
+    assert L.hodlr_debug_wait_fault(-2, 0, 0) == fs.HODLR_ERR_INVALID_ARG
+    assert L.hodlr_debug_wait_fault(0, -1, 1000) == fs.HODLR_ERR_INVALID_ARG
+    assert L.hodlr_debug_wait_fault(0, 0, -5) == fs.HODLR_ERR_INVALID_ARG
+    assert L.hodlr_debug_wait_fault(0, 0, 2 * 10**9) == fs.HODLR_ERR_INVALID_ARG
+    assert b"wait_fault" in L.hodlr_last_error_string()

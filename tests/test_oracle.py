@@ -146,3 +146,67 @@ def test_edge_single_leaf(oracle_lib):
     X, _, info = O.hsolve_general(pr, pr.B)
     assert info == 0
     assert rel(X, np.linalg.solve(pr.K, pr.B)) < 1e-13
+
+
+# ------------------------------------------------ the BLAS-backed restatement
+def _need_blas():
+    if O.blas_lib() is None:
+        pytest.skip("scipy's OpenBLAS not available")
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_blas_hsolve_matches_golden(oracle_lib, name):
+    """hsolve with its dgemm_/dgesv_ calls on OpenBLAS (the CPU baseline's
+    arithmetic) reproduces the fixtures of the verbatim reference build."""
+    _need_blas()
+    g = np.load(os.path.join(GOLDEN, name + ".npz"))
+    m, L, r, k = int(g["leaf"]), int(g["levels"]), int(g["rank"]), int(g["nrhs"])
+    pr = P.reference_problem(m, L, r, nrhs=k, master=int(g["master"]), offset=int(g["offset"]))
+    K, W, V = np.array(pr.K, order="F"), ref_region(pr), np.array(pr.V[0], order="F")
+    assert O.blas_hsolve(pr.n, k, r, 1 << L, K, W, V) == 0
+    assert rel(W[:, :k], g["x"]) < 1e-13
+
+
+@pytest.mark.parametrize("m,L,r,k", [(16, 2, 3, 1), (64, 3, 8, 1), (32, 4, 4, 5), (128, 4, 16, 3)])
+def test_blas_hsolve_is_bitwise_the_verbatim_reference(oracle_lib, m, L, r, k):
+    """Same calls in the same order on the same BLAS: the same bits as the
+    reference's own hsolve compiled against that BLAS."""
+    _need_blas()
+    if O.ref_lib() is None:
+        pytest.skip("reference checkout not mounted here")
+    pr = P.reference_problem(m, L, r, nrhs=k, master=777 + m)
+    K1, W1, V = np.array(pr.K, order="F"), ref_region(pr), np.array(pr.V[0], order="F")
+    K2, W2 = K1.copy(order="F"), W1.copy(order="F")
+    O.ref_hsolve(pr.n, k, r, 1 << L, K1, W1, V)
+    assert O.blas_hsolve(pr.n, k, r, 1 << L, K2, W2, V) == 0
+    np.testing.assert_array_equal(W1, W2)
+    np.testing.assert_array_equal(K1, K2)
+
+
+@pytest.mark.parametrize("nthreads", [1, 2, 8])
+def test_blas_hsolve_mt_matches_oracle(oracle_lib, nthreads):
+    """The threaded baseline (subtrees per thread, then row-chunked top
+    levels) against the oracle's generalised recursion, per-level factors."""
+    _need_blas()
+    pr = P.gaussian_problem(32, 5, 6, nrhs=3, seed=5)
+    X0, _, info = O.hsolve_general(pr, pr.B)
+    assert info == 0
+    L, r, k = pr.levels, pr.rank, pr.nrhs
+    K = np.array(pr.K, order="F")
+    W = np.zeros((pr.n, k + L * r), order="F")
+    W[:, :k] = pr.B
+    for l in range(L):
+        W[:, k + l * r:k + (l + 1) * r] = pr.U[l]
+    Vs = [np.asfortranarray(v) for v in pr.V]
+    assert O.blas_hsolve_mt(pr.leaf, L, r, K, Vs, W, k, nthreads) == 0
+    assert rel(W[:, :k], X0) < 1e-12
+
+
+@pytest.mark.parametrize("nthreads", [1, 4, 16])
+def test_blas_matvec_matches_oracle(oracle_lib, nthreads):
+    _need_blas()
+    pr = P.gaussian_problem(16, 5, 4, nrhs=3, seed=9, decay=2.0)
+    Y0 = O.hodlr_matvec(pr, pr.B)
+    Y = O.blas_matvec(pr.leaf, pr.levels, pr.rank, np.asfortranarray(pr.K), pr.U, pr.V, pr.s,
+                      np.asfortranarray(pr.B), nthreads)
+    assert rel(Y, Y0) < 1e-13

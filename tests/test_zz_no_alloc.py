@@ -1,12 +1,13 @@
 """hodlr_gemm_reduce_noalloc -- the reduction for callers that cannot
 allocate device memory -- checked against hodlr_gemm_reduce through the C ABI.
 
-Callers inside CUDA stream capture, or under a framework allocator that owns
-the device, cannot call cudaMalloc; this entry point takes its scratch from a
-fixed 16 MiB device array in the library instead.  Two calls in a row with
-different shapes check that the shared scratch carries nothing stale from one
-call into the next.  This file sorts last so that a stop-at-first-failure run
-has already run every other test.
+Callers under a framework allocator that owns the device, or in loops that
+cannot absorb cudaMalloc's synchronisation, cannot call cudaMalloc; this entry
+point takes its scratch from a fixed 16 MiB device array in the library
+instead.  Two calls in a row with different shapes check that the shared
+scratch carries nothing stale from one call into the next, and the device's
+free memory is checked to stay put across calls.  This file sorts last so that
+a stop-at-first-failure run has already run every other test.
 """
 import ctypes
 
@@ -42,6 +43,27 @@ def test_noalloc_matches_allocating_entry_point(hodlr, first, second):
         a, b = Wn.cpu().numpy(), Wr.cpu().numpy()
         assert np.isfinite(a).all()
         np.testing.assert_allclose(a, b, rtol=1e-13, atol=1e-13 * np.abs(b).max())
+
+
+def test_noalloc_allocates_no_device_memory(hodlr):
+    """After the first call (which may load the library's device code, and
+    with it the fixed array), further calls leave the device's free memory
+    exactly where it was: cudaMalloc hands out whole pages, so any allocation
+    would show."""
+    nrow, nPart, ncolV, ncolU = 1 << 17, 8, 32, 64
+    V, U = _col(nrow, ncolV, 3), _col(nrow, ncolU, 4)
+    W = torch.zeros((ncolU, nPart * ncolV), dtype=torch.float64, device="cuda").t()
+    f = hodlr.lib().hodlr_gemm_reduce_noalloc
+    args = (nrow, nPart, ncolV, ncolU, ctypes.c_void_p(V.data_ptr()), V.stride(1), ctypes.c_void_p(U.data_ptr()),
+            U.stride(1), ctypes.c_void_p(W.data_ptr()), W.stride(1))
+    assert f(*args) == hodlr.HODLR_OK
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info()
+    for _ in range(3):
+        assert f(*args) == hodlr.HODLR_OK
+    torch.cuda.synchronize()
+    free1, _ = torch.cuda.mem_get_info()
+    assert free1 == free0, (free0, free1)
 
 
 def test_noalloc_rejects_sizes_beyond_its_scratch(hodlr):
