@@ -156,6 +156,9 @@ struct hodlr_ctx {
   // skips its own leaf LU and takes over that status
   DevStatus *dst_leaf = nullptr;
   bool leaves_prefactored = false;
+  // mixed mode, leaf 128: the factorisation forms only the leaf inverses the
+  // sweeps apply; LU32 / ipiv are formed on request (ensure_leaf_lu)
+  bool lu_stale = false;
   float factor_ms = 0.f, solve_ms = 0.f;
   // graphs
   bool use_graphs = true;
@@ -464,6 +467,33 @@ static int cap_apply(hodlr_ctx *h, int l, int C, long long tb_stride, bool trans
   return HODLR_OK;
 }
 
+// The mixed path at leaf 128 factors its leaves by the blocked Gauss-Jordan
+// kernel, which forms the explicit inverses only.
+static bool leaf_inverse_only(const hodlr_ctx *h) { return h->mixed && h->m == 128 && h->Dinv32; }
+
+static cudaError_t launch_mixed_leaf_factor(hodlr_ctx *h, DevStatus *st, cudaStream_t s) {
+  const int m = h->m;
+  const long long mm = (long long)m * m;
+  if (leaf_inverse_only(h)) return launch_leaf_gj_inverse_f32(h->D, m, mm, m, h->nleaf, st, h->Dinv32, s);
+  float *Dinv = h->Dinv32;
+  const bool fused = Dinv && leaf_getrf_fused_inverse(m, sizeof(float));
+  cudaError_t e = launch_leaf_getrf<float>(h->D, m, mm, h->LU32, h->ipiv, m, h->nleaf, st, fused ? Dinv : nullptr, s);
+  if (e == cudaSuccess && Dinv && !fused) e = launch_leaf_inverse<float>(h->LU32, h->ipiv, m, h->nleaf, Dinv, s);
+  return e;
+}
+
+// The leaf LU factors and pivots of a factored mixed handle whose
+// factorisation formed only the inverses: formed now, from the leaf blocks.
+static int ensure_leaf_lu(hodlr_ctx *h) {
+  if (!h->lu_stale) return HODLR_OK;
+  CKS(reset_status(h));
+  CK(launch_leaf_getrf<float>(h->D, h->m, (long long)h->m * h->m, h->LU32, h->ipiv, h->m, h->nleaf, h->dst, nullptr,
+                              h->st));
+  CKS(sync_status(h, nullptr));
+  h->lu_stale = false;
+  return HODLR_OK;
+}
+
 // Factorisation sweep: leaf LU (+ explicit leaf inverses), Ut = D^{-1} U
 // (all levels at once), then for depth L-1 .. 0: T = V^T [Ut_d | Ut_u],
 // capacitance LU + inverse, eta = Sinv [s.T1d; s.T0d], Ut_d -= Ut_u eta.
@@ -477,9 +507,14 @@ template <typename T> static int factor_sweep(hodlr_ctx *h, bool leaves_done = f
   T *Dinv = Dinvptr<T>(h);
   const bool fused = Dinv && leaf_getrf_fused_inverse(m, sizeof(T));
   if (!leaves_done) {
-    PHASE(h, HODLR_PHASE_LEAF_LU,
-          launch_leaf_getrf<T>(h->D, m, (long long)m * m, LU, h->ipiv, m, h->nleaf, h->dst, fused ? Dinv : nullptr, s));
-    if (Dinv && !fused) PHASE(h, HODLR_PHASE_LEAF_LU, launch_leaf_inverse<T>(LU, h->ipiv, m, h->nleaf, Dinv, s));
+    if (sizeof(T) == 4) {
+      PHASE(h, HODLR_PHASE_LEAF_LU, launch_mixed_leaf_factor(h, h->dst, s));
+    } else {
+      PHASE(h, HODLR_PHASE_LEAF_LU,
+            launch_leaf_getrf<T>(h->D, m, (long long)m * m, LU, h->ipiv, m, h->nleaf, h->dst, fused ? Dinv : nullptr,
+                                 s));
+      if (Dinv && !fused) PHASE(h, HODLR_PHASE_LEAF_LU, launch_leaf_inverse<T>(LU, h->ipiv, m, h->nleaf, Dinv, s));
+    }
   }
   if (L == 0) return HODLR_OK;
   if (sizeof(T) == 4 && Dinv && m == 128) {
@@ -1210,12 +1245,8 @@ int hodlr_set_leaf_blocks(hodlr_handle h, const double *D, int64_t ld, int64_t l
     if (h->mixed && ps != h->st) {
       // the leaf LU (+ inverses) depends on the leaf blocks alone: it runs on
       // the side stream while the low-rank inputs are still being copied
-      float *Dinv = h->Dinv32;
-      const bool fused = Dinv && leaf_getrf_fused_inverse(m, sizeof(float));
       CK(cudaMemsetAsync(h->dst_leaf, 0, sizeof(DevStatus), ps));
-      CK(launch_leaf_getrf<float>(h->D, m, mm, h->LU32, h->ipiv, m, h->nleaf, h->dst_leaf, fused ? Dinv : nullptr,
-                                  ps));
-      if (Dinv && !fused) CK(launch_leaf_inverse<float>(h->LU32, h->ipiv, m, h->nleaf, Dinv, ps));
+      CK(launch_mixed_leaf_factor(h, h->dst_leaf, ps));
       h->leaves_prefactored = true;
     }
     return HODLR_OK;
@@ -1268,6 +1299,7 @@ int hodlr_factor(hodlr_handle h) {
   CKS(fst);
   cudaEventElapsedTime(&h->factor_ms, h->ev[0], h->ev[1]);
   h->factored = true;
+  h->lu_stale = leaf_inverse_only(h);
   return HODLR_OK;
 }
 
@@ -1424,6 +1456,7 @@ int hodlr_get_factors(hodlr_handle h, double *leaf_lu, int32_t *leaf_ipiv, doubl
   const long long n = h->n;
   const int m = h->m, L = h->L, r = h->r;
   cudaStream_t s = h->st;
+  if (leaf_lu || leaf_ipiv) CKS(ensure_leaf_lu(h));
   if (leaf_lu) {
     if (h->mixed)
       CK((launch_convert<float, double>(h->LU32, (long long)h->nleaf * m * m, leaf_lu, (long long)h->nleaf * m * m,
@@ -1624,6 +1657,7 @@ int hodlr_hsolve_ex(int nrow, int nrhs, int rank, int nPart, int LD, double *K, 
   if ((rc = hodlr_solve(h, dU, ld, nrhs, info)) != HODLR_OK) return fail(rc);
   // write back: K <- leaf LU (stacked, ld), U columns nrhs.. <- Utilde
   cudaStream_t s = h->st;
+  if ((rc = ensure_leaf_lu(h)) != HODLR_OK) return fail(rc);
   {
     cudaError_t e = h->mixed ? launch_unpack_leaves<float>(h->LU32, dK, ld, m, m, h->nleaf, s)
                              : launch_unpack_leaves<double>(h->LU, dK, ld, m, m, h->nleaf, s);
@@ -2654,6 +2688,7 @@ int hodlr_checkpoint_save(hodlr_handle h, void *buf, int64_t bytes) {
   if (!buf) return set_err(HODLR_ERR_INVALID_ARG, "null buffer");
   CKS(join_prep(h));  // the side stream may still be writing the leaf factors
   if (bytes < need) return set_err(HODLR_ERR_INVALID_ARG, "checkpoint buffer too small");
+  if (h->factored) CKS(ensure_leaf_lu(h));
   CK(cudaStreamSynchronize(h->st));
   unsigned char *out = static_cast<unsigned char *>(buf);
   unsigned char *p = out + sizeof(CkHeader);

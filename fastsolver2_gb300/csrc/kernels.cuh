@@ -33,6 +33,11 @@ struct TuningScope {
 // Dinv (may be NULL): also write the explicit inverses, formed from the
 // factors while they are still in shared memory (leaf_getrf_fused_inverse).
 bool leaf_getrf_fused_inverse(int m, int elem_bytes);
+// FP32 explicit inverses of nleaf leaf blocks of 128 rows (FP64 source in
+// the layout of launch_leaf_getrf) by blocked Gauss-Jordan with implicit row
+// pivoting; no LU factors.  A zero pivot is reported as HODLR_ERR_SINGULAR_LEAF.
+cudaError_t launch_leaf_gj_inverse_f32(const double *D, long long d_ld, long long d_stride, int m, int nleaf,
+                                       DevStatus *st, float *Dinv, cudaStream_t s);
 template <typename T>
 cudaError_t launch_leaf_getrf(const double *D, long long d_ld, long long d_stride, T *LU, int *ipiv,
                               int m, int nleaf, DevStatus *st, T *Dinv, cudaStream_t s);

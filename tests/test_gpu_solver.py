@@ -186,6 +186,78 @@ def test_mixed_refinement_reaches_tolerance(hodlr, resid):
     assert rel(X, Xo) < 1e-9
 
 
+def _check_plu(A, lu, piv, tol):
+    """P A = L U for one leaf: lu column-major (LAPACK layout), piv 1-based."""
+    m = A.shape[0]
+    Lf = np.tril(lu, -1) + np.eye(m)
+    Uf = np.triu(lu)
+    PA = np.array(A, copy=True)
+    for i in range(m):
+        p = piv[i] - 1
+        PA[[i, p]] = PA[[p, i]]
+    assert np.linalg.norm(PA - Lf @ Uf) / np.linalg.norm(A) < tol
+    for k in range(m):  # partial pivoting: |L| <= 1
+        assert np.abs(Lf[k + 1:, k]).max(initial=0.0) <= 1.0 + 1e-6
+
+
+@pytest.mark.parametrize("transpose", [False, True])
+def test_mixed_leaf128_inverse_and_factors_on_request(hodlr, transpose):
+    """Leaf 128 in the mixed mode: the factorisation forms the FP32 leaf
+    inverses by blocked Gauss-Jordan (no LU); solves refine to 1e-12 against
+    a dense FP64 solve, forward and transposed; the leaf LU factors and
+    pivots, asked for afterwards, are formed then and satisfy P A = L U."""
+    pr = P.gaussian_problem(128, 3, 16, nrhs=3, seed=23, shift=1.5)
+    s = make_solver(hodlr, pr, precision=hodlr.PREC_MIXED, refine_tol=1e-12)
+    s.factor()
+    B = to_dev(pr.B)
+    info = s.solve(B, transpose=transpose)
+    assert info.rel_residual <= 1e-12
+    A = pr.dense()
+    Xd = np.linalg.solve(A.T if transpose else A, pr.B)
+    assert rel(to_host(B), Xd) < 1e-9
+    nleaf = 1 << pr.levels
+    lu = torch.empty(nleaf * 128 * 128, dtype=torch.float64, device="cuda")
+    piv = torch.empty(pr.n, dtype=torch.int32, device="cuda")
+    s.get_factors(leaf_lu=lu, leaf_ipiv=piv)
+    lu = lu.cpu().numpy().reshape(nleaf, 128, 128)
+    piv = piv.cpu().numpy().reshape(nleaf, 128)
+    for i in range(nleaf):
+        _check_plu(pr.leaf_block(i), lu[i].T, piv[i], 1e-5)
+
+
+def test_mixed_hsolve_leaf128_writes_back_leaf_lu(hodlr):
+    """The drop-in entry point in the mixed mode at leaf 128 leaves the leaf
+    LU factors in K (dgesv's layout) as the FP64 path does: L U equals the
+    leaf block up to a row permutation, in FP32 accuracy."""
+    pr = P.reference_problem(128, 3, 8, nrhs=2, master=99)
+    N, L, r, k = pr.n, pr.levels, pr.rank, pr.nrhs
+    W = np.zeros((N, k + L * r), order="F")
+    W[:, :k] = pr.B
+    for l in range(L):
+        W[:, k + l * r:k + (l + 1) * r] = pr.U[0]
+    Kd, Wd, Vd = to_dev(pr.K), to_dev(W), to_dev(np.asfortranarray(pr.V[0]))
+    info = hodlr.hsolve(N, k, r, 1 << L, N, Kd, Wd, Vd, precision=hodlr.PREC_MIXED)
+    assert info.rel_residual <= 1e-12
+    K = to_host(Kd)
+    for i in range(1 << L):
+        lu = K[i * 128:(i + 1) * 128]
+        prod = (np.tril(lu, -1) + np.eye(128)) @ np.triu(lu)
+        Pm = prod @ np.linalg.inv(pr.leaf_block(i))   # a permutation matrix, up to FP32 rounding
+        Pr = np.rint(Pm)
+        assert np.abs(Pm - Pr).max() < 1e-4
+        assert (Pr.sum(axis=0) == 1).all() and (Pr.sum(axis=1) == 1).all() and (Pr >= 0).all()
+
+
+def test_mixed_leaf128_singular_leaf_reported(hodlr):
+    pr = P.gaussian_problem(128, 2, 8, nrhs=1, seed=4)
+    pr.K[3 * 128:4 * 128, 5] = 0.0   # leaf 3: a zero column
+    s = make_solver(hodlr, pr, precision=hodlr.PREC_MIXED)
+    with pytest.raises(hodlr.HodlrError) as e:
+        s.factor()
+    assert e.value.code == hodlr.HODLR_ERR_SINGULAR_LEAF
+    assert "(index 3)" in str(e.value)
+
+
 @pytest.mark.parametrize("precision", [0, 1])
 def test_transpose_solve(hodlr, precision):
     pr = P.gaussian_problem(64, 4, 8, nrhs=3, seed=21, orthonormal=True, decay=3.0, shift=2.0)
