@@ -58,6 +58,20 @@ bool make_tensor_map_f32(CUtensorMap *map, const float *base, long long rows, lo
            CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
+bool make_tensor_map_f32_rowblocks(CUtensorMap *map, const float *base, long long rows, long long cols, long long ld,
+                                   int row_blocks, int box_cols) {
+  EncodeTiledFn f = encode_fn();
+  if (!f || !base || rows < 32 || rows % 32 || cols < 1) return false;
+  if ((reinterpret_cast<uintptr_t>(base) & 15) || (ld * 4) % 16 || ld < rows) return false;
+  cuuint64_t dims[3] = {32, (cuuint64_t)(rows / 32), (cuuint64_t)cols};
+  cuuint64_t strides[2] = {128, (cuuint64_t)ld * 4};
+  cuuint32_t box[3] = {32, (cuuint32_t)row_blocks, (cuuint32_t)box_cols};
+  cuuint32_t es[3] = {1, 1, 1};
+  return f(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<float *>(base), dims, strides, box, es,
+           CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+           CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
 bool make_tensor_map_bf16(CUtensorMap *map, const void *base, long long inner, long long outer, long long ld,
                           int box_inner, int box_outer, int swizzle_bytes) {
   EncodeTiledFn f = encode_fn();
@@ -171,16 +185,8 @@ reduce_tn_kernel(const T *__restrict__ A, long long lda, const T *__restrict__ X
 // of 32, 16-byte aligned bases and leading dimensions.
 static constexpr int kTmaStages = 4;
 
-// Test hook of the bounded waits (set by hodlr_debug_wait_fault, off in
-// normal use): CTA `cta` of every reduce_tma_kernel launch does not issue the
-// copies of its stage `stage`, so nothing ever completes that stage's
-// mbarrier phase and the CTA's wait on it can only end by its clock budget,
-// `budget` cycles for that CTA (0 = the default budget; every other CTA keeps
-// the default).
-struct WaitFault {
-  int cta, stage;
-  long long budget;
-};
+// Test hook of the bounded waits (struct WaitFault, kernels.cuh), this
+// kernel's copy.
 __device__ WaitFault g_wait_fault = {-1, -1, 0};
 
 // Stage s of a reduce CTA: rows [row0 + 32 s, +32) of A (all ranks) and of
@@ -371,7 +377,9 @@ static void reduce_plan(long long nrows, int nbatch, int C, int target, int &nch
   if (base < target)
     nchunks = (int)std::min<long long>(ceil_div(target, base), ceil_div(nrows, 256));
   nchunks = std::max(1, nchunks);
-  chunk_rows = (int)std::min<long long>(nrows, (long long)ceil_div(ceil_div(nrows, nchunks), kRedBK) * kRedBK);
+  // chunks of whole 64-row steps where the block allows (the tensor-core kernel stages 64 rows)
+  const int step = nrows % 64 == 0 ? 64 : kRedBK;
+  chunk_rows = (int)std::min<long long>(nrows, (long long)ceil_div(ceil_div(nrows, nchunks), step) * step);
   nchunks = ceil_div(nrows, chunk_rows);
 }
 
@@ -411,8 +419,11 @@ static cudaError_t reduce_dispatch(const T *A, long long lda, const T *X, long l
     using D = typename std::remove_pointer<decltype(dst)>::type;
     bool done = false;
     cudaError_t err = cudaSuccess;
-    if constexpr (sizeof(T) == 4)
-      done = reduce_tma_try<D>(A, lda, X, ldx, nrows, nbatch, r, C, chunk_rows, nchunks, dst, skip, st, s, err);
+    if constexpr (sizeof(T) == 4) {
+      done = reduce_tc_try<D>(A, lda, X, ldx, nrows, nbatch, r, C, chunk_rows, nchunks, dst, skip, st, s, err);
+      if (!done)
+        done = reduce_tma_try<D>(A, lda, X, ldx, nrows, nbatch, r, C, chunk_rows, nchunks, dst, skip, st, s, err);
+    }
     if (done) return err;
 #define HODLR_RED(RTV, BNV) \
   err = reduce_rt<T, RTV, BNV, D>(A, lda, X, ldx, nrows, nbatch, r, C, chunk_rows, nchunks, nct, dst, skip, s)
@@ -731,6 +742,7 @@ extern "C" int hodlr_debug_wait_fault(int cta, int stage, long long budget_cycle
     return hodlr::set_last_error(HODLR_ERR_INVALID_ARG, "debug_wait_fault: bad arguments");
   const hodlr::WaitFault wf = {cta, cta < 0 ? -1 : stage, cta < 0 ? 0 : budget_cycles};
   cudaError_t e = cudaMemcpyToSymbol(hodlr::g_wait_fault, &wf, sizeof wf);
+  if (e == cudaSuccess) e = hodlr::reduce_tc_set_wait_fault(wf);
   if (e != cudaSuccess) return hodlr::set_last_error(HODLR_ERR_CUDA, cudaGetErrorString(e));
   return HODLR_OK;
 }

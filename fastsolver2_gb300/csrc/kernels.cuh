@@ -57,6 +57,24 @@ cudaError_t launch_leaf_getrs(const T *LU, const int *ipiv, int m, int nleaf, T 
 // in FP32 instead.  work: scratch of at least reduce_workspace_doubles(...)
 // doubles.
 size_t reduce_workspace_doubles(long long nrows, int nbatch, int r, int C, int elem_bytes);
+// The row reduction of FP32 operands on the tcgen05 tensor cores (rank <= 32;
+// launched when its preconditions hold, else false and nothing launched).
+template <typename OutT>
+bool reduce_tc_try(const float *V, long long ldv, const float *X, long long ldx, long long nrows, int nbatch, int r,
+                   int C, int chunk_rows, int nchunks, OutT *dst, const int *skip, DevStatus *st, cudaStream_t s,
+                   cudaError_t &err);
+
+// Test hook of the bounded waits (set by hodlr_debug_wait_fault, off in
+// normal use): CTA `cta` of every launch of the FP32 row-reduction kernels
+// does not issue the copies of its stage `stage`, so nothing ever completes
+// that stage's mbarrier phase and the CTA's wait on it can only end by its
+// clock budget, `budget` cycles for that CTA (0 = the default budget; every
+// other CTA keeps the default).  Each kernel's file holds its own device copy.
+struct WaitFault {
+  int cta, stage;
+  long long budget;
+};
+cudaError_t reduce_tc_set_wait_fault(const WaitFault &wf);
 template <typename T>
 cudaError_t launch_reduce_tn(const T *A, long long lda, const T *X, long long ldx, long long nrows,
                              int nbatch, int r, int C, double *out, double *work, const int *skip,

@@ -25,6 +25,13 @@ __device__ __forceinline__ uint64_t desc_sw64(unsigned saddr) {
          ((uint64_t)1 << 46) | ((uint64_t)4 << 61);
 }
 
+// The same with the 128-byte swizzle (rows of 128 bytes = 64 bf16, 8-row
+// atoms of 1024 bytes).
+__device__ __forceinline__ uint64_t desc_sw128(unsigned saddr) {
+  return (uint64_t)((saddr >> 4) & 0x3FFFu) | ((uint64_t)1 << 16) | ((uint64_t)(1024 >> 4) << 32) |
+         ((uint64_t)1 << 46) | ((uint64_t)2 << 61);
+}
+
 __device__ __forceinline__ void tc_alloc(unsigned *dst, unsigned ncols) {
   asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(dst)), "r"(ncols)
                : "memory");

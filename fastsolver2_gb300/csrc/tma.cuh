@@ -61,6 +61,15 @@ __device__ __forceinline__ void tma_load_2d(void *dst, const CUtensorMap *map, u
       : "memory");
 }
 
+// 3-D tile load: box at (x = innermost, y, z) into shared memory, completion
+// counted in bytes on `bar`.
+__device__ __forceinline__ void tma_load_3d(void *dst, const CUtensorMap *map, uint64_t *bar, int x, int y, int z) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];"
+      ::"r"(smem_u32(dst)), "l"(map), "r"(x), "r"(y), "r"(z), "r"(smem_u32(bar))
+      : "memory");
+}
+
 // 2-D tile store shared -> global, tracked by the bulk async-group of the
 // issuing thread.
 __device__ __forceinline__ void tma_store_2d(const CUtensorMap *map, const void *src, int x, int y) {
@@ -101,6 +110,13 @@ bool make_tensor_map_f32(CUtensorMap *map, const float *base, long long rows, lo
 // per line (line pitch `ld` elements, `outer` lines); box box_inner x
 // box_outer, swizzle 0, 32, 64 or 128 bytes.  Out-of-range elements load as
 // zero.
+// 3-D tensor map over the same column-major FP32 matrix seen as 32-row
+// blocks: (32 rows, rows / 32 blocks, cols), box (32, row_blocks, box_cols)
+// with the 128-byte swizzle -- a box of 32 * row_blocks rows whose 128-byte
+// lines (one 32-row block of one column) are swizzled as 2-D boxes of 32
+// rows are.  rows must be a multiple of 32.
+bool make_tensor_map_f32_rowblocks(CUtensorMap *map, const float *base, long long rows, long long cols, long long ld,
+                                   int row_blocks, int box_cols);
 bool make_tensor_map_bf16(CUtensorMap *map, const void *base, long long inner, long long outer, long long ld,
                           int box_inner, int box_outer, int swizzle_bytes);
 

@@ -234,8 +234,9 @@ update_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant
     const float alpha = (float)a.alpha;
     for (long long i = 0; i < nmine; ++i) {
       const int s = (int)(i % kStages), ac = (int)(i & 1);
-      if (!ws_wait(&sh->acc_full[ac], (unsigned)((i >> 1) & 1), sh)) break;
-      if (!ws_wait(&sh->full[s], (unsigned)((i / kStages) & 1), sh)) break;  // the C tile has landed
+      // warp-uniform outcomes: tcgen05.ld below is a warp-collective instruction
+      if (!__all_sync(0xffffffffu, ws_wait(&sh->acc_full[ac], (unsigned)((i >> 1) & 1), sh))) break;
+      if (!__all_sync(0xffffffffu, ws_wait(&sh->full[s], (unsigned)((i / kStages) & 1), sh))) break;  // C landed
       tc_fence_after();
       unsigned v[kBN / 32][32];
       const unsigned tl = tmem + ((unsigned)(32 * q) << 16) + (unsigned)(kBN * ac);

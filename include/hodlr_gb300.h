@@ -413,8 +413,9 @@ HODLR_API int hodlr_batch_autotune(hodlr_batch b, hodlr_tuning *per_forest, int 
 
 /* Test hook of the bounded device waits (no counterpart in the reference,
  * whose CPU tasks have no device waits).  While set (cta >= 0), CTA `cta` of
- * every launch of the FP32 row-reduction kernel (the TMA-fed V^T X of the
- * mixed path) does not issue the copies of its stage `stage`, so its wait on
+ * every launch of the FP32 row-reduction kernels (the TMA-fed V^T X of the
+ * mixed path, on the tensor cores or on the FMA pipe) does not issue the
+ * copies of its stage `stage` (counted over the CTA's launch), so its wait on
  * that stage ends only by a clock budget of `budget_cycles` SM cycles
  * (1 .. 1e9; 0 = the default of 1e9): the CTA records HODLR_ERR_TIMEOUT with
  * its index in the handle's status word, waits (bounded) for its copies in

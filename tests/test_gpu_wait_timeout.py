@@ -1,7 +1,8 @@
 """A bounded device wait that runs out (no GPU fault, no hang).
 
-The FP32 row-reduction kernel waits on an mbarrier for each stage's TMA
-copies, with a clock budget.  The test hook hodlr_debug_wait_fault makes one
+The FP32 row-reduction kernels (on the tensor cores, and on the FMA pipe with
+HODLR_NO_TCGEN05=1) wait on an mbarrier for each stage's TMA copies, with a
+clock budget.  The test hook hodlr_debug_wait_fault makes one
 CTA skip issuing one stage's copies, so nothing ever completes that wait: the
 CTA's wait ends by its (short) budget, it records HODLR_ERR_TIMEOUT with its
 index, waits for its own copies in flight and returns.  The factorisation
@@ -36,8 +37,10 @@ def solve(s, B0):
     return X, info
 
 
+@pytest.mark.parametrize("no_tc", ["0", "1"])
 @pytest.mark.parametrize("cta,stage", [(1, 0), (0, 2)])
-def test_reduce_wait_runs_out_and_reports_timeout(hodlr, cta, stage):
+def test_reduce_wait_runs_out_and_reports_timeout(hodlr, cta, stage, no_tc, monkeypatch):
+    monkeypatch.setenv("HODLR_NO_TCGEN05", no_tc)
     s, B0 = mixed_solver(hodlr)
     hodlr.debug_wait_fault(cta, stage, budget_cycles=200000)
     try:
