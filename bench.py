@@ -506,34 +506,38 @@ def run_ours(args, wl):
     F, S = algo_flops(n, m, L, r, k)
     nres = float(np.mean(iters)) + 1.0
     total_ms = sum(v[0] for v in phases.values())
-    # per-phase algorithmic work of one mixed step (FP64-equivalent flops)
+    # per-phase algorithmic work of one mixed step, split by the pipe that
+    # bounds it: (FP64 flops at this GPU's DFMA rate, FP32 flops at its FFMA
+    # rate, FP64-equivalent flops of the digit-product residual at the bf16
+    # MMA rate / 28 digit pairs); frac = that roofline time / the measured
+    # time, so a phase that mixes pipes (the capacitance step: FP64 LU, FP32
+    # inverse and application) is rated against each pipe for its own part
     nsw = float(np.mean(iters)) + 1.0        # sweeps = residual evaluations per solve
-    cap_f = sum((2 ** l) * ((2 / 3) * (2 * r) ** 3 + 2 * (2 * r) ** 3 + 2 * (2 * r) ** 2 * l * r) for l in range(L))
-    work = {
-        "leaf_lu": (2 / 3) * n * m * m + 2 * n * m * m,
-        "leaf_solve": 2 * n * m * L * r + nsw * 2 * n * m * k,
-        "reduce": sum(2 * n * r * (l + 1) * r for l in range(L)) + nsw * 2 * n * r * k * L,
-        "update": sum(2 * n * r * l * r for l in range(L)) + nsw * 2 * n * r * k * L,
-        "capacitance": cap_f + nsw * sum((2 ** l) * 2 * (2 * r) ** 2 * k for l in range(L)),
-        "resid_leaf": nsw * 2 * n * m * k,
-        "resid_reduce": nsw * 2 * n * r * k * L,
-        "resid_update": nsw * 2 * n * r * k * L,
+    cap_lu = sum((2 ** l) * (2 / 3) * (2 * r) ** 3 for l in range(L))
+    cap_fp32 = (sum((2 ** l) * (2 * (2 * r) ** 3 + 2 * (2 * r) ** 2 * l * r) for l in range(L))
+                + nsw * sum((2 ** l) * 2 * (2 * r) ** 2 * k for l in range(L)))
+    resid_pipe = {0: "fp64", 1: "dw", 2: "mma"}[args.resid]
+    work = {  # name: {pipe: flops}
+        "leaf_lu": {"fp32": (2 / 3) * n * m * m + 2 * n * m * m},
+        "leaf_solve": {"fp32": 2 * n * m * L * r + nsw * 2 * n * m * k},
+        "reduce": {"fp32": sum(2 * n * r * (l + 1) * r for l in range(L)) + nsw * 2 * n * r * k * L},
+        "update": {"fp32": sum(2 * n * r * l * r for l in range(L)) + nsw * 2 * n * r * k * L},
+        "capacitance": {"fp64": cap_lu, "fp32": cap_fp32},
+        "resid_leaf": {resid_pipe: nsw * 2 * n * m * k},
+        "resid_reduce": {resid_pipe: nsw * 2 * n * r * k * L},
+        "resid_update": {resid_pipe: nsw * 2 * n * r * k * L},
     }
-    # peaks: FP32 FFMA (measured 70 TFLOP/s); a double-word FMA costs 12 FP32
-    # instructions, so its FP64-equivalent peak is 70/12 TFLOP/s
     dw_tf = ffma_tf / 12.0   # a double-word FMA is 12 FP32 instructions
-    peak_of = {"leaf_lu": ffma_tf, "leaf_solve": ffma_tf, "reduce": ffma_tf,
-               "update": ffma_tf, "capacitance": dw_tf,
-               "resid_leaf": dw_tf if args.resid == 1 else (mma_tf / OZ_PAIRS if args.resid == 2 else dfma_tf),
-               "resid_reduce": dw_tf if args.resid == 1 else (mma_tf / OZ_PAIRS if args.resid == 2 else dfma_tf),
-               "resid_update": dw_tf if args.resid == 1 else (mma_tf / OZ_PAIRS if args.resid == 2 else dfma_tf)}
+    pipe_peak = {"fp64": dfma_tf, "fp32": ffma_tf, "dw": dw_tf, "mma": mma_tf / OZ_PAIRS}
     phase_report = {}
     for name, (pms, pn) in phases.items():
         per_step = pms / args.steps
         ent = {"ms_per_step": per_step, "launches_per_step": pn / args.steps}
         if name in work and per_step > 0:
-            ach = work[name] / (per_step * 1e-3) / 1e12
-            ent.update(tflops=ach, peak=peak_of[name], frac=ach / peak_of[name])
+            w = work[name]
+            t_bound = sum(f / (pipe_peak[pp] * 1e12) for pp, f in w.items()) * 1e3
+            ent.update(tflops=sum(w.values()) / (per_step * 1e-3) / 1e12, bound_ms=t_bound, frac=t_bound / per_step,
+                       pipes={pp: pipe_peak[pp] for pp in w})
         phase_report[name] = ent
     # the kernels of the dominant phases: (phases, bound, peak, native work
     # factor, ncu DRAM bytes per launch)
@@ -559,7 +563,8 @@ def run_ours(args, wl):
     upd_bytes = (sum(n * r * 4 + 2 * n * l * r * 4 for l in range(1, L))
                  + nsw * sum(n * r * 4 + 2 * n * k * 4 for l in range(L)))
     red_bytes = sum(n * r * 4 + n * (l + 1) * r * 4 for l in range(L)) + nsw * L * (n * r * 4 + n * k * 4)
-    kernels["reduce_tma_kernel"] = (("reduce",), "hbm", hbm_peak, red_bytes, TRAFFIC.get("reduce_tma_kernel"))
+    red_name = "reduce_tma_kernel" if os.environ.get("HODLR_NO_TCGEN05") == "1" else "reduce_tc_kernel"
+    kernels[red_name] = (("reduce",), "hbm", hbm_peak, red_bytes, TRAFFIC.get(red_name))
     # the update runs on the tcgen05 tensor cores (exact bf16x3 split) unless
     # HODLR_NO_TCGEN05=1 selects the FP32-FMA TMA kernel; both are HBM-bound
     upd_name = "update_tma_kernel" if os.environ.get("HODLR_NO_TCGEN05") == "1" else "update_tc_kernel"
@@ -580,7 +585,7 @@ def run_ours(args, wl):
                     "algorithmic_bytes_per_launch": factor / max(nl, 1),
                     "avg_launch_ms": kms / max(nl, 1), "launches_per_step": nl}
         else:
-            kwork = factor * sum(work[ph] for ph in phs)
+            kwork = factor * sum(sum(work[ph].values()) for ph in phs)
             ach = kwork / (kms * 1e-3) / 1e12
             roof = {"kernel": kname, "bound": bound, "achieved": ach, "peak": pk, "unit": "TFLOP/s",
                     "frac": ach / pk if pk else None, "traffic": traffic,
@@ -820,6 +825,9 @@ OZ_PAIRS = 28   # digit pairs (s + t <= 6 of 7 x 7) per FP64 product in the tens
 # mixed step at N=2^20 (a dram__bytes capture of this benchmark's kernels)
 TRAFFIC = {"update_tc_kernel": 38.775e9 / 155, "update_tma_kernel": 38.804e9 / 155,
            "reduce_tma_kernel": 25.553e9 / 156,
+           # ncu DRAM bytes of one step's tensor-core reductions at N=2^17 were 1.0177 x their algorithmic
+           # bytes (2.134 GB of 2.097 GB); the same ratio applied to the N=2^20 step's 24.43 GB / 156 launches
+           "reduce_tc_kernel": 1.0177 * 156.587e6,
            "oz_tc_kernel<0>": 21.130e9 / 11, "oz_tc_kernel<1>": (20.116e9 + 0.134e9) / 11}
 
 
