@@ -70,6 +70,12 @@ class System(ctypes.Structure):
                 ("rank", ctypes.c_int32), ("nrhs", ctypes.c_int32)]
 
 
+class TreeDesc(ctypes.Structure):
+    _fields_ = [("top_levels", ctypes.c_int32), ("subtrees", ctypes.POINTER(Desc)),
+                ("coupling_rank", ctypes.POINTER(ctypes.c_int32)), ("nrhs_max", ctypes.c_int32),
+                ("flags", ctypes.c_int32), ("stream", ctypes.c_void_p)]
+
+
 class BatchDesc(ctypes.Structure):
     _fields_ = [("systems", ctypes.POINTER(System)), ("count", ctypes.c_int32), ("precision", ctypes.c_int32),
                 ("residual", ctypes.c_int32), ("refine_tol", ctypes.c_double), ("refine_max_iter", ctypes.c_int32),
@@ -108,6 +114,15 @@ SIGNATURES = {
     "hodlr_debug_wait_fault": (_I, [_I, _I, _I64]),
     "hodlr_gemm_broadcast": (_I, [_I, _I, _I, _I, _I, _D, _VP, _I64, _VP, _I64, _D, _VP, _I64]),
     "hodlr_node_solve": (_I, [_I, _I, _I, _VP, _I64, _VP, _I64]),
+    "hodlr_node_solve_irregular": (_I, [_I, _I, _I, _I, _VP, _I64, _VP, _I64, _VP, _I64, _VP, _I64]),
+    "hodlr_tree_create": (_I, [ctypes.POINTER(TreeDesc), ctypes.POINTER(_VP)]),
+    "hodlr_tree_destroy": (_I, [_VP]),
+    "hodlr_tree_subtree": (_I, [_VP, _I, ctypes.POINTER(_VP)]),
+    "hodlr_tree_rows": (_I, [_VP, ctypes.POINTER(_I64), _VP]),
+    "hodlr_tree_set_coupling": (_I, [_VP, _I, _I, _I, _VP, _I64, _VP, _I64]),
+    "hodlr_tree_factor": (_I, [_VP]),
+    "hodlr_tree_solve": (_I, [_VP, _VP, _I64, _I, ctypes.POINTER(SolveInfo)]),
+    "hodlr_tree_matvec": (_I, [_VP, _VP, _I64, _VP, _I64, _I]),
     "hodlr_generate": (_I, [_VP, ctypes.c_uint64, _D, _I, _D, _VP, _I64, _I]),
     "hodlr_profile": (_I, [_VP, _I, _VP, _VP, _I]),
     "hodlr_last_timings": (_I, [_VP, ctypes.POINTER(_D), ctypes.POINTER(_D)]),
@@ -366,6 +381,93 @@ class Batch:
         nf, f, s = ctypes.c_int(), ctypes.c_double(), ctypes.c_double()
         check(lib().hodlr_batch_stats(self.h, ctypes.byref(nf), ctypes.byref(f), ctypes.byref(s)))
         return nf.value, f.value, s.value
+
+
+class _Subtree(Solver):
+    """A tree's subtree handle (owned by the tree: close() does not destroy it)."""
+
+    def __init__(self, h, n, leaf, levels, rank):
+        self.h, self.desc = h, None
+        self.n, self.leaf, self.levels, self.rank = n, leaf, levels, rank
+
+    def close(self):
+        self.h = None
+
+    __del__ = close
+
+
+class Tree:
+    """Irregular tree (hodlr_tree_*): 2^T uniform subtrees, each with its own
+    leaf size, depth, rank and precision, under T top levels whose nodes couple
+    their children with ranks (r0, r1) that may differ.
+
+    subtrees: list of (leaf, levels, rank) or dicts with those keys and
+    optionally precision / residual / refine_tol / refine_max_iter.
+    coupling_ranks: 2 (2^T - 1) ranks, node p = 2^l - 1 + q first child then
+    second.  Each subtree is a Solver-like handle (``tree.subtree(j)``) whose
+    set_* calls fill its leaves and bases."""
+
+    def __init__(self, top_levels, subtrees, coupling_ranks, nrhs_max=1, precision=PREC_FP64,
+                 residual=RESID_FP64_TENSOR, refine_tol=1e-12, refine_max_iter=10, stream=None):
+        self.h = None
+        nsub = 1 << top_levels
+        if len(subtrees) != nsub or len(coupling_ranks) != 2 * (nsub - 1):
+            raise ValueError("need 2^T subtrees and 2 (2^T - 1) coupling ranks")
+        descs = (Desc * nsub)()
+        self._shapes = []
+        for j, sd in enumerate(subtrees):
+            if not isinstance(sd, dict):
+                sd = dict(zip(("leaf", "levels", "rank"), sd))
+            leaf, levels, rank = sd["leaf"], sd["levels"], sd["rank"]
+            descs[j] = Desc(leaf << levels, leaf, levels, rank, 1, sd.get("precision", precision),
+                            sd.get("residual", residual), sd.get("refine_tol", refine_tol),
+                            sd.get("refine_max_iter", refine_max_iter), 0, None)
+            self._shapes.append((leaf << levels, leaf, levels, rank))
+        ranks = (ctypes.c_int32 * len(coupling_ranks))(*[int(r) for r in coupling_ranks])
+        self.desc = TreeDesc(top_levels, descs, ranks, nrhs_max, 0, stream)
+        self._keep = (descs, ranks)
+        h = ctypes.c_void_p()
+        check(lib().hodlr_tree_create(ctypes.byref(self.desc), ctypes.byref(h)))
+        self.h = h
+        self.top_levels, self.ranks = top_levels, list(coupling_ranks)
+        n = _I64()
+        offs = (_I64 * (nsub + 1))()
+        check(lib().hodlr_tree_rows(self.h, ctypes.byref(n), offs))
+        self.n, self.offsets = n.value, [offs[i] for i in range(nsub + 1)]
+
+    def close(self):
+        if self.h:
+            lib().hodlr_tree_destroy(self.h)
+            self.h = None
+
+    __del__ = close
+
+    def subtree(self, j):
+        h = ctypes.c_void_p()
+        check(lib().hodlr_tree_subtree(self.h, j, ctypes.byref(h)))
+        return _Subtree(h, *self._shapes[j])
+
+    def set_coupling(self, level, pos, child, U, V):
+        check(lib().hodlr_tree_set_coupling(self.h, level, pos, child, _ptr(U), _ld(U), _ptr(V), _ld(V)))
+
+    def factor(self):
+        check(lib().hodlr_tree_factor(self.h))
+
+    def solve(self, B):
+        info = SolveInfo()
+        check(lib().hodlr_tree_solve(self.h, _ptr(B), _ld(B), B.shape[1] if B.dim() == 2 else 1,
+                                     ctypes.byref(info)))
+        return info
+
+    def matvec(self, X, Y):
+        check(lib().hodlr_tree_matvec(self.h, _ptr(X), _ld(X), _ptr(Y), _ld(Y), X.shape[1] if X.dim() == 2 else 1))
+
+
+def node_solve_irregular(nnode, r0, r1, VTu0, VTu1, VTd0, VTd1):
+    """NodeSolveRegionTask for nnode stacked nodes (hodlr_node_solve_irregular), in place on VTd0 / VTd1."""
+    nrhs = VTd0.shape[1] if VTd0.dim() == 2 else 1
+    check(lib().hodlr_node_solve_irregular(nnode, r0, r1, nrhs, _ptr(VTu0), _ld(VTu0), _ptr(VTu1), _ld(VTu1),
+                                           _ptr(VTd0), _ld(VTd0), _ptr(VTd1), _ld(VTd1)))
 
 
 def hsolve(nrow, nrhs, rank, nPart, LD, K, U, V, precision=PREC_FP64, stream=None):

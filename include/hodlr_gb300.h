@@ -292,6 +292,18 @@ HODLR_API int hodlr_gemm_broadcast(int nrow, int nPart, int nBlock, int K, int N
 HODLR_API int hodlr_node_solve(int nnode, int r, int nrhs, const double *VTu, int64_t ldu, double *VTd,
                                int64_t ldd);
 
+/* NodeSolveRegionTask (src/tasks/node_solve_region.cc:77-97) for nnode
+ * nodes whose children have unequal ranks r0, r1 (1..64 each): node p's
+ * blocks are rows [p r1, (p+1) r1) of VTu0 (V0^T u0, nnode r1 x r0) and VTd0
+ * (nnode r1 x nrhs), rows [p r0, (p+1) r0) of VTu1 (V1^T u1, nnode r0 x r1)
+ * and VTd1 (nnode r0 x nrhs).  S = [I_r0, VTu1; VTu0, I_r1] ((r0+r1)-square)
+ * is solved against [VTd1; VTd0] by FP64 LU with partial pivoting, and the
+ * solution is copied back as the reference does: its first r0 rows into
+ * VTd1, the last r1 into VTd0.  Device pointers, column-major; synchronous. */
+HODLR_API int hodlr_node_solve_irregular(int nnode, int r0, int r1, int nrhs, const double *VTu0, int64_t ldu0,
+                                         const double *VTu1, int64_t ldu1, double *VTd0, int64_t ldd0,
+                                         double *VTd1, int64_t ldd1);
+
 /* Copy out the problem held by the handle (device or host destinations; any
  * may be NULL): leaf blocks in the layout of hodlr_set_leaf_blocks
  * (ld, leaf_stride), U and V as L blocks of N x r (leading dimension N,
@@ -410,6 +422,57 @@ HODLR_API int hodlr_autotune(hodlr_handle h, int nrhs, hodlr_tuning *best);
 HODLR_API int hodlr_set_tuning(hodlr_handle h, const hodlr_tuning *t);
 HODLR_API int hodlr_get_tuning(hodlr_handle h, hodlr_tuning *t);
 HODLR_API int hodlr_batch_autotune(hodlr_batch b, hodlr_tuning *per_forest, int capacity);
+
+/* ------------------------------------------------------ irregular trees
+ * One HODLR matrix whose top T levels join 2^T uniform subtrees, each with
+ * its own leaf size, depth, rank and precision, and whose top nodes may
+ * couple their children with unequal ranks -- the matrices of fastSolver2's
+ * SPMD drivers without padding: spmd_driver/solver.cc (one subtree per
+ * shard under spmd_level top levels), solver_irregular_part.cc:73-79 (the
+ * first `-heavy` shards with ten times the leaf size) and
+ * solver_irregular_ranks.cc:99-132 (shard ranks rank0 / rank1, top coupling
+ * bases with the sibling's rank).  Top node p (depth l, position q,
+ * p = 2^l - 1 + q) with children c0, c1 holds
+ *     A[c0,c1] = U_c0 V_c1^T  (rank coupling_rank[2p]),
+ *     A[c1,c0] = U_c1 V_c0^T  (rank coupling_rank[2p+1]),
+ * and the factorisation solves each node's (r0+r1)-square system as
+ * hodlr_node_solve_irregular does.  The subtrees are handles of their own
+ * (set their leaf blocks and bases with the hodlr_set_* calls on the handle
+ * hodlr_tree_subtree returns); the top levels run in FP64.  Rows are the
+ * subtrees' rows in order (hodlr_tree_rows). */
+typedef struct hodlr_tree_desc {
+  int32_t top_levels;             /* T, 1..7 */
+  const hodlr_desc *subtrees;     /* 2^T subtree descriptions, left to right;
+                                     nrhs_max and stream are set by the tree */
+  const int32_t *coupling_rank;   /* 2 (2^T - 1) ranks, each 1..64 */
+  int32_t nrhs_max;               /* largest nrhs of a solve or product */
+  int32_t flags;                  /* reserved, 0 */
+  void *stream;                   /* cudaStream_t, or NULL (own stream) */
+} hodlr_tree_desc;
+
+typedef struct hodlr_tree_ctx *hodlr_tree;
+
+HODLR_API int hodlr_tree_create(const hodlr_tree_desc *desc, hodlr_tree *out);
+HODLR_API int hodlr_tree_destroy(hodlr_tree t);
+/* Subtree j's handle (owned by the tree; do not destroy it). */
+HODLR_API int hodlr_tree_subtree(hodlr_tree t, int j, hodlr_handle *out);
+/* Total rows n and, if row_offsets is given, the first row of every subtree
+ * (2^T + 1 entries, the last = n). */
+HODLR_API int hodlr_tree_rows(hodlr_tree t, int64_t *n, int64_t *row_offsets);
+/* Coupling bases of child `child` (0 or 1) of top node (level, pos): U_c
+ * (rows of c x its own rank) and V_c (rows of c x the sibling's rank), the
+ * child's rows packed from its first row; leading dimensions ldu, ldv.  Host
+ * or device memory. */
+HODLR_API int hodlr_tree_set_coupling(hodlr_tree t, int level, int pos, int child, const double *U, int64_t ldu,
+                                      const double *V, int64_t ldv);
+/* Subtree factorisations, U~ = A_sub^{-1} U of every coupling column, and
+ * the top nodes' LU factors, deepest level first. */
+HODLR_API int hodlr_tree_factor(hodlr_tree t);
+/* X = A^{-1} B in place (device, n x nrhs, ldb).  info: the largest
+ * refinement count and relative residual over the subtrees' own solves. */
+HODLR_API int hodlr_tree_solve(hodlr_tree t, double *B, int64_t ldb, int nrhs, hodlr_solve_info *info);
+/* Y = A X in FP64 from the exact representation (device). */
+HODLR_API int hodlr_tree_matvec(hodlr_tree t, const double *X, int64_t ldx, double *Y, int64_t ldy, int nrhs);
 
 /* Test hook of the bounded device waits (no counterpart in the reference,
  * whose CPU tasks have no device waits).  While set (cta >= 0), CTA `cta` of

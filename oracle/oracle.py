@@ -266,6 +266,82 @@ def hodlr_matvec(prob, X):
     return Y
 
 
+# ---------------------------------------------------------------- irregular trees
+
+def node_solve_irregular(r0, r1, VTu0, VTu1, VTd0, VTd1):
+    """NodeSolveRegionTask::cpu_task (src/tasks/node_solve_region.cc:77-97)
+    restated: S = I with S(i, r0+j) = VTu1(i, j), S(r0+j, i) = VTu0(j, i),
+    B = [VTd1; VTd0], S.solve(B) (PtrMatrix::solve = dgesv,
+    src/ptr_matrix.cc:101-111), the first r0 rows back into VTd1 and the last
+    r1 into VTd0.  VTu0: r1 x r0, VTu1: r0 x r1, VTd0: r1 x k, VTd1: r0 x k.
+    Returns (VTd0', VTd1', info)."""
+    n = r0 + r1
+    S = np.eye(n, order="F")
+    for i in range(r0):
+        for j in range(r1):
+            S[i, r0 + j] = VTu1[i, j]
+            S[r0 + j, i] = VTu0[j, i]
+    B = np.asfortranarray(np.vstack([VTd1, VTd0]))
+    LU, ipiv, info = dgetrf(S)
+    X = dgetrs(LU, ipiv, B)
+    return np.array(X[r0:], order="F"), np.array(X[:r0], order="F"), info
+
+
+def tree_solve(tp, B):
+    """Solve A X = B for an irregular tree (problems.TreeProblem) in the order
+    of fastSolver2's SPMD solve (spmd_driver/solver_irregular_ranks.cc:145-235):
+    every subtree solves its right-hand sides together with all of its
+    top-level coupling columns (the hsolve of its own levels), then the top
+    levels run deepest first -- VTu = V^T u and VTd = V^T d on each child
+    (LMatrix::gemm), the node solve of unequal ranks (node_solve_irregular) and
+    d -= u VTd (LMatrix::gemm_inplace), d being the solution columns and the
+    coupling columns of the levels above."""
+    T = tp.top_levels
+    B = np.asarray(B, dtype=np.float64).reshape(tp.n, -1)
+    k = B.shape[1]
+    X = np.array(B, order="F")
+    Ut = [np.zeros((tp.n, 64), order="F") for _ in range(T)]   # level l's transformed bases, child-wide ranks
+    for (l, q, h), U in tp.Uc.items():
+        rows = tp.child_rows(l, q, h)
+        Ut[l][rows, :U.shape[1]] = U
+    info = 0
+    for j, sub in enumerate(tp.subs):
+        rows = slice(tp.offsets[j], tp.offsets[j + 1])
+        widths = [tp.u_rank(l, j) for l in range(T)]
+        W = np.hstack([X[rows]] + [Ut[l][rows, :widths[l]] for l in range(T)])
+        Xj, _, inf = hsolve_general(sub, W)
+        info = info or inf
+        X[rows] = Xj[:, :k]
+        c = k
+        for l in range(T):
+            Ut[l][rows, :widths[l]] = Xj[:, c:c + widths[l]]
+            c += widths[l]
+    for l in range(T - 1, -1, -1):
+        for q in range(1 << l):
+            p = (1 << l) - 1 + q
+            r0, r1 = tp.ranks[2 * p], tp.ranks[2 * p + 1]
+            R = [tp.child_rows(l, q, h) for h in (0, 1)]
+            j0 = [tp.child_leaves(l, q, h)[0] for h in (0, 1)]
+            own = [Ut[l][R[0], :r0], Ut[l][R[1], :r1]]
+            anc = [[(a, tp.u_rank(a, j0[h])) for a in range(l)] for h in (0, 1)]
+            dcols = [np.hstack([X[R[h]]] + [Ut[a][R[h], :w] for a, w in anc[h]]) for h in (0, 1)]
+            V = [tp.Vc[(l, q, 0)], tp.Vc[(l, q, 1)]]
+            VTu0 = dgemm("T", "N", 1.0, V[0], own[0], 0.0, np.zeros((r1, r0)))
+            VTu1 = dgemm("T", "N", 1.0, V[1], own[1], 0.0, np.zeros((r0, r1)))
+            VTd0 = dgemm("T", "N", 1.0, V[0], dcols[0], 0.0, np.zeros((r1, dcols[0].shape[1])))
+            VTd1 = dgemm("T", "N", 1.0, V[1], dcols[1], 0.0, np.zeros((r0, dcols[1].shape[1])))
+            VTd0, VTd1, inf = node_solve_irregular(r0, r1, VTu0, VTu1, VTd0, VTd1)
+            info = info or inf
+            for h, eta in ((0, VTd1), (1, VTd0)):
+                d = dgemm("N", "N", -1.0, own[h], eta, 1.0, dcols[h])
+                X[R[h]] = d[:, :k]
+                c = k
+                for a, w in anc[h]:
+                    Ut[a][R[h], :w] = d[:, c:c + w]
+                    c += w
+    return X, info
+
+
 # ---------------------------------------------------------------- BLAS-backed restatement
 
 def blas_hsolve(nrow, nrhs, rank, nPart, K, U, V):

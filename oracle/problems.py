@@ -118,6 +118,89 @@ def gaussian_problem(leaf, levels, rank, nrhs=1, seed=0, shift=4.0,
     return Problem(leaf, levels, rank, K, U, V, s, B)
 
 
+@dataclass
+class TreeProblem:
+    """An irregular tree: 2^T uniform subtrees (their own leaf, depth, rank)
+    under T top levels; top node p = 2^l - 1 + q couples its children c0, c1
+    by A[c0,c1] = U_c0 V_c1^T (rank ranks[2p]) and A[c1,c0] = U_c1 V_c0^T
+    (rank ranks[2p+1]).  Uc[(l, q, h)] is U of child h (its rows x its own
+    rank), Vc[(l, q, h)] its V (its rows x the sibling's rank)."""
+    top_levels: int
+    subs: List[Problem]
+    ranks: List[int]
+    Uc: dict
+    Vc: dict
+    B: np.ndarray
+
+    @property
+    def offsets(self):
+        return np.concatenate([[0], np.cumsum([s.n for s in self.subs])]).astype(int).tolist()
+
+    @property
+    def n(self):
+        return self.offsets[-1]
+
+    def child_leaves(self, l, q, h):
+        span = 1 << (self.top_levels - 1 - l)
+        return (2 * q + h) * span, (2 * q + h + 1) * span
+
+    def child_rows(self, l, q, h):
+        j0, j1 = self.child_leaves(l, q, h)
+        return slice(self.offsets[j0], self.offsets[j1])
+
+    def u_rank(self, l, j):
+        """Rank of the depth-l coupling U on the rows of subtree j."""
+        T = self.top_levels
+        p = (1 << l) - 1 + (j >> (T - l))
+        return self.ranks[2 * p + ((j >> (T - 1 - l)) & 1)]
+
+    def dense(self):
+        A = np.zeros((self.n, self.n))
+        off = self.offsets
+        for j, s in enumerate(self.subs):
+            A[off[j]:off[j + 1], off[j]:off[j + 1]] = s.dense()
+        for l in range(self.top_levels):
+            for q in range(1 << l):
+                c0, c1 = self.child_rows(l, q, 0), self.child_rows(l, q, 1)
+                A[c0, c1] = self.Uc[(l, q, 0)] @ self.Vc[(l, q, 1)].T
+                A[c1, c0] = self.Uc[(l, q, 1)] @ self.Vc[(l, q, 0)].T
+        return A
+
+    def matvec(self, X):
+        """A X from the representation (subtree products by the oracle)."""
+        X = np.asarray(X, dtype=np.float64).reshape(self.n, -1)
+        Y = np.zeros_like(X)
+        off = self.offsets
+        for j, s in enumerate(self.subs):
+            Y[off[j]:off[j + 1]] = oracle.hodlr_matvec(s, X[off[j]:off[j + 1]])
+        for l in range(self.top_levels):
+            for q in range(1 << l):
+                c0, c1 = self.child_rows(l, q, 0), self.child_rows(l, q, 1)
+                Y[c0] += self.Uc[(l, q, 0)] @ (self.Vc[(l, q, 1)].T @ X[c1])
+                Y[c1] += self.Uc[(l, q, 1)] @ (self.Vc[(l, q, 0)].T @ X[c0])
+        return Y
+
+
+def tree_problem(top_levels, shapes, coupling_ranks, nrhs=1, seed=0, shift=4.0, orthonormal=False, decay=None):
+    """Gaussian irregular tree: subtree j is gaussian_problem(*shapes[j])
+    (leaf, levels, rank), the coupling bases N(0,1)/sqrt(child rows)."""
+    rng = np.random.default_rng(seed)
+    subs = [gaussian_problem(m, L, r, nrhs=1, seed=seed * 1000 + 1 + j, shift=shift, orthonormal=orthonormal,
+                             decay=decay) for j, (m, L, r) in enumerate(shapes)]
+    tp = TreeProblem(top_levels, subs, list(coupling_ranks), {}, {}, None)
+    for l in range(top_levels):
+        for q in range(1 << l):
+            p = (1 << l) - 1 + q
+            for h in (0, 1):
+                rows = tp.child_rows(l, q, h)
+                nr = rows.stop - rows.start
+                ru, rv = coupling_ranks[2 * p + h], coupling_ranks[2 * p + 1 - h]
+                tp.Uc[(l, q, h)] = np.asfortranarray(rng.standard_normal((nr, ru)) / np.sqrt(nr))
+                tp.Vc[(l, q, h)] = np.asfortranarray(rng.standard_normal((nr, rv)) / np.sqrt(nr))
+    tp.B = np.asfortranarray(rng.standard_normal((tp.n, nrhs)))
+    return tp
+
+
 def rel_residual(prob, X, B=None):
     """||B - A X||_F / ||B||_F with A X from the FP64 HODLR matvec."""
     B = prob.B if B is None else B

@@ -131,3 +131,28 @@ def test_wait_fault_hook_rejects_bad_arguments_on_host(fs):
     assert L.hodlr_debug_wait_fault(0, 0, -5) == fs.HODLR_ERR_INVALID_ARG
     assert L.hodlr_debug_wait_fault(0, 0, 2 * 10**9) == fs.HODLR_ERR_INVALID_ARG
     assert b"wait_fault" in L.hodlr_last_error_string()
+
+
+def test_tree_calls_reject_bad_arguments_on_host(fs):
+    """Argument checks of the irregular-tree entry points run before any device call."""
+    L = fs.lib()
+    d = fs.Desc(128, 32, 2, 4, 1, 0, 0, 1e-12, 10, 0, None)
+    subs = (fs.Desc * 2)(d, d)
+    h = ctypes.c_void_p()
+    for top, ranks in ((0, [4, 4]), (8, [4, 4]), (1, [0, 4]), (1, [4, 65])):
+        r = (ctypes.c_int32 * 2)(*ranks)
+        desc = fs.TreeDesc(top, subs, r, 1, 0, None)
+        assert L.hodlr_tree_create(ctypes.byref(desc), ctypes.byref(h)) == fs.HODLR_ERR_INVALID_ARG
+    assert L.hodlr_tree_create(None, ctypes.byref(h)) == fs.HODLR_ERR_INVALID_ARG
+    for call in (lambda: L.hodlr_tree_factor(None), lambda: L.hodlr_tree_solve(None, None, 0, 1, None),
+                 lambda: L.hodlr_tree_matvec(None, None, 0, None, 0, 1),
+                 lambda: L.hodlr_tree_set_coupling(None, 0, 0, 0, None, 0, None, 0),
+                 lambda: L.hodlr_tree_subtree(None, 0, ctypes.byref(h)),
+                 lambda: L.hodlr_tree_rows(None, None, None)):
+        assert call() == fs.HODLR_ERR_INVALID_ARG
+    assert L.hodlr_tree_destroy(None) == fs.HODLR_OK
+    bad = [(0, 4, 4, 1), (1, 0, 4, 1), (1, 4, 65, 1), (1, 4, 4, 0)]
+    for nnode, r0, r1, k in bad:
+        assert L.hodlr_node_solve_irregular(nnode, r0, r1, k, 8, 64, 8, 64, 8, 64, 8, 64) == fs.HODLR_ERR_INVALID_ARG
+    # leading dimensions shorter than the stacked blocks
+    assert L.hodlr_node_solve_irregular(2, 4, 3, 1, 8, 5, 8, 8, 8, 6, 8, 8) == fs.HODLR_ERR_INVALID_ARG

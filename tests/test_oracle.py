@@ -210,3 +210,31 @@ def test_blas_matvec_matches_oracle(oracle_lib, nthreads):
     Y = O.blas_matvec(pr.leaf, pr.levels, pr.rank, np.asfortranarray(pr.K), pr.U, pr.V, pr.s,
                       np.asfortranarray(pr.B), nthreads)
     assert rel(Y, Y0) < 1e-13
+
+
+@pytest.mark.parametrize("r0,r1,k", [(5, 3, 2), (1, 7, 1), (12, 12, 4)])
+def test_node_solve_irregular_oracle_matches_dense(oracle_lib, r0, r1, k):
+    """node_solve_region.cc:77-97: [I, VTu1; VTu0, I] [eta0; eta1] = [VTd1; VTd0],
+    eta0 written to VTd1 and eta1 to VTd0."""
+    rng = np.random.default_rng(r0 * 31 + r1)
+    VTu0, VTu1 = rng.standard_normal((r1, r0)) * 0.3, rng.standard_normal((r0, r1)) * 0.3
+    VTd0, VTd1 = rng.standard_normal((r1, k)), rng.standard_normal((r0, k))
+    o0, o1, info = O.node_solve_irregular(r0, r1, VTu0, VTu1, VTd0, VTd1)
+    S = np.block([[np.eye(r0), VTu1], [VTu0, np.eye(r1)]])
+    eta = np.linalg.solve(S, np.vstack([VTd1, VTd0]))
+    assert info == 0
+    assert rel(o1, eta[:r0]) < 1e-14 and rel(o0, eta[r0:]) < 1e-14
+
+
+@pytest.mark.parametrize("T,shapes,ranks", [
+    (1, [(16, 2, 3), (160, 2, 3)], [3, 3]),                                    # heavy shard, leaf x10
+    (1, [(32, 2, 6), (32, 2, 2)], [6, 2]),                                     # shard ranks rank0 / rank1
+    (2, [(16, 2, 3), (160, 2, 3), (16, 3, 5), (32, 1, 2)], [5, 3, 4, 6, 2, 7]),
+])
+def test_tree_oracle_matches_dense(oracle_lib, T, shapes, ranks):
+    tp = P.tree_problem(T, shapes, ranks, nrhs=3, seed=T + len(shapes))
+    X, info = O.tree_solve(tp, tp.B)
+    A = tp.dense()
+    assert info == 0
+    assert rel(X, np.linalg.solve(A, tp.B)) < 1e-13
+    assert rel(tp.matvec(X), A @ X) < 1e-14
