@@ -42,6 +42,13 @@ template <typename T>
 cudaError_t launch_leaf_getrf(const double *D, long long d_ld, long long d_stride, T *LU, int *ipiv,
                               int m, int nleaf, DevStatus *st, T *Dinv, cudaStream_t s);
 
+// The same factorisation for leaves too large for one CTA's shared memory:
+// blocked right-looking LU over panels of 32 columns, each panel step one
+// launch over the leaves and one over (trailing column tile, leaf).
+template <typename T>
+cudaError_t launch_leaf_getrf_blocked(const double *D, long long d_ld, long long d_stride, T *LU, int *ipiv, int m,
+                                      int nleaf, DevStatus *st, cudaStream_t s);
+
 // K2: X := D_i^{-1} X (or D_i^{-T} X) on the rows of every leaf i for the
 // columns [0, ncols) of X (ld ldx).  skip (device flag, may be NULL): when
 // *skip != 0 the kernel returns immediately.

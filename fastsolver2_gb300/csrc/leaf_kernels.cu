@@ -157,8 +157,7 @@ cudaError_t launch_leaf_getrf(const double *D, long long d_ld, long long d_strid
     HODLR_LAUNCH(k, nleaf, 256, bytes, s, D, d_ld, d_stride, LU, ipiv, m, st, Dinv);
   } else {
     if (Dinv) return cudaErrorInvalidValue;  // caller forms the inverse separately
-    HODLR_LAUNCH((leaf_getrf_kernel<T, false>), nleaf, 256, 0, s, D, d_ld, d_stride, LU, ipiv, m, st,
-                 (T *)nullptr);
+    return launch_leaf_getrf_blocked<T>(D, d_ld, d_stride, LU, ipiv, m, nleaf, st, s);
   }
   return cudaGetLastError();
 }
@@ -175,8 +174,10 @@ cudaError_t launch_leaf_getrs(const T *LU, const int *ipiv, int m, int nleaf, T 
   size_t avail = cap - piv_bytes - (lu_smem ? lu_bytes : 0);
   int ct_max = (int)std::min<size_t>(avail / ((size_t)m * sizeof(T)), 128);
   if (ct_max < 1) return cudaErrorInvalidValue;
-  int ntile = ceil_div(ncols, ct_max);
+  // enough column tiles to give every SM a CTA when the leaves are few and large
+  int ntile = std::max(ceil_div(ncols, ct_max), std::min(ncols, ceil_div(kNumSMs, nleaf)));
   int ct = ceil_div(ncols, ntile);
+  ntile = ceil_div(ncols, ct);
   size_t bytes = (size_t)m * ct * sizeof(T) + piv_bytes + (lu_smem ? lu_bytes : 0);
   dim3 grid(ntile, nleaf);
   cudaError_t e = cudaSuccess;
