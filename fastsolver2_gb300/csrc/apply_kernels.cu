@@ -56,6 +56,8 @@ template <typename T>
 cudaError_t launch_leaf_inverse(const T *LU, const int *ipiv, int m, int nleaf, T *Dinv, cudaStream_t s) {
   const size_t lu_bytes = (size_t)m * m * sizeof(T), piv_bytes = (size_t)m * 4 + 16;
   const bool lu_smem = lu_bytes + piv_bytes + (size_t)m * 8 * sizeof(T) <= kSmemCap;
+  if (!lu_smem && leaf_inverse_blocked_smem(m, sizeof(T)) <= kSmemCap)
+    return launch_leaf_inverse_blocked<T>(LU, ipiv, m, nleaf, Dinv, s);
   const size_t avail = kSmemCap - piv_bytes - (lu_smem ? lu_bytes : 0);
   const int ct_max = (int)std::min<size_t>(avail / ((size_t)m * sizeof(T)), 128);
   const int ntile = ceil_div(m, ct_max), ct = ceil_div(m, ntile);
@@ -404,15 +406,17 @@ __device__ __forceinline__ V row_entry(const V (&v)[RS], int p) {
   return __shfl_sync(0xffffffffu, slot_get<RS>(v, p >> 5), p & 31);
 }
 
-template <int M>
-__global__ void __launch_bounds__(256, 3) cap_factor_cols_kernel(CapFactorArgs a) {
-  constexpr int RS = M / 32, CW = M / 8;
+template <int M, int NW>
+__global__ void __launch_bounds__(NW * 32, NW * 32 * (M / NW) >= 4096 ? 1 : (NW >= 16 ? 2 : 3))
+cap_factor_cols_kernel(CapFactorArgs a) {
+  constexpr int RS = M / 32, CW = M / NW;
   __shared__ double s_l[2][M];   // multipliers by physical row
   __shared__ float s_l32[2][M];
   __shared__ int4 s_piv[2];      // (pivot row, row at position k, pivot row's position, -)
   __shared__ int s_info;
-  __shared__ float s_u[M * M];   // U rounded to FP32, by position, [j][i]
-  __shared__ float s_z[M * M];   // L^{-1} P by position, [j][i]
+  extern __shared__ float cols_dyn[];
+  float *s_u = cols_dyn;         // U rounded to FP32, by position, [j][i] (M * M)
+  float *s_z = cols_dyn + M * M; // L^{-1} P by position, [j][i] (M * M)
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int pn = blockIdx.x, node = a.node_base + pn, r = a.r, n2 = 2 * r;
   const long long o0 = (long long)(2 * pn) * a.tb_stride, o1 = (long long)(2 * pn + 1) * a.tb_stride;
@@ -426,7 +430,7 @@ __global__ void __launch_bounds__(256, 3) cap_factor_cols_kernel(CapFactorArgs a
   for (int c = 0; c < CW; ++c)
 #pragma unroll
     for (int s = 0; s < RS; ++s) {
-      const int i = lane + 32 * s, j = warp + 8 * c;
+      const int i = lane + 32 * s, j = warp + NW * c;
       double v = (i == j) ? 1.0 : 0.0;
       if (j < n2 && i < n2) {
         auto T = [&](long long off) -> double { return a.Tb32 ? (double)a.Tb32[off] : a.Tb[off]; };
@@ -514,17 +518,17 @@ __global__ void __launch_bounds__(256, 3) cap_factor_cols_kernel(CapFactorArgs a
     };
     // lookahead: the owner of column k+1 finishes it and publishes step k+1
     const int k1 = k + 1;
-    if (k1 < n2 && (k1 & 7) == warp) {
+    if (k1 < n2 && (k1 % NW) == warp) {
 #pragma unroll
       for (int c = 0; c < CW; ++c)  // constant register index: the column stays in registers
-        if (warp + 8 * c == k1) {
+        if (warp + NW * c == k1) {
           update(A[c]);
           pivot_column(k1, A[c]);
         }
     }
 #pragma unroll
     for (int c = 0; c < CW; ++c) {
-      const int j = warp + 8 * c;
+      const int j = warp + NW * c;
       if (j < n2 && j > k1) update(A[c]);
       if (j < n2) {  // identity column j: the same row operation with the FP32 multipliers
         const float z = row_entry<RS>(Z[c], pb);
@@ -541,7 +545,7 @@ __global__ void __launch_bounds__(256, 3) cap_factor_cols_kernel(CapFactorArgs a
   for (int c = 0; c < CW; ++c)
 #pragma unroll
     for (int s = 0; s < RS; ++s) {
-      const int j = warp + 8 * c;
+      const int j = warp + NW * c;
       s_u[pos[s] + j * M] = static_cast<float>(A[c][s]);
       s_z[pos[s] + j * M] = Z[c][s];
       if (pos[s] < n2 && j < n2) gS[pos[s] + (long long)j * n2] = A[c][s];
@@ -550,7 +554,7 @@ __global__ void __launch_bounds__(256, 3) cap_factor_cols_kernel(CapFactorArgs a
 #pragma unroll
   for (int c = 0; c < CW; ++c)
 #pragma unroll
-    for (int s = 0; s < RS; ++s) Z[c][s] = s_z[lane + 32 * s + (warp + 8 * c) * M];
+    for (int s = 0; s < RS; ++s) Z[c][s] = s_z[lane + 32 * s + (warp + NW * c) * M];
   // X = U^{-1} Z, column by column in the warps that hold them (rows by position now)
   for (int k = n2 - 1; k >= 0; --k) {
     const float rd = 1.f / s_u[k + k * M];
@@ -559,7 +563,7 @@ __global__ void __launch_bounds__(256, 3) cap_factor_cols_kernel(CapFactorArgs a
     for (int s = 0; s < RS; ++s) u[s] = s_u[lane + 32 * s + k * M];
 #pragma unroll
     for (int c = 0; c < CW; ++c) {
-      if (warp + 8 * c >= n2) continue;
+      if (warp + NW * c >= n2) continue;
       const float x = row_entry<RS>(Z[c], k) * rd;
 #pragma unroll
       for (int s = 0; s < RS; ++s) {
@@ -574,14 +578,17 @@ __global__ void __launch_bounds__(256, 3) cap_factor_cols_kernel(CapFactorArgs a
   for (int c = 0; c < CW; ++c)
 #pragma unroll
     for (int s = 0; s < RS; ++s) {
-      const int i = lane + 32 * s, j = warp + 8 * c;
+      const int i = lane + 32 * s, j = warp + NW * c;
       if (i < n2 && j < n2) g32[i + (long long)j * n2] = Z[c][s];
     }
 }
 
-template <int M>
+template <int M, int NW>
 static cudaError_t launch_cap_cols(const CapFactorArgs &a, cudaStream_t s) {
-  HODLR_LAUNCH(cap_factor_cols_kernel<M>, a.nnode, 256, 0, s, a);
+  const size_t bytes = (size_t)2 * M * M * sizeof(float);
+  cudaError_t e = set_smem(cap_factor_cols_kernel<M, NW>, bytes);
+  if (e != cudaSuccess) return e;
+  HODLR_LAUNCH((cap_factor_cols_kernel<M, NW>), a.nnode, NW * 32, bytes, s, a);
   return cudaGetLastError();
 }
 
@@ -599,8 +606,9 @@ cudaError_t launch_cap_factor(const CapFactorArgs &a, cudaStream_t s) {
   if (a.nnode <= 0) return cudaSuccess;
   if (a.r < 1 || a.r > 64) return cudaErrorInvalidValue;
   const int n2 = 2 * a.r;
-  if (a.sinv32 && n2 <= 32) return launch_cap_cols<32>(a, s);
-  if (a.sinv32 && n2 <= 64) return launch_cap_cols<64>(a, s);
+  if (a.sinv32 && n2 <= 32) return launch_cap_cols<32, 8>(a, s);
+  if (a.sinv32 && n2 <= 64) return current_tuning().cap_warps == 16 ? launch_cap_cols<64, 16>(a, s) : launch_cap_cols<64, 8>(a, s);
+  if (a.sinv32) return launch_cap_cols<128, 16>(a, s);
   if (n2 == 32) return launch_cap_reg<32>(a, s);
   if (n2 == 64) return launch_cap_reg<64>(a, s);
   if (n2 == 128) return launch_cap_reg<128>(a, s);

@@ -2474,6 +2474,8 @@ int hodlr_batch_stats(hodlr_batch b, int *nforests, double *factor_ms, double *s
 // sweeps on the handle's own inputs with a seeded scratch right-hand side.
 static const int kRedCands[] = {2, 4, 8};
 static const int kUpdCands[] = {0, 64};
+static const int kCapWarpCands[] = {8, 16};
+static const int kUpdTcCands[] = {0, 1, 2};
 
 template <typename Measure>
 static int tune_search(Tuning &cur, double &cur_ms, Measure measure) {
@@ -2494,12 +2496,30 @@ static int tune_search(Tuning &cur, double &cur_ms, Measure measure) {
     CKS(measure(t, ms));
     if (ms < cur_ms) cur = t, cur_ms = ms;
   }
+  for (int sh : kUpdTcCands) {
+    if (sh == cur.upd_tc_shape) continue;
+    Tuning t = cur;
+    t.upd_tc_shape = sh;
+    double ms = 0.0;
+    CKS(measure(t, ms));
+    if (ms < cur_ms) cur = t, cur_ms = ms;
+  }
+  for (int w : kCapWarpCands) {
+    if (w == cur.cap_warps) continue;
+    Tuning t = cur;
+    t.cap_warps = w;
+    double ms = 0.0;
+    CKS(measure(t, ms));
+    if (ms < cur_ms) cur = t, cur_ms = ms;
+  }
   return HODLR_OK;
 }
 
 static bool valid_tuning(const hodlr_tuning &t) {
   return (t.red_ctas_per_sm == 2 || t.red_ctas_per_sm == 4 || t.red_ctas_per_sm == 8) &&
-         (t.update_tile_rows == 0 || t.update_tile_rows == 64 || t.update_tile_rows == 128);
+         (t.update_tile_rows == 0 || t.update_tile_rows == 64 || t.update_tile_rows == 128) &&
+         (t.cap_warps == 0 || t.cap_warps == 8 || t.cap_warps == 16) && t.update_tc_shape >= 0 &&
+         t.update_tc_shape <= 2;
 }
 
 extern "C" {
@@ -2508,6 +2528,8 @@ int hodlr_set_tuning(hodlr_handle h, const hodlr_tuning *t) {
   if (!h || !t || !valid_tuning(*t)) return set_err(HODLR_ERR_INVALID_ARG, "bad tuning");
   h->tune.red_ctas_per_sm = t->red_ctas_per_sm;
   h->tune.upd_bm = t->update_tile_rows == 128 ? 0 : t->update_tile_rows;
+  h->tune.cap_warps = t->cap_warps == 0 ? 8 : t->cap_warps;
+  h->tune.upd_tc_shape = t->update_tc_shape;
   clear_graphs(h);
   h->factored = false;
   return HODLR_OK;
@@ -2517,6 +2539,8 @@ int hodlr_get_tuning(hodlr_handle h, hodlr_tuning *t) {
   if (!h || !t) return set_err(HODLR_ERR_INVALID_ARG, "null argument");
   t->red_ctas_per_sm = h->tune.red_ctas_per_sm;
   t->update_tile_rows = h->tune.upd_bm;
+  t->cap_warps = h->tune.cap_warps;
+  t->update_tc_shape = h->tune.upd_tc_shape;
   t->ms = -1.0;
   return HODLR_OK;
 }
@@ -2555,6 +2579,8 @@ int hodlr_autotune(hodlr_handle h, int nrhs, hodlr_tuning *best) {
   if (best) {
     best->red_ctas_per_sm = cur.red_ctas_per_sm;
     best->update_tile_rows = cur.upd_bm;
+    best->cap_warps = cur.cap_warps;
+    best->update_tc_shape = cur.upd_tc_shape;
     best->ms = cur_ms;
   }
   return HODLR_OK;
@@ -2599,6 +2625,8 @@ int hodlr_batch_autotune(hodlr_batch b, hodlr_tuning *per_forest, int capacity) 
     if (per_forest && (int)fi < capacity) {
       per_forest[fi].red_ctas_per_sm = cur.red_ctas_per_sm;
       per_forest[fi].update_tile_rows = cur.upd_bm;
+      per_forest[fi].cap_warps = cur.cap_warps;
+      per_forest[fi].update_tc_shape = cur.upd_tc_shape;
       per_forest[fi].ms = cur_ms;
     }
   }
@@ -2623,7 +2651,7 @@ int hodlr_batch_autotune(hodlr_batch b, hodlr_tuning *per_forest, int capacity) 
 namespace {
 
 constexpr char kCkMagic[8] = {'H', 'O', 'D', 'L', 'R', 'C', 'K', '1'};
-constexpr uint32_t kCkVersion = 1;
+constexpr uint32_t kCkVersion = 2;
 
 struct CkHeader {
   char magic[8];
@@ -2632,7 +2660,7 @@ struct CkHeader {
   int32_t leaf, levels, rank, nrhs_max, precision, residual;
   double refine_tol;
   int32_t refine_max_iter, flags;
-  int32_t red_ctas_per_sm, update_tile_rows;
+  int32_t red_ctas_per_sm, update_tile_rows, cap_warps, update_tc_shape;
   uint64_t payload, checksum;
 };
 
@@ -2716,6 +2744,8 @@ int hodlr_checkpoint_save(hodlr_handle h, void *buf, int64_t bytes) {
   hd.flags = h->d.flags;
   hd.red_ctas_per_sm = h->tune.red_ctas_per_sm;
   hd.update_tile_rows = h->tune.upd_bm;
+  hd.cap_warps = h->tune.cap_warps;
+  hd.update_tc_shape = h->tune.upd_tc_shape;
   hd.payload = (uint64_t)(p - out) - sizeof(CkHeader);
   uint64_t a = 1, c = 0;
   ck_sum(out + sizeof(CkHeader), hd.payload, a, c);
@@ -2749,7 +2779,7 @@ int hodlr_checkpoint_load(const void *buf, int64_t bytes, void *stream, hodlr_ha
   d.refine_max_iter = hd.refine_max_iter;
   d.flags = hd.flags;
   d.stream = stream;
-  hodlr_tuning t{hd.red_ctas_per_sm, hd.update_tile_rows, -1.0};
+  hodlr_tuning t{hd.red_ctas_per_sm, hd.update_tile_rows, hd.cap_warps, hd.update_tc_shape, -1.0};
   if (!valid_tuning(t)) return set_err(HODLR_ERR_INVALID_ARG, "checkpoint holds unknown launch shapes");
   hodlr_handle h = nullptr;
   CKS(hodlr_create(&d, &h));

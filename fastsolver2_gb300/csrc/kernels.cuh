@@ -15,6 +15,8 @@ int set_last_error(int code, const char *msg);
 struct Tuning {
   int red_ctas_per_sm = 4;  // split-K target of the row reductions, CTAs per SM (2, 4 or 8)
   int upd_bm = 0;           // FP32 update tile rows: 0 = 128 when the block allows, else 64
+  int cap_warps = 8;        // mixed-path capacitance LU (2r <= 64): warps per node, 8 or 16
+  int upd_tc_shape = 0;     // tcgen05 update: 0 = 128x64 tiles, 3-stage ring; 1 = 128x64, 2 stages; 2 = 128x32, 5 stages
 };
 constexpr int kMaxRedCtasPerSm = 8;
 constexpr int kNumSMs = 152;
@@ -48,6 +50,14 @@ cudaError_t launch_leaf_getrf(const double *D, long long d_ld, long long d_strid
 template <typename T>
 cudaError_t launch_leaf_getrf_blocked(const double *D, long long d_ld, long long d_stride, T *LU, int *ipiv, int m,
                                       int nleaf, DevStatus *st, cudaStream_t s);
+
+// Explicit inverses from those factors for leaves whose LU does not fit one
+// CTA's shared memory: (32-column tile, leaf) CTAs, blocked triangular solves
+// of the interchanged identity.  Shared memory per CTA:
+// leaf_inverse_blocked_smem(m, sizeof(T)).
+size_t leaf_inverse_blocked_smem(int m, int elem_bytes);
+template <typename T>
+cudaError_t launch_leaf_inverse_blocked(const T *LU, const int *ipiv, int m, int nleaf, T *Dinv, cudaStream_t s);
 
 // K2: X := D_i^{-1} X (or D_i^{-T} X) on the rows of every leaf i for the
 // columns [0, ncols) of X (ld ldx).  skip (device flag, may be NULL): when

@@ -20,6 +20,12 @@ constexpr int kPanelNb = 32;      // panel width
 constexpr int kTrailCols = 32;    // columns per trailing-update CTA
 constexpr int kTrailRows = 128;   // rows of L21 staged per pass
 
+template <typename T>
+static cudaError_t set_dyn_smem(T kernel, size_t bytes) {
+  if (bytes <= 48 * 1024) return cudaSuccess;
+  return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+}
+
 // LU[leaf] = (T) D[leaf]; the first non-finite entry is reported.
 template <typename T>
 __global__ void __launch_bounds__(256) leaf_blocked_init_kernel(const double *__restrict__ D, long long d_ld,
@@ -200,11 +206,134 @@ __global__ void __launch_bounds__(256) leaf_trail_kernel(T *LU, int m, int j0, i
   }
 }
 
+// Explicit inverses D^{-1} = U^{-1} L^{-1} P from the LU factors of every leaf:
+// CTA (tile, leaf) owns columns [c0, c0 + 32) of the inverse, all m rows in
+// shared memory.  The identity's columns get the interchanges, then a blocked
+// unit-lower solve (32-row diagonal blocks in DTRSM's order, the rows below
+// updated by the block's L panel in passes of 128 rows) and a blocked upper
+// solve from the bottom (diagonal blocks by division, the rows above updated
+// by the block's U panel) -- the DGETRS order on the identity.
 template <typename T>
-static cudaError_t set_dyn_smem(T kernel, size_t bytes) {
-  if (bytes <= 48 * 1024) return cudaSuccess;
-  return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+__global__ void __launch_bounds__(256) leaf_inverse_blocked_kernel(const T *__restrict__ LU, const int *__restrict__ ipiv,
+                                                                   int m, T *Dinv) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T *sX = reinterpret_cast<T *>(smem_raw);                 // m x 32, ld m
+  T *sP = sX + (size_t)m * kTrailCols;                      // panel pass: 128 x 32, [k * 128 + r]
+  T *sD = sP + kTrailRows * kPanelNb;                       // diagonal block 32 x 32, ld 32
+  const int leaf = blockIdx.y, tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, grp = tid >> 5;
+  const T *A = LU + (long long)leaf * m * m;
+  const int *piv = ipiv + (long long)leaf * m;
+  const int c0 = blockIdx.x * kTrailCols, nc = min(kTrailCols, m - c0);
+  for (int e = tid; e < m * kTrailCols; e += nt) {
+    const int i = e % m, c = e / m;
+    sX[e] = (c < nc && i == c0 + c) ? T(1) : T(0);
+  }
+  __syncthreads();
+  if (tid < nc)
+    for (int k = 0; k < m; ++k) {
+      const int p = piv[k] - 1;
+      if (p != k) swap_vals(sX[k + tid * m], sX[p + tid * m]);
+    }
+  // rows [r0, r0 + nr) -= A(rows, kb block) * X(kb block rows, :), the panel streamed in 128-row passes
+  auto panel_update = [&](int kb0, int kbn, int r0, int r1) {
+    for (int p0 = r0; p0 < r1; p0 += kTrailRows) {
+      const int nr = min(kTrailRows, r1 - p0);
+      __syncthreads();
+      for (int e = tid; e < kTrailRows * kbn; e += nt) {
+        const int r = e % kTrailRows, k = e / kTrailRows;
+        sP[k * kTrailRows + r] = r < nr ? A[(p0 + r) + (long long)(kb0 + k) * m] : T(0);
+      }
+      __syncthreads();
+      T acc[4][4];
+#pragma unroll
+      for (int a = 0; a < 4; ++a)
+#pragma unroll
+        for (int b = 0; b < 4; ++b) {
+          const int r = lane + 32 * a;
+          acc[a][b] = r < nr ? sX[(p0 + r) + (4 * grp + b) * m] : T(0);
+        }
+      for (int k = 0; k < kbn; ++k) {
+        T l[4], u[4];
+#pragma unroll
+        for (int a = 0; a < 4; ++a) l[a] = sP[k * kTrailRows + lane + 32 * a];
+#pragma unroll
+        for (int b = 0; b < 4; ++b) u[b] = sX[(kb0 + k) + (4 * grp + b) * m];
+#pragma unroll
+        for (int a = 0; a < 4; ++a)
+#pragma unroll
+          for (int b = 0; b < 4; ++b) acc[a][b] -= l[a] * u[b];
+      }
+#pragma unroll
+      for (int a = 0; a < 4; ++a)
+#pragma unroll
+        for (int b = 0; b < 4; ++b) {
+          const int r = lane + 32 * a;
+          if (r < nr) sX[(p0 + r) + (4 * grp + b) * m] = acc[a][b];
+        }
+    }
+  };
+  auto load_diag = [&](int kb0, int kbn) {
+    __syncthreads();
+    for (int e = tid; e < kbn * kbn; e += nt) {
+      const int i = e % kbn, k = e / kbn;
+      sD[i + k * kPanelNb] = A[(kb0 + i) + (long long)(kb0 + k) * m];
+    }
+    __syncthreads();
+  };
+  // L Y = P X, unit lower, 32-row blocks top down
+  for (int kb0 = 0; kb0 < m; kb0 += kPanelNb) {
+    const int kbn = min(kPanelNb, m - kb0);
+    load_diag(kb0, kbn);
+    for (int k = 0; k + 1 < kbn; ++k) {
+      for (int e = tid; e < (kbn - k - 1) * kTrailCols; e += nt) {
+        const int i = k + 1 + e % (kbn - k - 1), c = e / (kbn - k - 1);
+        sX[(kb0 + i) + c * m] -= sX[(kb0 + k) + c * m] * sD[i + k * kPanelNb];
+      }
+      __syncthreads();
+    }
+    if (kb0 + kbn < m) panel_update(kb0, kbn, kb0 + kbn, m);
+  }
+  // U X = Y, 32-row blocks bottom up
+  for (int kb0 = ((m - 1) / kPanelNb) * kPanelNb; kb0 >= 0; kb0 -= kPanelNb) {
+    const int kbn = min(kPanelNb, m - kb0);
+    load_diag(kb0, kbn);
+    for (int k = kbn - 1; k >= 0; --k) {
+      if (tid < kTrailCols) sX[(kb0 + k) + tid * m] /= sD[k + k * kPanelNb];
+      __syncthreads();
+      for (int e = tid; e < k * kTrailCols; e += nt) {
+        const int i = e % k, c = e / k;
+        sX[(kb0 + i) + c * m] -= sX[(kb0 + k) + c * m] * sD[i + k * kPanelNb];
+      }
+      __syncthreads();
+    }
+    if (kb0 > 0) panel_update(kb0, kbn, 0, kb0);
+  }
+  __syncthreads();
+  T *out = Dinv + (long long)leaf * m * m;
+  for (int e = tid; e < m * nc; e += nt) {
+    const int i = e % m, c = e / m;
+    out[i + (long long)(c0 + c) * m] = sX[i + c * m];
+  }
 }
+
+size_t leaf_inverse_blocked_smem(int m, int elem_bytes) {
+  return (size_t)elem_bytes * ((size_t)m * kTrailCols + (size_t)kTrailRows * kPanelNb + (size_t)kPanelNb * kPanelNb);
+}
+
+template <typename T>
+cudaError_t launch_leaf_inverse_blocked(const T *LU, const int *ipiv, int m, int nleaf, T *Dinv, cudaStream_t s) {
+  const size_t bytes = leaf_inverse_blocked_smem(m, sizeof(T));
+  cudaError_t e = set_dyn_smem(leaf_inverse_blocked_kernel<T>, bytes);
+  if (e != cudaSuccess) return e;
+  dim3 grid(ceil_div(m, kTrailCols), nleaf);
+  HODLR_LAUNCH(leaf_inverse_blocked_kernel<T>, grid, 256, bytes, s, LU, ipiv, m, Dinv);
+  return cudaGetLastError();
+}
+
+template cudaError_t launch_leaf_inverse_blocked<double>(const double *, const int *, int, int, double *,
+                                                         cudaStream_t);
+template cudaError_t launch_leaf_inverse_blocked<float>(const float *, const int *, int, int, float *, cudaStream_t);
+
 
 template <typename T>
 cudaError_t launch_leaf_getrf_blocked(const double *D, long long d_ld, long long d_stride, T *LU, int *ipiv, int m,

@@ -206,9 +206,11 @@ update_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant
       tile_of(i, rt, ct, b);
       const float *sA = reinterpret_cast<const float *>(base + s * kStageBytes);  // [kKS][kBM]
       const float *sE = reinterpret_cast<const float *>(base + s * kStageBytes + kABytes32 + WsCfg::kCBytes);
+      constexpr int kEtaTasks = 4 * kBN;  // column j of C, 8 K values per task (fewer tasks than threads at BN 32)
 #pragma unroll
-      for (int t = 0; t < 4 * kBN / kSplitThreads; ++t) {  // eta planes: column j of C, 8 K values per task
+      for (int t = 0; t < (kEtaTasks + kSplitThreads - 1) / kSplitThreads; ++t) {  // eta planes
         const int task = tid + kSplitThreads * t, j = task >> 2, c = task & 3, jg = ct * kBN + j;
+        if (task >= kEtaTasks) continue;
         const float4 e0 = *reinterpret_cast<const float4 *>(sE + j * kKS + 8 * c);
         const float4 e1 = *reinterpret_cast<const float4 *>(sE + j * kKS + 8 * c + 4);
         float x[8] = {e0.x, e0.y, e0.z, e0.w, e1.x, e1.y, e1.z, e1.w};
@@ -314,7 +316,11 @@ bool update_tc_try(const UpdateArgs &a, DevStatus *st, cudaStream_t s, cudaError
       a.M % kBM || a.nbatch % 2 || a.b_s1 != (long long)a.ldb * a.N || a.b_s2 % 4 || a.ldb < 2 * a.b_s2)
     return false;
   bool done = false;
-  err = update_tc_launch<64, 3, 8>(a, st, s, done);
+  switch (current_tuning().upd_tc_shape) {
+    case 1: err = update_tc_launch<64, 2, 8>(a, st, s, done); break;
+    case 2: err = update_tc_launch<32, 5, 8>(a, st, s, done); break;
+    default: err = update_tc_launch<64, 3, 8>(a, st, s, done); break;
+  }
   return done || err != cudaSuccess;
 }
 

@@ -402,7 +402,9 @@ HODLR_API int hodlr_batch_stats(hodlr_batch b, int *nforests, double *factor_ms,
 
 /* ------------------------------------------------------------ autotuner
  * Launch shapes of the tunable kernels: the split-K target of the row
- * reductions (CTAs per SM) and the row tile of the FP32 low-rank update.
+ * reductions (CTAs per SM), the row tile of the FP32-FMA low-rank update,
+ * the tile and ring depth of the tensor-core update and the warps per
+ * capacitance system of the mixed path.
  * No counterpart in the reference (its BLAS calls have no launch shapes).
  * hodlr_autotune times complete factor + solve sweeps of the handle's own
  * inputs (a seeded scratch right-hand side of nrhs columns) for a coordinate
@@ -415,6 +417,9 @@ HODLR_API int hodlr_batch_stats(hodlr_batch b, int *nforests, double *factor_ms,
 typedef struct hodlr_tuning {
   int32_t red_ctas_per_sm;   /* 2, 4 or 8 */
   int32_t update_tile_rows;  /* 0 (128 where the blocks allow it, else 64) or 64 */
+  int32_t cap_warps;         /* mixed path, 2r <= 64: warps per capacitance system, 8 or 16 (0 = 8) */
+  int32_t update_tc_shape;   /* tensor-core update: 0 = 128x64 tiles through a 3-stage ring,
+                                1 = 128x64 tiles, 2 stages, 2 = 128x32 tiles, 5 stages */
   double ms;                 /* autotune: factor + solve milliseconds with these shapes */
 } hodlr_tuning;
 

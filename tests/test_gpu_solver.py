@@ -448,7 +448,9 @@ def test_autotune_picks_valid_shapes_and_keeps_results(hodlr, precision):
     s = make_solver(hodlr, pr, precision=precision)
     t = s.autotune(nrhs=4)
     assert t["red_ctas_per_sm"] in (2, 4, 8) and t["update_tile_rows"] in (0, 64) and t["ms"] > 0
-    assert s.get_tuning()["red_ctas_per_sm"] == t["red_ctas_per_sm"]
+    assert t["cap_warps"] in (8, 16) and t["update_tc_shape"] in (0, 1, 2)
+    got = s.get_tuning()
+    assert all(got[key] == t[key] for key in ("red_ctas_per_sm", "update_tile_rows", "cap_warps", "update_tc_shape"))
     B = to_dev(pr.B)
     s.solve(B)   # autotune left the handle factored
     Xo, _, _ = O.hsolve_general(pr, pr.B)
@@ -461,6 +463,28 @@ def test_autotune_picks_valid_shapes_and_keeps_results(hodlr, precision):
             B2 = to_dev(pr.B)
             s.solve(B2)
             assert rel(to_host(B2), Xo) < (1e-12 if precision == 0 else 1e-10)
+
+
+@pytest.mark.parametrize("r", [16, 32, 48, 64])
+def test_capacitance_and_update_shapes_keep_results(hodlr, r):
+    """The mixed path's tuned kernel shapes (warps per capacitance system;
+    tensor-core update tile and ring depth) change only rounding: each reaches
+    the refinement target and agrees with the oracle's FP64 solve."""
+    pr = P.gaussian_problem(128, 5, r, nrhs=5, seed=40 + r, orthonormal=True, decay=3.0, shift=1.5)
+    s = make_solver(hodlr, pr, precision=hodlr.PREC_MIXED, refine_tol=1e-12)
+    Xo, _, _ = O.hsolve_general(pr, pr.B)
+    for warps in (8, 16):
+        for shape in (0, 1, 2):
+            s.set_tuning(cap_warps=warps, update_tc_shape=shape)
+            assert s.get_tuning()["cap_warps"] == warps and s.get_tuning()["update_tc_shape"] == shape
+            s.factor()
+            B = to_dev(pr.B)
+            info = s.solve(B)
+            assert info.rel_residual <= 1e-12
+            assert rel(to_host(B), Xo) < 1e-9
+    with pytest.raises(hodlr.HodlrError):
+        s.set_tuning(cap_warps=12)
+    s.close()
 
 
 @pytest.mark.parametrize("m,L,r,k", [(128, 6, 32, 4), (64, 5, 16, 3), (256, 3, 64, 2), (128, 4, 24, 70)])
