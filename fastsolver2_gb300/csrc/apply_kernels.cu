@@ -23,8 +23,7 @@ static constexpr size_t kSmemCap = 220 * 1024;
 
 template <typename K>
 static cudaError_t set_smem(K kernel, size_t bytes) {
-  if (bytes <= 48 * 1024) return cudaSuccess;
-  return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  return allow_dyn_smem(kernel, bytes);
 }
 
 // --------------------------------------------------------- leaf inverse

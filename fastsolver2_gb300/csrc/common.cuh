@@ -41,6 +41,16 @@ void debug_after_launch(const char *name, cudaStream_t s);
 
 inline int ceil_div(long long a, long long b) { return (int)((a + b - 1) / b); }
 
+// Lets `func` (a __global__ function) take up to the device's opt-in shared
+// memory per block, less its static shared memory.  The attribute is only an
+// upper bound -- each launch's own size decides occupancy -- so it is raised
+// once per (function, device) and never lowered: a graph captured with a
+// large launch stays launchable after the same kernel ran with a smaller size.
+cudaError_t allow_max_dyn_smem(const void *func);
+template <typename K> inline cudaError_t allow_dyn_smem(K kernel, size_t bytes) {
+  return bytes <= 48 * 1024 ? cudaSuccess : allow_max_dyn_smem(reinterpret_cast<const void *>(kernel));
+}
+
 // Launch shape of an n x c column-major elementwise pass: blockIdx.y strides
 // over columns, x over rows (no 64-bit index division in the kernels).
 inline dim3 grid2d(long long n, int c) {

@@ -109,10 +109,8 @@ __global__ void chol_inv_kernel(const double *G, double *Rinv, int r, DevStatus 
 
 cudaError_t launch_chol_inv(const double *G, double *Rinv, int r, int nbatch, DevStatus *st, cudaStream_t s) {
   const size_t bytes = (size_t)2 * r * r * sizeof(double);
-  if (bytes > 48 * 1024) {
-    cudaError_t e = cudaFuncSetAttribute(chol_inv_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
-    if (e != cudaSuccess) return e;
-  }
+  cudaError_t e = allow_dyn_smem(chol_inv_kernel, bytes);
+  if (e != cudaSuccess) return e;
   HODLR_LAUNCH(chol_inv_kernel, nbatch, 64, bytes, s, G, Rinv, r, st);
   return cudaGetLastError();
 }

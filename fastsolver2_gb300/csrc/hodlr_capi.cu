@@ -21,6 +21,8 @@
 #include <cstdlib>
 #include <cstring>
 #include <map>
+#include <mutex>
+#include <set>
 #include <string>
 #include <tuple>
 #include <vector>
@@ -32,6 +34,24 @@
 namespace hodlr {
 static std::atomic<long long> g_launches{0};
 void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+
+cudaError_t allow_max_dyn_smem(const void *func) {
+  static std::mutex mu;
+  static std::set<std::pair<const void *, int>> done;
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  std::lock_guard<std::mutex> lock(mu);
+  if (done.count({func, dev})) return cudaSuccess;
+  cudaFuncAttributes fa;
+  int optin = 0;
+  e = cudaFuncGetAttributes(&fa, func);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize, optin - (int)fa.sharedSizeBytes);
+  if (e == cudaSuccess) done.insert({func, dev});
+  return e;
+}
 bool debug_sync() {
   static const bool on = [] {
     const char *v = getenv("HODLR_DEBUG_SYNC");

@@ -22,8 +22,7 @@ constexpr int kTrailRows = 128;   // rows of L21 staged per pass
 
 template <typename T>
 static cudaError_t set_dyn_smem(T kernel, size_t bytes) {
-  if (bytes <= 48 * 1024) return cudaSuccess;
-  return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  return allow_dyn_smem(kernel, bytes);
 }
 
 // LU[leaf] = (T) D[leaf]; the first non-finite entry is reported.
@@ -212,10 +211,12 @@ __global__ void __launch_bounds__(256) leaf_trail_kernel(T *LU, int m, int j0, i
 // unit-lower solve (32-row diagonal blocks in DTRSM's order, the rows below
 // updated by the block's L panel in passes of 128 rows) and a blocked upper
 // solve from the bottom (diagonal blocks by division, the rows above updated
-// by the block's U panel) -- the DGETRS order on the identity.
+// by the block's U panel) -- the DGETRS order on the identity.  (For solves
+// with a few right-hand sides the one-CTA-per-column-tile kernel of
+// launch_leaf_getrs, which spreads the columns over every SM, is faster.)
 template <typename T>
-__global__ void __launch_bounds__(256) leaf_inverse_blocked_kernel(const T *__restrict__ LU, const int *__restrict__ ipiv,
-                                                                   int m, T *Dinv) {
+__global__ void __launch_bounds__(256) leaf_inverse_blocked_kernel(const T *__restrict__ LU,
+                                                                   const int *__restrict__ ipiv, int m, T *Dinv) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T *sX = reinterpret_cast<T *>(smem_raw);                 // m x 32, ld m
   T *sP = sX + (size_t)m * kTrailCols;                      // panel pass: 128 x 32, [k * 128 + r]
@@ -224,6 +225,7 @@ __global__ void __launch_bounds__(256) leaf_inverse_blocked_kernel(const T *__re
   const T *A = LU + (long long)leaf * m * m;
   const int *piv = ipiv + (long long)leaf * m;
   const int c0 = blockIdx.x * kTrailCols, nc = min(kTrailCols, m - c0);
+  T *out = Dinv + (long long)leaf * m * m + (long long)c0 * m;
   for (int e = tid; e < m * kTrailCols; e += nt) {
     const int i = e % m, c = e / m;
     sX[e] = (c < nc && i == c0 + c) ? T(1) : T(0);
@@ -309,10 +311,9 @@ __global__ void __launch_bounds__(256) leaf_inverse_blocked_kernel(const T *__re
     if (kb0 > 0) panel_update(kb0, kbn, 0, kb0);
   }
   __syncthreads();
-  T *out = Dinv + (long long)leaf * m * m;
   for (int e = tid; e < m * nc; e += nt) {
     const int i = e % m, c = e / m;
-    out[i + (long long)(c0 + c) * m] = sX[i + c * m];
+    out[i + (long long)c * m] = sX[i + c * m];
   }
 }
 

@@ -176,7 +176,7 @@ static cudaError_t launch_tree_nodes(const TreeNode *nodes, int node_base, int c
                                      bool factor, int nrhs, double *lu, int *ipiv, double *eta, DevStatus *st,
                                      cudaStream_t s) {
   const size_t bytes = tree_node_smem(nmax);
-  cudaError_t e = cudaFuncSetAttribute(tree_node_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  cudaError_t e = allow_dyn_smem(tree_node_kernel, bytes);
   if (e != cudaSuccess) return e;
   HODLR_LAUNCH(tree_node_kernel, count, 256, bytes, s, nodes, node_base, red, (int)factor, nrhs, lu, ipiv, eta,
                st);
