@@ -169,6 +169,7 @@ struct hodlr_ctx {
   // hodlr_set_lowrank): pst, the copy-done event, one prepared event per input
   // (leaf blocks, then level l at 1 + l), and the last one enqueued
   cudaStream_t pst = nullptr;
+  cudaStream_t cst = nullptr;  // captures the body of the refinement loop's conditional graph node
   cudaEvent_t pcopy = nullptr, plast = nullptr;
   std::vector<cudaEvent_t> pready;
   // mixed mode: the leaf LU (+ inverses) started on the side stream as soon
@@ -317,6 +318,7 @@ static void free_ctx(hodlr_ctx *h) {
     if (e) cudaEventDestroy(e);
   if (h->pcopy) cudaEventDestroy(h->pcopy);
   if (h->pst) cudaStreamDestroy(h->pst);
+  if (h->cst) cudaStreamDestroy(h->cst);
   if (h->own_stream && h->st) cudaStreamDestroy(h->st);
   delete h;
 }
@@ -819,64 +821,136 @@ static int residual(hodlr_ctx *h, bool trans, const double *X, long long ldx, co
   return matvec_fp64(h, trans, X, ldx, B, ldb, R, ldr, k, -1.0, skip);
 }
 
+// While the handle's stream is being captured (and no per-phase event nodes
+// are recorded, which conditional bodies cannot hold): a graph conditional
+// node of type WHILE whose body, captured from body() on the handle's body
+// stream, runs again as long as a kernel of it (or one before the node) sets
+// the condition.  Returns false in *used when the stream is not capturing.
+static bool capturing_plain(hodlr_ctx *h) {
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing(h->st, &cs) != cudaSuccess) return false;
+  return cs == cudaStreamCaptureStatusActive && !h->profile;
+}
+
+static int cond_create(hodlr_ctx *h, cudaGraphConditionalHandle *hc) {
+  cudaStreamCaptureStatus cs;
+  cudaGraph_t g = nullptr;
+  CK(cudaStreamGetCaptureInfo(h->st, &cs, nullptr, &g, nullptr, nullptr, nullptr));
+  CK(cudaGraphConditionalHandleCreate(hc, g, 0, cudaGraphCondAssignDefault));
+  return HODLR_OK;
+}
+
+template <typename F>
+static int cond_while(hodlr_ctx *h, cudaGraphConditionalHandle hc, F body) {
+  cudaStreamCaptureStatus cs;
+  cudaGraph_t g = nullptr;
+  const cudaGraphNode_t *deps = nullptr;
+  size_t nd = 0;
+  CK(cudaStreamGetCaptureInfo(h->st, &cs, nullptr, &g, &deps, nullptr, &nd));
+  cudaGraphNodeParams p = {};
+  p.type = cudaGraphNodeTypeConditional;
+  p.conditional.handle = hc;
+  p.conditional.type = cudaGraphCondTypeWhile;
+  p.conditional.size = 1;
+  cudaGraphNode_t node;
+  CK(cudaGraphAddNode(&node, g, deps, nullptr, nd, &p));
+  CK(cudaStreamUpdateCaptureDependencies(h->st, &node, nullptr, 1, cudaStreamSetCaptureDependencies));
+  if (!h->cst) CK(cudaStreamCreateWithFlags(&h->cst, cudaStreamNonBlocking));
+  cudaGraph_t bg = p.conditional.phGraph_out[0];
+  CK(cudaStreamBeginCaptureToGraph(h->cst, bg, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+  cudaStream_t main = h->st;
+  h->st = h->cst;
+  const int rc = body();
+  h->st = main;
+  cudaGraph_t out = nullptr;
+  const cudaError_t ce = cudaStreamEndCapture(h->cst, &out);
+  CKS(rc);
+  CK(ce);
+  return HODLR_OK;
+}
+
 // Mixed-precision solve with FP64 iterative refinement.  B (FP64, n x k) is
-// overwritten by X.  All control stays on the device: the refinement check
-// sets st->done, which predicates every later kernel, so the whole loop is
-// one stream-ordered (graph-capturable) sequence.
+// overwritten by X.  All control stays on the device.  Run eagerly, the loop
+// is unrolled to its maximum length and the refinement check sets st->done,
+// which predicates every later kernel.  Captured into a graph, the first
+// residual and check run once and the corrections are the body of a WHILE
+// conditional node, repeated only while the check asks for another one.
 static int mixed_solve(hodlr_ctx *h, double *B, long long ldb, int k, bool trans) {
   const long long n = h->n;
-  cudaStream_t s = h->st;
   const int *done = &h->dst->done;
   double *bn = h->norms, *rn = h->norms + (size_t)h->kmax * h->nsys;
   const int maxit = std::max(0, h->d.refine_max_iter);
+  const bool cond = capturing_plain(h) && maxit > 0;
+  cudaGraphConditionalHandle hc = 0;
+  if (cond) CKS(cond_create(h, &hc));
   // the double-word residuals land in R2, and their norms and the next
   // right-hand side come from one fused pass; the tensor-core residual also
   // folds the correction into the slicing of the iterate
   const bool fused = h->emulated || (h->oz && !trans);
   const bool tensor = h->oz && !trans;
-  if (fused) {
-    const int P = h->forest ? h->nleaf : 64;
-    const int *seg = h->forest ? h->seg_leaf : nullptr;
-    PHASE(h, HODLR_PHASE_MISC, launch_rhs_prepare(B, ldb, n, k, P, h->B64, h->X32, h->nwork, s));
-    PHASE(h, HODLR_PHASE_MISC, launch_partial_norms(h->nwork, P, k, seg, h->nsys, bn, nullptr, s));
-    CKS(solve_sweep<float>(h, h->X32, n, k, trans, nullptr));
-    if (!tensor) PHASE(h, HODLR_PHASE_MISC, (launch_convert<float, double>(h->X32, n, h->X64, n, n, k, s)));
-    for (int it = 0; it <= maxit; ++it) {
+  const int P = h->forest ? h->nleaf : 64;
+  const int *seg = h->forest ? h->seg_leaf : nullptr;
+  auto norms = [&](const double *X, double *out, const int *skip) {
+    if (!h->forest) return launch_colnorms(X, n, n, k, out, h->nwork, skip, h->st);
+    return launch_seg_colnorms(X, n, h->m, h->nleaf, k, h->seg_leaf, h->nsys, out, h->nwork, skip, h->st);
+  };
+  // residual of the current iterate, its norms (and, fused, the next right-hand side)
+  auto resid_step = [&](bool first) -> int {
+    if (fused) {
       if (tensor)
-        CKS(residual_tensor(h, h->X64, n, h->B64, n, nullptr, n, k, done, h->X32, it == 0));
+        CKS(residual_tensor(h, h->X64, n, h->B64, n, nullptr, n, k, done, h->X32, first));
       else
         CKS(residual(h, trans, h->X64, n, h->B64, n, nullptr, n, k, done));
-      PHASE(h, HODLR_PHASE_MISC, launch_resid_finish(h->R2, n, k, P, h->X32, h->nwork, done, s));
-      PHASE(h, HODLR_PHASE_MISC, launch_partial_norms(h->nwork, P, k, seg, h->nsys, rn, done, s));
-      CK(launch_refine_check(rn, bn, k * h->nsys, h->d.refine_tol, h->dst, it < maxit ? 1 : 0, s));
-      if (it == maxit) break;
-      CKS(solve_sweep<float>(h, h->X32, n, k, trans, done));
-      if (!tensor)
-        PHASE(h, HODLR_PHASE_MISC, (launch_add_correction<float>(h->X64, n, h->X32, n, h->X64, n, n, k, done, s)));
+      PHASE(h, HODLR_PHASE_MISC, launch_resid_finish(h->R2, n, k, P, h->X32, h->nwork, done, h->st));
+      PHASE(h, HODLR_PHASE_MISC, launch_partial_norms(h->nwork, P, k, seg, h->nsys, rn, done, h->st));
+    } else {
+      CKS(residual(h, trans, h->X64, n, h->B64, n, h->R64, n, k, done));
+      CK(norms(h->R64, rn, done));
     }
-    CK(launch_axpy(h->X64, n, B, ldb, n, k, 1.0, false, nullptr, s));
     return HODLR_OK;
-  }
-  // native FP64 residual
-  auto norms = [&](const double *X, double *out, const int *skip) {
-    if (!h->forest) return launch_colnorms(X, n, n, k, out, h->nwork, skip, s);
-    return launch_seg_colnorms(X, n, h->m, h->nleaf, k, h->seg_leaf, h->nsys, out, h->nwork, skip, s);
   };
-  CK(launch_axpy(B, ldb, h->B64, n, n, k, 1.0, false, nullptr, s));
-  CK(norms(h->B64, bn, nullptr));
-  CK((launch_convert<double, float>(h->B64, n, h->X32, n, n, k, s)));
-  CKS(solve_sweep<float>(h, h->X32, n, k, trans, nullptr));
-  CK((launch_convert<float, double>(h->X32, n, h->X64, n, n, k, s)));
-  for (int it = 0; it <= maxit; ++it) {
-    CKS(residual(h, trans, h->X64, n, h->B64, n, h->R64, n, k, done));
-    CK(norms(h->R64, rn, done));
-    CK(launch_refine_check(rn, bn, k * h->nsys, h->d.refine_tol, h->dst, it < maxit ? 1 : 0, s));
-    if (it == maxit) break;
-    CK((launch_convert<double, float>(h->R64, n, h->X32, n, n, k, s)));
+  // a correction: the FP32 sweep on the residual, added to the iterate
+  auto correction = [&]() -> int {
+    if (!fused) CK((launch_convert<double, float>(h->R64, n, h->X32, n, n, k, h->st)));
     CKS(solve_sweep<float>(h, h->X32, n, k, trans, done));
-    CK((launch_add_correction<float>(h->X64, n, h->X32, n, h->X64, n, n, k, done, s)));
+    if (!tensor)
+      PHASE(h, HODLR_PHASE_MISC,
+            (launch_add_correction<float>(h->X64, n, h->X32, n, h->X64, n, n, k, done, h->st)));
+    return HODLR_OK;
+  };
+  auto check = [&](int it) -> int {
+    if (cond) CK(launch_refine_check_cond(rn, bn, k * h->nsys, h->d.refine_tol, h->dst, maxit, hc, h->st));
+    else CK(launch_refine_check(rn, bn, k * h->nsys, h->d.refine_tol, h->dst, it < maxit ? 1 : 0, h->st));
+    return HODLR_OK;
+  };
+  if (fused) {
+    PHASE(h, HODLR_PHASE_MISC, launch_rhs_prepare(B, ldb, n, k, P, h->B64, h->X32, h->nwork, h->st));
+    PHASE(h, HODLR_PHASE_MISC, launch_partial_norms(h->nwork, P, k, seg, h->nsys, bn, nullptr, h->st));
+    CKS(solve_sweep<float>(h, h->X32, n, k, trans, nullptr));
+    if (!tensor) PHASE(h, HODLR_PHASE_MISC, (launch_convert<float, double>(h->X32, n, h->X64, n, n, k, h->st)));
+  } else {  // native FP64 residual
+    CK(launch_axpy(B, ldb, h->B64, n, n, k, 1.0, false, nullptr, h->st));
+    CK(norms(h->B64, bn, nullptr));
+    CK((launch_convert<double, float>(h->B64, n, h->X32, n, n, k, h->st)));
+    CKS(solve_sweep<float>(h, h->X32, n, k, trans, nullptr));
+    CK((launch_convert<float, double>(h->X32, n, h->X64, n, n, k, h->st)));
   }
-  CK(launch_axpy(h->X64, n, B, ldb, n, k, 1.0, false, nullptr, s));
+  CKS(resid_step(true));
+  CKS(check(0));
+  if (cond) {
+    CKS(cond_while(h, hc, [&]() -> int {
+      CKS(correction());
+      CKS(resid_step(false));
+      return check(1);
+    }));
+  } else {
+    for (int it = 1; it <= maxit; ++it) {
+      CKS(correction());
+      CKS(resid_step(false));
+      CKS(check(it));
+    }
+  }
+  CK(launch_axpy(h->X64, n, B, ldb, n, k, 1.0, false, nullptr, h->st));
   return HODLR_OK;
 }
 

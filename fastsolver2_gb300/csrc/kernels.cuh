@@ -225,6 +225,11 @@ cudaError_t launch_scatter_rhs(const RhsCopy *tab, int count, long long maxn, co
 // if rel <= tol set st->done = 1.  If advance, count an iteration when not done.
 cudaError_t launch_refine_check(const double *rnorm, const double *bnorm, int c, double tol,
                                 DevStatus *st, int advance, cudaStream_t s);
+// The same check inside a captured graph's refinement loop: unless done, a
+// correction is counted while fewer than maxit were applied, and the graph's
+// loop condition `cond` is set to whether one follows.
+cudaError_t launch_refine_check_cond(const double *rnorm, const double *bnorm, int c, double tol, DevStatus *st,
+                                     int maxit, cudaGraphConditionalHandle cond, cudaStream_t s);
 // Scan X (n x c) for NaN/Inf; report HODLR_ERR_NONFINITE_INPUT with the row.
 cudaError_t launch_check_finite(const double *X, long long ldx, long long n, int c, DevStatus *st,
                                 cudaStream_t s);

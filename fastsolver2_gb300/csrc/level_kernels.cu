@@ -368,6 +368,34 @@ cudaError_t launch_refine_check(const double *rnorm, const double *bnorm, int c,
   return cudaGetLastError();
 }
 
+__global__ void refine_check_cond_kernel(const double *rnorm, const double *bnorm, int c, double tol,
+                                         DevStatus *st, int maxit, cudaGraphConditionalHandle cond) {
+  if (threadIdx.x != 0) return;
+  unsigned more = 0;
+  if (!st->done) {
+    double rel = 0.0;
+    for (int j = 0; j < c; ++j) {
+      const double b = bnorm[j] > 0.0 ? bnorm[j] : 1.0;
+      const double q = rnorm[j] / b;
+      rel = (q > rel || q != q) ? q : rel;
+    }
+    st->resid = rel;
+    if (rel <= tol) {
+      st->done = 1;
+    } else if (st->iters < maxit) {
+      st->iters += 1;
+      more = 1;
+    }
+  }
+  cudaGraphSetConditional(cond, more);
+}
+
+cudaError_t launch_refine_check_cond(const double *rnorm, const double *bnorm, int c, double tol, DevStatus *st,
+                                     int maxit, cudaGraphConditionalHandle cond, cudaStream_t s) {
+  HODLR_LAUNCH(refine_check_cond_kernel, 1, 32, 0, s, rnorm, bnorm, c, tol, st, maxit, cond);
+  return cudaGetLastError();
+}
+
 __global__ void check_finite_kernel(const double *X, long long ldx, long long n, int c, DevStatus *st) {
   HODLR_FOR_2D(i, j, n, c) {
     if (!isfinite(X[i + j * ldx])) report_error(st, HODLR_ERR_NONFINITE_INPUT, i);
