@@ -574,3 +574,43 @@ def test_unequal_sibling_ranks_by_zero_padding(hodlr, precision, rank0, rank1):
     assert rel(X, Xd) < (1e-11 if precision == 0 else 1e-10)
     if precision == 1:
         assert info.rel_residual <= 1e-12
+
+
+@pytest.mark.parametrize("resid", [0, 1, 2])
+def test_refinement_loop_same_eager_captured_replayed(hodlr, resid):
+    """The first solve runs the refinement loop unrolled and predicated; the
+    second captures it as a graph conditional WHILE node, the third replays
+    it.  An unreachable tolerance makes the loop run all refine_max_iter
+    corrections and stop with HODLR_ERR_NOT_CONVERGED every time, leaving
+    the same iterate; a reachable one gives bitwise-equal solutions."""
+    pr = P.gaussian_problem(128, 5, 32, nrhs=3, seed=5, orthonormal=True, decay=6.0, shift=1.5)
+    s = make_solver(hodlr, pr, precision=hodlr.PREC_MIXED, residual=resid, refine_tol=1e-30, refine_max_iter=3)
+    s.factor()
+    B0 = to_dev(pr.B)
+    B = to_dev(pr.B)   # one buffer: solve graphs are cached per right-hand-side pointer
+    outs = []
+    for _ in range(3):
+        B.copy_(B0)
+        torch.cuda.synchronize()   # the library runs on its own stream
+        with pytest.raises(hodlr.HodlrError) as e:
+            s.solve(B)
+        assert e.value.code == hodlr.HODLR_ERR_NOT_CONVERGED
+        assert "after 3 corrections" in str(e.value)
+        outs.append(to_host(B))
+    np.testing.assert_array_equal(outs[0], outs[1])
+    np.testing.assert_array_equal(outs[0], outs[2])
+    s.close()
+    s = make_solver(hodlr, pr, precision=hodlr.PREC_MIXED, residual=resid, refine_tol=1e-12, refine_max_iter=10)
+    s.factor()
+    outs, its = [], []
+    for _ in range(3):
+        B.copy_(B0)
+        torch.cuda.synchronize()   # the library runs on its own stream
+        info = s.solve(B)
+        assert info.rel_residual <= 1e-12
+        outs.append(to_host(B))
+        its.append(info.iterations)
+    assert its[0] == its[1] == its[2] >= 1
+    np.testing.assert_array_equal(outs[0], outs[1])
+    np.testing.assert_array_equal(outs[0], outs[2])
+    s.close()
