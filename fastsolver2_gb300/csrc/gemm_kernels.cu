@@ -98,6 +98,13 @@ static constexpr int kRedBK = 32;   // rows staged per step
 static thread_local const Tuning *g_tuning = nullptr;
 static const Tuning kDefaultTuning{};
 const Tuning &current_tuning() { return g_tuning ? *g_tuning : kDefaultTuning; }
+
+long long persistent_ctas(long long units) {
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  return std::max<long long>(1, std::min<long long>(units, sms > 0 ? sms : kNumSMs));
+}
 TuningScope::TuningScope(const Tuning *t) : prev(g_tuning) { g_tuning = t; }
 TuningScope::~TuningScope() { g_tuning = prev; }
 

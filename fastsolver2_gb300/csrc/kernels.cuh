@@ -21,6 +21,11 @@ struct Tuning {
 constexpr int kMaxRedCtasPerSm = 8;
 constexpr int kNumSMs = 152;
 const Tuning &current_tuning();
+// CTAs of a persistent launch over `units` work items: one per SM, at most
+// one per unit.  The persistent kernels stride over their units by the grid
+// size and write per unit, so the grid changes only how the units are shared
+// out, never the results.
+long long persistent_ctas(long long units);
 struct TuningScope {
   const Tuning *prev;
   explicit TuningScope(const Tuning *t);

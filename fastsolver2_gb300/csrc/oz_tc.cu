@@ -650,10 +650,7 @@ static cudaError_t launch_mode(int mode, const CUtensorMap &a0, const CUtensorMa
   auto kern = mode == 0 ? oz_tc_kernel<0> : oz_tc_kernel<1>;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
   if (e != cudaSuccess) return e;
-  int dev = 0, sms = 0;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  const long long grid = std::min<long long>(a.items, sms > 0 ? sms : 148);
+  const long long grid = persistent_ctas(a.items);
   HODLR_LAUNCH(kern, (unsigned)grid, kThreads, bytes, s, a0, b0, a1, b1, a);
   return cudaGetLastError();
 }

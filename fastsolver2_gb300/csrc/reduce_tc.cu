@@ -391,10 +391,7 @@ bool reduce_tc_try(const float *V, long long ldv, const float *X, long long ldx,
   ra.nunits = (long long)ra.nct * nchunks * nbatch;
   ra.skip = skip;
   ra.st = st;
-  int dev = 0, sms = 0;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  const long long grid = std::min<long long>(ra.nunits, sms > 0 ? sms : 148);
+  const long long grid = persistent_ctas(ra.nunits);
   HODLR_LAUNCH(k, (unsigned)grid, kRcThreads, kRcSmem, s, mx, mv, ra, dst);
   err = cudaGetLastError();
   return true;

@@ -300,10 +300,7 @@ static cudaError_t update_tc_launch(const UpdateArgs &a, DevStatus *st, cudaStre
     attr = true;
   }
   const long long ntiles = (long long)nrt * nct * a.nbatch;
-  int dev = 0, sms = 0;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  const long long grid = std::min<long long>(ntiles, sms > 0 ? sms : 148);
+  const long long grid = persistent_ctas(ntiles);
   HODLR_LAUNCH(k, (unsigned)grid, ws_threads(SW), WsCfg::kSmem, s, ma, mc, me, a, nrt, nct, ntiles, st);
   return cudaGetLastError();
 }
