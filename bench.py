@@ -250,8 +250,11 @@ def run_ours(args, wl):
     launches0 = fs.kernel_launches()
     ffma_tf, dfma_tf, mma_tf = probe_peaks()   # live FMA-pipe and warp-level bf16 MMA rates
     with torch.cuda.stream(stream):
+        # FLAG_STREAM_INPUTS: in the e2e leg the host V of each level is copied
+        # by the factorisation, beside the levels below it
         mixed = fs.Solver(n, m, L, r, nrhs_max=k, precision=fs.PREC_MIXED, residual=args.resid,
-                          refine_tol=1e-12, refine_max_iter=10, stream=sp)
+                          refine_tol=1e-12, refine_max_iter=10, stream=sp,
+                          flags=0 if args.plain_inputs else fs.FLAG_STREAM_INPUTS)
         B0 = colmajor(n, k)
         mixed.generate(SEED + rank, shift=1.5, orthonormal=True, decay=6.0, B=B0)
         B = colmajor(n, k)
@@ -958,6 +961,8 @@ def main():
     ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 comparator")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--plain-inputs", action="store_true",
+                    help="e2e: copy every input when it is set (no V streamed in by the factorisation)")
     ap.add_argument("--no-ragged", action="store_true", help="skip the 512-system ragged batch")
     ap.add_argument("--no-tune", action="store_true", help="default launch shapes (no autotuning pass)")
     ap.add_argument("--no-phase-timing", action="store_true",

@@ -23,6 +23,8 @@ HODLR_ERR_TIMEOUT = 7
 HODLR_ERR_NOT_FACTORED = 8
 HODLR_ERR_OUT_OF_MEMORY = 9
 
+FLAG_STREAM_INPUTS = 1
+
 PREC_FP64 = 0
 PREC_MIXED = 1
 RESID_FP64 = 0
@@ -199,9 +201,9 @@ class Solver:
     device work when it returns."""
 
     def __init__(self, n, leaf, levels, rank, nrhs_max=1, precision=PREC_FP64, residual=RESID_FP64_TENSOR,
-                 refine_tol=1e-12, refine_max_iter=10, stream=None):
+                 refine_tol=1e-12, refine_max_iter=10, stream=None, flags=0):
         self.h = None
-        self.desc = Desc(n, leaf, levels, rank, nrhs_max, precision, residual, refine_tol, refine_max_iter, 0,
+        self.desc = Desc(n, leaf, levels, rank, nrhs_max, precision, residual, refine_tol, refine_max_iter, flags,
                          stream)
         h = ctypes.c_void_p()
         check(lib().hodlr_create(ctypes.byref(self.desc), ctypes.byref(h)))

@@ -170,6 +170,15 @@ struct hodlr_ctx {
   // (leaf blocks, then level l at 1 + l), and the last one enqueued
   cudaStream_t pst = nullptr;
   cudaStream_t cst = nullptr;  // captures the body of the refinement loop's conditional graph node
+  // HODLR_FLAG_STREAM_INPUTS: per level, the pinned host source of a V whose
+  // copy waits for the next factorisation (nullptr: V is on the device); the
+  // factorisation copies them deepest level first on the side stream, level l
+  // signalling vready[l], while the sweep runs
+  std::vector<const double *> vsrc;
+  std::vector<int64_t> vsrc_ld;
+  std::vector<cudaEvent_t> vready;
+  cudaEvent_t vfork = nullptr;
+  std::vector<const double *> sv_captured;  // the sources the streamed factor graphs copy from
   cudaEvent_t pcopy = nullptr, plast = nullptr;
   std::vector<cudaEvent_t> pready;
   // mixed mode: the leaf LU (+ inverses) started on the side stream as soon
@@ -185,6 +194,8 @@ struct hodlr_ctx {
   bool use_graphs = true;
   int factor_runs = 0;
   GraphEntry factor_graph;
+  int factor_sv_runs = 0, factor_sv_nl_runs = 0;  // with the V copies streamed in (HODLR_FLAG_STREAM_INPUTS)
+  GraphEntry factor_sv_graph, factor_sv_nl_graph;
   int factor_nl_runs = 0;  // the factorisation without its leaf LU (leaves_prefactored)
   GraphEntry factor_nl_graph;
   std::map<std::tuple<const double *, long long, int, int>, GraphEntry> solve_graphs;
@@ -233,6 +244,16 @@ struct hodlr_ctx {
   Tuning tune;              // launch shapes of the tunable kernels (hodlr_autotune)
 };
 
+static void clear_sv_graphs(hodlr_ctx *h) {
+  for (GraphEntry *g : {&h->factor_sv_graph, &h->factor_sv_nl_graph}) {
+    if (g->exec) cudaGraphExecDestroy(g->exec);
+    destroy_recs(g->recs);
+    *g = GraphEntry();
+  }
+  h->factor_sv_runs = h->factor_sv_nl_runs = 0;
+  h->sv_captured.clear();
+}
+
 static void clear_graphs(hodlr_ctx *h) {
   for (auto &g : h->solve_graphs) {
     if (g.second.exec) cudaGraphExecDestroy(g.second.exec);
@@ -248,6 +269,7 @@ static void clear_graphs(hodlr_ctx *h) {
   destroy_recs(h->factor_nl_graph.recs);
   h->factor_nl_graph = GraphEntry();
   h->factor_nl_runs = 0;
+  clear_sv_graphs(h);
   h->last_recs = nullptr;
 }
 
@@ -319,6 +341,9 @@ static void free_ctx(hodlr_ctx *h) {
   if (h->pcopy) cudaEventDestroy(h->pcopy);
   if (h->pst) cudaStreamDestroy(h->pst);
   if (h->cst) cudaStreamDestroy(h->cst);
+  for (auto &e : h->vready)
+    if (e) cudaEventDestroy(e);
+  if (h->vfork) cudaEventDestroy(h->vfork);
   if (h->own_stream && h->st) cudaStreamDestroy(h->st);
   delete h;
 }
@@ -519,10 +544,27 @@ static int ensure_leaf_lu(hodlr_ctx *h) {
 // Factorisation sweep: leaf LU (+ explicit leaf inverses), Ut = D^{-1} U
 // (all levels at once), then for depth L-1 .. 0: T = V^T [Ut_d | Ut_u],
 // capacitance LU + inverse, eta = Sinv [s.T1d; s.T0d], Ut_d -= Ut_u eta.
-template <typename T> static int factor_sweep(hodlr_ctx *h, bool leaves_done = false) {
+static int prepare_level_v(hodlr_ctx *h, int l, long long row0, long long count, cudaStream_t ps);
+
+template <typename T> static int factor_sweep(hodlr_ctx *h, bool leaves_done = false, bool streamed_v = false) {
   const long long n = h->n;
   const int m = h->m, L = h->L, r = h->r;
   cudaStream_t s = h->st;
+  if (streamed_v) {
+    // the V copies of the levels that wait for them, deepest first, on the
+    // side stream (forked from and, level by level, joined back into the
+    // sweep), each level's derived copies right after its V
+    CK(cudaEventRecord(h->vfork, s));
+    CK(cudaStreamWaitEvent(h->pst, h->vfork, 0));
+    for (int l = L - 1; l >= 0; --l) {
+      if (h->vsrc[l]) {
+        CK(cudaMemcpy2DAsync(h->Vlev(l), sizeof(double) * n, h->vsrc[l], sizeof(double) * h->vsrc_ld[l],
+                             sizeof(double) * n, r, cudaMemcpyHostToDevice, h->pst));
+        CKS(prepare_level_v(h, l, 0, -1, h->pst));
+      }
+      CK(cudaEventRecord(h->vready[l], h->pst));
+    }
+  }
   T *LU = LUptr<T>(h);
   T *Ut = Utptr<T>(h);
   const T *Vt = Vptr<T>(h);
@@ -556,6 +598,7 @@ template <typename T> static int factor_sweep(hodlr_ctx *h, bool leaves_done = f
     const int nb = h->nb(l);
     const long long rows = h->rows(l);
     const int Cd = l * r, Ct = Cd + r;
+    if (streamed_v) CK(cudaStreamWaitEvent(s, h->vready[l], 0));
     PHASE(h, HODLR_PHASE_REDUCE,
           launch_reduce_tn<T>(Vt + (long long)l * n * r, n, Ut, n, rows, nb, r, Ct, h->Tbuf, h->red, nullptr, s, h->dst,
                               sizeof(T) == 4 ? h->Tbuf32 : nullptr));
@@ -975,8 +1018,29 @@ static int prepare_leaves(hodlr_ctx *h, long long leaf0 = 0, long long count = -
   return HODLR_OK;
 }
 
-// Level l, rows [row0, row0 + count) (default: all rows).
-static int prepare_level(hodlr_ctx *h, int l, long long row0 = 0, long long count = -1, cudaStream_t ps = nullptr) {
+// Level l, rows [row0, row0 + count) (default: all rows): the copies derived
+// from U (prepare_level_u), from V (prepare_level_v), or both.
+static int prepare_level_u(hodlr_ctx *h, int l, long long row0 = 0, long long count = -1,
+                           cudaStream_t ps = nullptr) {
+  if (!h->mixed) return HODLR_OK;
+  const cudaStream_t st = ps ? ps : h->st;
+  const long long n = h->n, off = (long long)l * n * h->r + row0;
+  if (count < 0) count = n;
+  if (h->emulated && h->oz) {
+    h->dw_stale = true;
+  } else if (h->emulated) {
+    CK(launch_split(h->Ulev(l) + row0, n, h->U2 + off, n, count, h->r, nullptr, st));
+  }
+  if (h->oz) {  // U: row-scaled digits, rows of r contiguous entries
+    const long long r = h->r, L = h->L;
+    CK(launch_oz_slice_rows(h->Ulev(l) + row0, count, 0, 1, n, count, (int)r, h->Usl + l * n * r + row0 * r, r,
+                            L * n * r, h->Uexp + l * n + row0, st));
+  }
+  return HODLR_OK;
+}
+
+static int prepare_level_v(hodlr_ctx *h, int l, long long row0 = 0, long long count = -1,
+                           cudaStream_t ps = nullptr) {
   if (!h->mixed) return HODLR_OK;
   const cudaStream_t st = ps ? ps : h->st;
   const long long n = h->n, off = (long long)l * n * h->r + row0;
@@ -985,17 +1049,37 @@ static int prepare_level(hodlr_ctx *h, int l, long long row0 = 0, long long coun
   if (h->emulated && h->oz) {
     h->dw_stale = true;
   } else if (h->emulated) {
-    CK(launch_split(h->Ulev(l) + row0, n, h->U2 + off, n, count, h->r, nullptr, st));
     CK(launch_split(h->Vlev(l) + row0, n, h->V2 + off, n, count, h->r, nullptr, st));
   }
-  if (h->oz) {
+  if (h->oz) {  // V: digits scaled per 64-row chunk of each column, column-major
     const long long r = h->r, L = h->L;
-    // U: row-scaled digits, rows of r contiguous entries
-    CK(launch_oz_slice_rows(h->Ulev(l) + row0, count, 0, 1, n, count, (int)r, h->Usl + l * n * r + row0 * r, r,
-                            L * n * r, h->Uexp + l * n + row0, st));
-    // V: digits scaled per 64-row chunk of each column, column-major
     CK(launch_oz_slice_cols(h->Vlev(l) + row0, n, count, (int)r, h->Vsl + l * r * n + row0, n, L * r * n,
                             h->Vexp + l * (n / kOzChunk) * r + (row0 / kOzChunk) * r, nullptr, st));
+  }
+  return HODLR_OK;
+}
+
+static int prepare_level(hodlr_ctx *h, int l, long long row0 = 0, long long count = -1, cudaStream_t ps = nullptr) {
+  CKS(prepare_level_u(h, l, row0, count, ps));
+  return prepare_level_v(h, l, row0, count, ps);
+}
+
+static bool any_streamed_v(const hodlr_ctx *h) {
+  for (const double *p : h->vsrc)
+    if (p) return true;
+  return false;
+}
+
+// Copy the V of every level still waiting for a factorisation now, on the
+// handle's stream (for calls that read V before one).
+static int flush_streamed_v(hodlr_ctx *h) {
+  for (int l = 0; l < h->L; ++l) {
+    if (!h->vsrc[l]) continue;
+    CKS(join_prep(h));
+    CK(cudaMemcpy2DAsync(h->Vlev(l), sizeof(double) * h->n, h->vsrc[l], sizeof(double) * h->vsrc_ld[l],
+                         sizeof(double) * h->n, h->r, cudaMemcpyHostToDevice, h->st));
+    CKS(prepare_level_v(h, l, 0, -1, h->st));
+    h->vsrc[l] = nullptr;
   }
   return HODLR_OK;
 }
@@ -1124,6 +1208,8 @@ static int create_ctx(const hodlr_desc &d, const std::vector<int> &sys_levels, h
   h->kmax = d.nrhs_max;
   h->mixed = d.precision == HODLR_PREC_MIXED;
   h->has_level.assign(h->L, 0);
+  h->vsrc.assign(h->L, nullptr);
+  h->vsrc_ld.assign(h->L, 0);
   h->nsys = (int)sys_levels.size();
   h->forest = h->nsys > 1;
   set_geometry(h, sys_levels);
@@ -1353,17 +1439,30 @@ int hodlr_set_lowrank(hodlr_handle h, int level, const double *U, int64_t ldu, c
   if (level < 0 || level >= h->L) return set_err(HODLR_ERR_INVALID_ARG, "level out of range");
   if (ldu < h->n || ldv < h->n) return set_err(HODLR_ERR_INVALID_ARG, "ld < n");
   CKS(wait_prepared(h, 1 + level));
+  // HODLR_FLAG_STREAM_INPUTS and V in pinned host memory: V's copy waits for
+  // the factorisation, which overlaps it with the levels below this one
+  bool defer = false;
+  if (h->d.flags & HODLR_FLAG_STREAM_INPUTS) {
+    cudaPointerAttributes a{};
+    if (cudaPointerGetAttributes(&a, V) == cudaSuccess && a.type == cudaMemoryTypeHost) defer = true;
+    (void)cudaGetLastError();
+  }
   // plain (2-D) copies: the sources may be device or host memory
   CK(cudaMemcpy2DAsync(h->Ulev(level), sizeof(double) * h->n, U, sizeof(double) * ldu, sizeof(double) * h->n,
                        h->r, cudaMemcpyDefault, h->st));
-  CK(cudaMemcpy2DAsync(h->Vlev(level), sizeof(double) * h->n, V, sizeof(double) * ldv, sizeof(double) * h->n,
-                       h->r, cudaMemcpyDefault, h->st));
+  if (!defer)
+    CK(cudaMemcpy2DAsync(h->Vlev(level), sizeof(double) * h->n, V, sizeof(double) * ldv, sizeof(double) * h->n,
+                         h->r, cudaMemcpyDefault, h->st));
+  h->vsrc[level] = defer ? V : nullptr;
+  h->vsrc_ld[level] = ldv;
   if (s)
     CK(cudaMemcpyAsync(h->slev(level), s, sizeof(double) * h->r, cudaMemcpyDefault, h->st));
   else
     CK(launch_fill(h->slev(level), h->r, 1.0, h->st));
   h->has_level[level] = 1;
   h->factored = false;
+  if (defer)
+    return prepare_input(h, 1 + level, [&](cudaStream_t ps) { return prepare_level_u(h, level, 0, -1, ps); });
   return prepare_input(h, 1 + level, [&](cudaStream_t ps) { return prepare_level(h, level, 0, -1, ps); });
 }
 
@@ -1380,13 +1479,29 @@ int hodlr_factor(hodlr_handle h) {
   const bool nl = h->leaves_prefactored;
   h->leaves_prefactored = false;
   if (nl) CK(cudaMemcpyAsync(h->dst, h->dst_leaf, sizeof(DevStatus), cudaMemcpyDeviceToDevice, h->st));
+  // V copies streamed in by this factorisation (HODLR_FLAG_STREAM_INPUTS): their
+  // own graphs, captured again when the host sources change
+  bool sv = any_streamed_v(h) && side_prep_ok(h);
+  if (sv && h->vready.empty()) {
+    h->vready.assign(h->L, nullptr);
+    for (auto &e : h->vready)
+      if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) sv = false;
+    if (cudaEventCreateWithFlags(&h->vfork, cudaEventDisableTiming) != cudaSuccess) sv = false;
+  }
+  if (!sv) CKS(flush_streamed_v(h));
+  if (sv && h->sv_captured != h->vsrc) {
+    clear_sv_graphs(h);
+    h->sv_captured = h->vsrc;
+  }
+  GraphEntry &g = sv ? (nl ? h->factor_sv_nl_graph : h->factor_sv_graph) : (nl ? h->factor_nl_graph : h->factor_graph);
+  int &runs = sv ? (nl ? h->factor_sv_nl_runs : h->factor_sv_runs) : (nl ? h->factor_nl_runs : h->factor_runs);
   CK(cudaEventRecord(h->ev[0], h->st));
-  int rc = run_graphed(h, nl ? h->factor_nl_graph : h->factor_graph, nl ? h->factor_nl_runs : h->factor_runs,
-                       [&]() -> int {
-                         if (h->mixed) return factor_sweep<float>(h, nl);
-                         return factor_sweep<double>(h, nl);
-                       });
+  int rc = run_graphed(h, g, runs, [&]() -> int {
+    if (h->mixed) return factor_sweep<float>(h, nl, sv);
+    return factor_sweep<double>(h, nl, sv);
+  });
   CKS(rc);
+  if (sv) std::fill(h->vsrc.begin(), h->vsrc.end(), nullptr);
   CK(cudaEventRecord(h->ev[1], h->st));
   int fst = sync_status(h, nullptr);
   collect_phases(h);
@@ -1453,6 +1568,7 @@ int hodlr_matvec(hodlr_handle h, int transpose, const double *X, int64_t ldx, do
   if (nrhs < 1 || nrhs > h->kmax) return set_err(HODLR_ERR_INVALID_ARG, "nrhs out of range");
   if (ldx < h->n || ldy < h->n) return set_err(HODLR_ERR_INVALID_ARG, "ld < n");
   CKS(reset_status(h));
+  CKS(flush_streamed_v(h));
   CKS(matvec_fp64(h, transpose != 0, X, ldx, nullptr, 0, Y, ldy, nrhs, 1.0, nullptr));
   return sync_status(h, nullptr);
 }
@@ -1576,6 +1692,7 @@ int hodlr_get_factors(hodlr_handle h, double *leaf_lu, int32_t *leaf_ipiv, doubl
 int hodlr_get_inputs(hodlr_handle h, double *D, int64_t ld, int64_t leaf_stride, double *U, double *V,
                      double *s) {
   if (!h) return set_err(HODLR_ERR_INVALID_ARG, "null handle");
+  CKS(flush_streamed_v(h));
   const int m = h->m;
   const long long mm = (long long)m * m, n = h->n;
   cudaStream_t st = h->st;
@@ -1628,6 +1745,7 @@ int hodlr_generate(hodlr_handle h, uint64_t seed, double shift, int orthonormal,
   const int m = h->m, L = h->L, r = h->r;
   cudaStream_t s = h->st;
   CKS(reset_status(h));
+  std::fill(h->vsrc.begin(), h->vsrc.end(), nullptr);  // V is generated here
   CK(launch_gen_leaves(h->D, m, h->nleaf, seed, shift, s));
   h->has_D = true;
   h->leaves_prefactored = false;
@@ -1899,6 +2017,7 @@ int hodlr_set_seeded(hodlr_handle h, const int64_t *useeds, const int64_t *vseed
   if (!h || !useeds || !vseeds || !dseeds) return set_err(HODLR_ERR_INVALID_ARG, "null argument");
   CKS(join_prep(h));  // the inputs are rewritten: set-time preparation still reading them ends first
   if (h->forest) return set_err(HODLR_ERR_INVALID_ARG, "batch handles take hodlr_batch_set_* inputs");
+  std::fill(h->vsrc.begin(), h->vsrc.end(), nullptr);
   const long long n = h->n;
   const int m = h->m, L = h->L, r = h->r, nl = h->nleaf;
   cudaStream_t s = h->st;
@@ -1949,6 +2068,7 @@ int hodlr_set_uvd(hodlr_handle h, const double *U, int64_t ldu, const double *V,
   if (!h || !U || !V || !Dg) return set_err(HODLR_ERR_INVALID_ARG, "null argument");
   CKS(join_prep(h));  // the inputs are rewritten: set-time preparation still reading them ends first
   if (ldu < h->n || ldv < h->n) return set_err(HODLR_ERR_INVALID_ARG, "ld < n");
+  std::fill(h->vsrc.begin(), h->vsrc.end(), nullptr);
   const long long n = h->n;
   const int m = h->m, L = h->L, r = h->r;
   cudaStream_t s = h->st;

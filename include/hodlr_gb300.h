@@ -68,6 +68,14 @@ enum {
                                     double-word residual) */
 };
 
+/* hodlr_desc.flags */
+enum {
+  HODLR_FLAG_STREAM_INPUTS = 1  /* hodlr_set_lowrank with V in pinned host memory copies U at once and
+                                   leaves V's copy to the next hodlr_factor, which streams the levels'
+                                   V deepest first alongside the sweep (level l waits only for its own V):
+                                   the host V buffers must stay valid until that hodlr_factor returns */
+};
+
 typedef struct hodlr_desc {
   int64_t n;              /* N = leaf * 2^levels */
   int32_t leaf;           /* m, leaf block size */
@@ -78,7 +86,7 @@ typedef struct hodlr_desc {
   int32_t residual;       /* HODLR_RESID_* (mixed path only) */
   double refine_tol;      /* target max_j ||b_j - A x_j|| / ||b_j|| (mixed), e.g. 1e-12 */
   int32_t refine_max_iter;/* refinement iteration cap (mixed) */
-  int32_t flags;          /* reserved, 0 */
+  int32_t flags;          /* HODLR_FLAG_* (0: none) */
   void *stream;           /* cudaStream_t; NULL = legacy default stream */
 } hodlr_desc;
 

@@ -614,3 +614,55 @@ def test_refinement_loop_same_eager_captured_replayed(hodlr, resid):
     np.testing.assert_array_equal(outs[0], outs[1])
     np.testing.assert_array_equal(outs[0], outs[2])
     s.close()
+
+
+def _pinned_colmajor(a):
+    """A pinned host tensor holding the Fortran-ordered array a, column-major."""
+    return torch.from_numpy(np.ascontiguousarray(np.asarray(a, dtype=np.float64).T)).pin_memory().t()
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_streamed_v_inputs_match_plain_inputs(hodlr, precision):
+    """HODLR_FLAG_STREAM_INPUTS: V from pinned host memory is copied by the
+    factorisation (deepest level first, beside the sweep).  Factor + solve in
+    the eager, captured and replayed runs, and again after the host buffers
+    change (the streamed graphs are captured again), equal a handle whose
+    inputs were set from the device, bit for bit; a product before any
+    factorisation copies the waiting V first."""
+    pr = P.gaussian_problem(128, 5, 32, nrhs=4, seed=77, orthonormal=True, decay=3.0, shift=1.5)
+    ref = make_solver(hodlr, pr, precision=precision, refine_tol=1e-12)
+    ref.factor()
+    Bref = to_dev(pr.B)
+    ref.solve(Bref)
+    xref = to_host(Bref)
+    X = to_dev(np.random.default_rng(3).standard_normal((pr.n, 4)))
+    Yref = torch.empty((4, pr.n), dtype=torch.float64, device="cuda").t()
+    ref.matvec(X, Yref)
+    torch.cuda.synchronize()
+
+    s = hodlr.Solver(pr.n, pr.leaf, pr.levels, pr.rank, nrhs_max=4, precision=precision, refine_tol=1e-12,
+                     flags=hodlr.FLAG_STREAM_INPUTS)
+    D = to_dev(pr.K)
+    s.set_leaf_blocks(D)
+    sets = [[(_pinned_colmajor(pr.U[l]), _pinned_colmajor(pr.V[l])) for l in range(pr.levels)] for _ in range(2)]
+    sv = [to_dev(pr.s[l]) for l in range(pr.levels)] if pr.s is not None else [None] * pr.levels
+
+    def set_all(which):
+        for l in range(pr.levels):
+            s.set_lowrank(l, sets[which][l][0], sets[which][l][1], sv[l])
+
+    set_all(0)
+    Y = torch.empty((4, pr.n), dtype=torch.float64, device="cuda").t()
+    s.matvec(X, Y)                      # before any factorisation: the waiting V is copied first
+    torch.cuda.synchronize()
+    assert torch.equal(Y, Yref)
+    B = to_dev(pr.B)
+    for which in (0, 0, 0, 1, 1):       # eager, captured, replayed; new buffers: captured, replayed
+        set_all(which)
+        s.factor()
+        B.copy_(to_dev(pr.B))
+        torch.cuda.synchronize()
+        s.solve(B)
+        np.testing.assert_array_equal(to_host(B), xref)
+    s.close()
+    ref.close()
