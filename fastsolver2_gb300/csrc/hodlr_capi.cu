@@ -176,8 +176,9 @@ struct hodlr_ctx {
   // signalling vready[l], while the sweep runs
   std::vector<const double *> vsrc;
   std::vector<int64_t> vsrc_ld;
-  std::vector<cudaEvent_t> vready;
+  std::vector<cudaEvent_t> vready, vcopied;
   cudaEvent_t vfork = nullptr;
+  cudaStream_t vcs = nullptr;  // the streamed V copies (the side stream prepares each level after its copy)
   std::vector<const double *> sv_captured;  // the sources the streamed factor graphs copy from
   cudaEvent_t pcopy = nullptr, plast = nullptr;
   std::vector<cudaEvent_t> pready;
@@ -343,7 +344,10 @@ static void free_ctx(hodlr_ctx *h) {
   if (h->cst) cudaStreamDestroy(h->cst);
   for (auto &e : h->vready)
     if (e) cudaEventDestroy(e);
+  for (auto &e : h->vcopied)
+    if (e) cudaEventDestroy(e);
   if (h->vfork) cudaEventDestroy(h->vfork);
+  if (h->vcs) cudaStreamDestroy(h->vcs);
   if (h->own_stream && h->st) cudaStreamDestroy(h->st);
   delete h;
 }
@@ -551,18 +555,27 @@ template <typename T> static int factor_sweep(hodlr_ctx *h, bool leaves_done = f
   const int m = h->m, L = h->L, r = h->r;
   cudaStream_t s = h->st;
   if (streamed_v) {
-    // the V copies of the levels that wait for them, deepest first, on the
-    // side stream (forked from and, level by level, joined back into the
-    // sweep), each level's derived copies right after its V
+    // the V copies of the levels that wait for them, deepest first and back
+    // to back on their own stream (so that the host link never waits for the
+    // SMs); each level's derived copies on the side stream after its copy;
+    // both forked from the sweep and joined back into it level by level
     CK(cudaEventRecord(h->vfork, s));
+    CK(cudaStreamWaitEvent(h->vcs, h->vfork, 0));
     CK(cudaStreamWaitEvent(h->pst, h->vfork, 0));
     for (int l = L - 1; l >= 0; --l) {
       if (h->vsrc[l]) {
         CK(cudaMemcpy2DAsync(h->Vlev(l), sizeof(double) * n, h->vsrc[l], sizeof(double) * h->vsrc_ld[l],
-                             sizeof(double) * n, r, cudaMemcpyHostToDevice, h->pst));
+                             sizeof(double) * n, r, cudaMemcpyHostToDevice, h->vcs));
+        CK(cudaEventRecord(h->vcopied[l], h->vcs));
+        CK(cudaStreamWaitEvent(h->pst, h->vcopied[l], 0));
         CKS(prepare_level_v(h, l, 0, -1, h->pst));
       }
       CK(cudaEventRecord(h->vready[l], h->pst));
+    }
+    if (!h->vsrc[0]) {  // join the copy stream through the side stream's last event
+      CK(cudaEventRecord(h->vcopied[0], h->vcs));
+      CK(cudaStreamWaitEvent(h->pst, h->vcopied[0], 0));
+      CK(cudaEventRecord(h->vready[0], h->pst));
     }
   }
   T *LU = LUptr<T>(h);
@@ -1484,10 +1497,17 @@ int hodlr_factor(hodlr_handle h) {
   bool sv = any_streamed_v(h) && side_prep_ok(h);
   if (sv && h->vready.empty()) {
     h->vready.assign(h->L, nullptr);
-    for (auto &e : h->vready)
-      if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) sv = false;
+    h->vcopied.assign(h->L, nullptr);
+    for (auto *v : {&h->vready, &h->vcopied})
+      for (auto &e : *v)
+        if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) sv = false;
     if (cudaEventCreateWithFlags(&h->vfork, cudaEventDisableTiming) != cudaSuccess) sv = false;
+    if (cudaStreamCreateWithFlags(&h->vcs, cudaStreamNonBlocking) != cudaSuccess) {
+      h->vcs = nullptr;
+      sv = false;
+    }
   }
+  if (sv && (!h->vcs || !h->vfork)) sv = false;
   if (!sv) CKS(flush_streamed_v(h));
   if (sv && h->sv_captured != h->vsrc) {
     clear_sv_graphs(h);
