@@ -5,6 +5,9 @@
 //   LMatrix::gemmRed / gemmBro / node_solve             include/lmatrix.hpp:119-169
 //   KTree::solve (leaf solve), hsolve                   include/tree.hpp:362-389,
 //                                                       src/tasks/leaf_solve.cc:8-10
+//   the SPMD drivers' per-shard subtrees under top levels with unequal
+//   sibling ranks (IrregularTree)                       spmd_driver/solver_irregular_part.cc,
+//                                                       spmd_driver/solver_irregular_ranks.cc
 // The Legion context/runtime arguments are gone (one process, one GPU); the
 // matrices are plain column-major buffers (host or device), and failures
 // throw hodlr_gb300::Error instead of asserting.
@@ -170,6 +173,73 @@ struct LMatrix {
   static void node_solve(int nnode, int r, int nrhs, const double *VTu, int64_t ldu, double *VTd, int64_t ldd) {
     check(hodlr_node_solve(nnode, r, nrhs, VTu, ldu, VTd, ldd));
   }
+  // LMatrix::node_solve(VTu0, VTu1, VTd0, VTd1, ...) of the SPMD drivers
+  // (include/lmatrix.hpp:127-130, src/tasks/node_solve_region.cc:77-97): the
+  // (rank0 + rank1)-square systems of siblings with unequal ranks, in place.
+  static void node_solve(int nnode, int rank0, int rank1, int nrhs, const double *VTu0, int64_t ldu0,
+                         const double *VTu1, int64_t ldu1, double *VTd0, int64_t ldd0, double *VTd1, int64_t ldd1) {
+    check(hodlr_node_solve_irregular(nnode, rank0, rank1, nrhs, VTu0, ldu0, VTu1, ldu1, VTd0, ldd0, VTd1, ldd1));
+  }
+};
+
+// The matrix of the SPMD drivers on one GPU: one uniform subtree per shard
+// (its own leaf size, depth, rank and precision) under top levels whose
+// nodes couple their children with ranks that may differ (see
+// hodlr_tree_create).  Shard j's leaves and bases are set on subtree(j) with
+// the HMatrix-style calls; the top levels' bases with set_coupling.
+class IrregularTree {
+ public:
+  IrregularTree(int top_levels, const std::vector<hodlr_desc> &shards, const std::vector<int32_t> &coupling_ranks,
+                int nrhs_max = 1, void *stream = nullptr) {
+    hodlr_tree_desc d{};
+    d.top_levels = top_levels;
+    d.subtrees = shards.data();
+    d.coupling_rank = coupling_ranks.data();
+    d.nrhs_max = nrhs_max;
+    d.stream = stream;
+    if ((int)shards.size() != (1 << top_levels) || (int)coupling_ranks.size() != 2 * ((1 << top_levels) - 1))
+      throw Error(HODLR_ERR_INVALID_ARG, "need 2^T shards and 2 (2^T - 1) coupling ranks");
+    check(hodlr_tree_create(&d, &t_));
+  }
+  IrregularTree(const IrregularTree &) = delete;
+  IrregularTree &operator=(const IrregularTree &) = delete;
+  ~IrregularTree() {
+    if (t_) hodlr_tree_destroy(t_);
+  }
+
+  hodlr_handle subtree(int j) const {
+    hodlr_handle h = nullptr;
+    check(hodlr_tree_subtree(t_, j, &h));
+    return h;
+  }
+  void set_leaf_blocks(int j, const double *K, int64_t ld, int64_t leaf_stride) {
+    check(hodlr_set_leaf_blocks(subtree(j), K, ld, leaf_stride));
+  }
+  void set_level(int j, int l, const double *U, int64_t ldu, const double *V, int64_t ldv,
+                 const double *s = nullptr) {
+    check(hodlr_set_lowrank(subtree(j), l, U, ldu, V, ldv, s));
+  }
+  // Child `child` of top node (level, pos): U with its own rank, V with the sibling's.
+  void set_coupling(int level, int pos, int child, const double *U, int64_t ldu, const double *V, int64_t ldv) {
+    check(hodlr_tree_set_coupling(t_, level, pos, child, U, ldu, V, ldv));
+  }
+  int64_t rows() const {
+    int64_t n = 0;
+    check(hodlr_tree_rows(t_, &n, nullptr));
+    return n;
+  }
+  void factor() { check(hodlr_tree_factor(t_)); }
+  hodlr_solve_info solve(double *B, int64_t ldb, int nrhs = 1) {
+    hodlr_solve_info info{};
+    check(hodlr_tree_solve(t_, B, ldb, nrhs, &info));
+    return info;
+  }
+  void matvec(const double *X, int64_t ldx, double *Y, int64_t ldy, int nrhs = 1) {
+    check(hodlr_tree_matvec(t_, X, ldx, Y, ldy, nrhs));
+  }
+
+ private:
+  hodlr_tree t_ = nullptr;
 };
 
 }  // namespace hodlr_gb300

@@ -108,9 +108,9 @@ def test_dense_blocks_and_uvd_solve(hodlr):
     assert np.linalg.norm(host(B) - Xo) / np.linalg.norm(Xo) < 1e-12
 
 
-def _build_cpp():
-    exe = os.path.join(ROOT, "tests", "cpp", "test_solver")
-    src = os.path.join(ROOT, "tests", "cpp", "test_solver.cc")
+def _build_cpp(name="test_solver"):
+    exe = os.path.join(ROOT, "tests", "cpp", name)
+    src = os.path.join(ROOT, "tests", "cpp", name + ".cc")
     lib = os.path.join(ROOT, "fastsolver2_gb300")
     cuda = os.environ.get("CUDA_HOME", "/usr/local/cuda")
     if not os.path.exists(exe) or os.path.getmtime(exe) < os.path.getmtime(src):
@@ -135,3 +135,15 @@ def test_cpp_hmatrix_driver(hodlr, tmp_path, leaf, levels, rank):
     pr = P.reference_problem(leaf, levels, rank, nrhs=1)
     Xo, _, _ = O.hsolve_general(pr, pr.B)
     assert np.linalg.norm(x - Xo[:, 0]) / np.linalg.norm(Xo) < 1e-12
+
+
+def test_cpp_irregular_tree_driver(hodlr):
+    """The C++ host class IrregularTree (and the unequal-rank LMatrix::node_solve)
+    on a two-shard tree with a heavy shard and unequal ranks."""
+    exe = _build_cpp("test_tree")
+    out = subprocess.run([exe], capture_output=True, text=True, timeout=300)
+    assert out.returncode == 0, out.stderr
+    rep = json.loads(out.stdout.strip().splitlines()[-1])
+    assert rep["rows"] == (32 << 3) + (320 << 3)
+    assert rep["rel_residual"] < 1e-12
+    assert rep["node_solve_err"] < 1e-14
