@@ -769,14 +769,18 @@ __global__ void __launch_bounds__(256) cap_apply_kernel(CapApplyArgs a) {
 // Mixed path: eta = op(Sinv) RHS in FP32 (the FP32 inverse against the FP32
 // T blocks), written as FP32 for the FP32 updates (eta32, rows scaled by
 // out_scale).  Same tiling as above.
-template <int MT>
+template <int NP, int CPT>
 __global__ void __launch_bounds__(256) cap_apply_f32_kernel(CapApplyArgs a) {
+  // eta = op(S^-1) RHS for one node and CT columns at a time: thread (rg, ct)
+  // owns rows 4 rg .. 4 rg + 3 and the column quads 4 ct + 4 CTH g (g < CPT / 4);
+  // the inverse ([q][i]) and the right-hand sides ([q][j]) are read as float4
+  // runs, every output summed over q in increasing order
+  constexpr int RG = NP / 4, CTH = 256 / RG, CT = CTH * CPT, SP = NP + 4, RP = CT + 4, NG = CPT / 4;
   if (a.skip && *a.skip) return;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int r = a.r, n2 = 2 * r;
-  constexpr int NP = MT * 32;
-  float *sS = reinterpret_cast<float *>(smem_raw);  // [q][i]
-  float *sR = sS + NP * (NP + 1);                    // [j][q], padded
+  float *sS = reinterpret_cast<float *>(smem_raw);  // [q][i], row stride SP
+  float *sR = sS + NP * SP;                          // [q][j], row stride RP
   const int p = blockIdx.y;
   const int node = a.node_base + p;
   const float *Sg = a.sinv32 + (long long)node * n2 * n2;
@@ -784,54 +788,76 @@ __global__ void __launch_bounds__(256) cap_apply_f32_kernel(CapApplyArgs a) {
     const int i = e % NP, q = e / NP;
     float v = 0.f;
     if (i < n2 && q < n2) v = a.trans ? Sg[q + (long long)i * n2] : Sg[i + (long long)q * n2];
-    sS[q * (NP + 1) + i] = v;
+    sS[q * SP + i] = v;
   }
   const float *T0 = a.Tb32 + (long long)(2 * p) * a.tb_stride;
   const float *T1 = a.Tb32 + (long long)(2 * p + 1) * a.tb_stride;
-  const int ti = threadIdx.x & 31, tj = threadIdx.x >> 5;
-  for (int c0 = blockIdx.x * 32; c0 < a.C; c0 += gridDim.x * 32) {
-    const int nc = min(32, a.C - c0);
+  const int rg = threadIdx.x % RG, ct = threadIdx.x / RG;
+  const bool vec_out = (n2 & 3) == 0;
+  float *E = a.eta32 + (long long)p * n2 * a.C;
+  for (int c0 = blockIdx.x * CT; c0 < a.C; c0 += gridDim.x * CT) {
+    const int nc = min(CT, a.C - c0);
     __syncthreads();
-    for (int e = threadIdx.x; e < NP * 32; e += blockDim.x) {
-      const int q = e % NP, j = e / NP;
-      float v = 0.f;
-      if (q < n2 && j < nc) {
-        if (!a.trans)
-          v = (q < r) ? (a.scale ? (float)a.scale[q] : 1.f) * T1[q + (long long)(c0 + j) * r]
-                      : (a.scale ? (float)a.scale[q - r] : 1.f) * T0[(q - r) + (long long)(c0 + j) * r];
-        else
-          v = (q < r) ? T0[q + (long long)(c0 + j) * r] : T1[(q - r) + (long long)(c0 + j) * r];
+    // four columns per task: loads coalesced over q, one float4 store per task
+    // (consecutive q land on distinct bank quads: RP / 4 is odd)
+    for (int e = threadIdx.x; e < NP * (CT / 4); e += blockDim.x) {
+      const int q = e % NP, j4 = 4 * (e / NP);
+      const float *src = nullptr;
+      float scv = 1.f;
+      if (q < n2) {
+        if (!a.trans) {
+          src = q < r ? T1 + q : T0 + (q - r);
+          if (a.scale) scv = (float)a.scale[q < r ? q : q - r];
+        } else {
+          src = q < r ? T0 + q : T1 + (q - r);
+        }
       }
-      sR[j * (NP + 1) + q] = v;
+      float v[4];
+#pragma unroll
+      for (int w = 0; w < 4; ++w) v[w] = (src && j4 + w < nc) ? scv * src[(long long)(c0 + j4 + w) * r] : 0.f;
+      *reinterpret_cast<float4 *>(sR + q * RP + j4) = make_float4(v[0], v[1], v[2], v[3]);
     }
     __syncthreads();
-    float acc[MT][4];
+    float acc[4][CPT];
 #pragma unroll
-    for (int u = 0; u < MT; ++u)
+    for (int u = 0; u < 4; ++u)
 #pragma unroll
-      for (int v = 0; v < 4; ++v) acc[u][v] = 0.f;
+      for (int v = 0; v < CPT; ++v) acc[u][v] = 0.f;
     for (int q = 0; q < n2; ++q) {
-      float sv[MT];
+      const float4 sv = *reinterpret_cast<const float4 *>(sS + q * SP + 4 * rg);
 #pragma unroll
-      for (int u = 0; u < MT; ++u) sv[u] = sS[q * (NP + 1) + ti + 32 * u];
+      for (int g = 0; g < NG; ++g) {
+        const float4 rv = *reinterpret_cast<const float4 *>(sR + q * RP + 4 * ct + 4 * CTH * g);
+        const float su[4] = {sv.x, sv.y, sv.z, sv.w}, rw[4] = {rv.x, rv.y, rv.z, rv.w};
 #pragma unroll
-      for (int v = 0; v < 4; ++v) {
-        const float rv = sR[(tj + 8 * v) * (NP + 1) + q];
+        for (int u = 0; u < 4; ++u)
 #pragma unroll
-        for (int u = 0; u < MT; ++u) acc[u][v] = fmaf(sv[u], rv, acc[u][v]);
+          for (int w = 0; w < 4; ++w) acc[u][4 * g + w] = fmaf(su[u], rw[w], acc[u][4 * g + w]);
       }
     }
+    float sc[4];
 #pragma unroll
-    for (int u = 0; u < MT; ++u) {
-      const int i = ti + 32 * u;
-      if (i >= n2) continue;
-      const float sc = a.out_scale ? (float)a.out_scale[i % r] : 1.f;
-#pragma unroll
-      for (int v = 0; v < 4; ++v) {
-        const int j = tj + 8 * v;
-        if (j < nc) a.eta32[(long long)p * n2 * a.C + i + (long long)(c0 + j) * n2] = acc[u][v] * sc;
-      }
+    for (int u = 0; u < 4; ++u) {
+      const int i = 4 * rg + u;
+      sc[u] = (i < n2 && a.out_scale) ? (float)a.out_scale[i % r] : 1.f;
     }
+#pragma unroll
+    for (int g = 0; g < NG; ++g)
+#pragma unroll
+      for (int w = 0; w < 4; ++w) {
+        const int j = 4 * ct + 4 * CTH * g + w;
+        if (j >= nc || 4 * rg >= n2) continue;
+        float *o = E + 4 * rg + (long long)(c0 + j) * n2;
+        if (vec_out) {
+          *reinterpret_cast<float4 *>(o) =
+              make_float4(acc[0][4 * g + w] * sc[0], acc[1][4 * g + w] * sc[1], acc[2][4 * g + w] * sc[2],
+                          acc[3][4 * g + w] * sc[3]);
+        } else {
+#pragma unroll
+          for (int u = 0; u < 4; ++u)
+            if (4 * rg + u < n2) o[u] = acc[u][4 * g + w] * sc[u];
+        }
+      }
   }
 }
 
@@ -840,20 +866,21 @@ cudaError_t launch_cap_apply(const CapApplyArgs &a, cudaStream_t s) {
     if (a.nnode <= 0 || a.C <= 0) return cudaSuccess;
     if (a.r < 1 || a.r > 64) return cudaErrorInvalidValue;
     const int n2 = 2 * a.r;
-    const int MT = n2 <= 32 ? 1 : (n2 <= 64 ? 2 : 4);
-    const int NP = MT * 32;
-    const size_t bytes = sizeof(float) * ((size_t)NP * (NP + 1) + 32ull * (NP + 1));
-    const int tiles = ceil_div(a.C, 32);
-    const int groups = std::max(1, std::min(tiles, ceil_div(4 * 152, a.nnode)));
-    dim3 grid(groups, a.nnode);
-#define HODLR_CAPF(MTV)                                 \
-  {                                                     \
-    auto k = cap_apply_f32_kernel<MTV>;                 \
-    cudaError_t e = set_smem(k, bytes);                 \
-    if (e != cudaSuccess) return e;                     \
-    HODLR_LAUNCH(k, grid, 256, bytes, s, a);            \
+    // NP rows (n2 padded), CPT columns per thread: CT = (256 / (NP / 4)) * CPT columns per pass
+#define HODLR_CAPF(NPV, CPTV)                                                                        \
+  {                                                                                                  \
+    constexpr int CT = (256 / (NPV / 4)) * CPTV;                                                     \
+    const size_t bytes = sizeof(float) * ((size_t)NPV * (NPV + 4) + (size_t)NPV * (CT + 4));         \
+    const int tiles = ceil_div(a.C, CT);                                                             \
+    const int groups = std::max(1, std::min(tiles, ceil_div(4 * kNumSMs, a.nnode)));                 \
+    auto k = cap_apply_f32_kernel<NPV, CPTV>;                                                        \
+    cudaError_t e = set_smem(k, bytes);                                                              \
+    if (e != cudaSuccess) return e;                                                                  \
+    HODLR_LAUNCH(k, dim3(groups, a.nnode), 256, bytes, s, a);                                        \
   }
-    if (MT == 1) HODLR_CAPF(1) else if (MT == 2) HODLR_CAPF(2) else HODLR_CAPF(4)
+    if (n2 <= 32) HODLR_CAPF(32, 4)
+    else if (n2 <= 64) { if (a.C <= 64) HODLR_CAPF(64, 4) else HODLR_CAPF(64, 8) }
+    else { if (a.C <= 32) HODLR_CAPF(128, 4) else HODLR_CAPF(128, 8) }
 #undef HODLR_CAPF
     return cudaGetLastError();
   }
