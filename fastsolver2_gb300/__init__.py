@@ -299,7 +299,7 @@ class Solver:
         check(lib().hodlr_autotune(self.h, nrhs, ctypes.byref(t)))
         return t.as_dict()
 
-    def set_tuning(self, red_ctas_per_sm=4, update_tile_rows=0, cap_warps=8, update_tc_shape=0):
+    def set_tuning(self, red_ctas_per_sm=4, update_tile_rows=0, cap_warps=0, update_tc_shape=0):
         t = Tuning(red_ctas_per_sm, update_tile_rows, cap_warps, update_tc_shape, -1.0)
         check(lib().hodlr_set_tuning(self.h, ctypes.byref(t)))
 

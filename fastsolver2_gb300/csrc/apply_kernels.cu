@@ -406,7 +406,7 @@ __device__ __forceinline__ V row_entry(const V (&v)[RS], int p) {
 }
 
 template <int M, int NW>
-__global__ void __launch_bounds__(NW * 32, NW * 32 * (M / NW) >= 4096 ? 1 : (NW >= 16 ? 2 : 3))
+__global__ void __launch_bounds__(NW * 32, (NW >= 32 || NW * 32 * (M / NW) >= 4096) ? 1 : (NW >= 16 ? 2 : 3))
 cap_factor_cols_kernel(CapFactorArgs a) {
   constexpr int RS = M / 32, CW = M / NW;
   __shared__ double s_l[2][M];   // multipliers by physical row
@@ -606,7 +606,16 @@ cudaError_t launch_cap_factor(const CapFactorArgs &a, cudaStream_t s) {
   if (a.r < 1 || a.r > 64) return cudaErrorInvalidValue;
   const int n2 = 2 * a.r;
   if (a.sinv32 && n2 <= 32) return launch_cap_cols<32, 8>(a, s);
-  if (a.sinv32 && n2 <= 64) return current_tuning().cap_warps == 16 ? launch_cap_cols<64, 16>(a, s) : launch_cap_cols<64, 8>(a, s);
+  if (a.sinv32 && n2 <= 64) {
+    // warps per system: the tuned value, or by level -- the few-node levels run
+    // one pivot chain per SM, so more warps shorten it; the wide levels keep
+    // three 8-warp systems per SM
+    int w = current_tuning().cap_warps;
+    if (w == 0) w = a.nnode <= 64 ? 32 : (a.nnode <= 256 ? 16 : 8);
+    if (w == 32) return launch_cap_cols<64, 32>(a, s);
+    if (w == 16) return launch_cap_cols<64, 16>(a, s);
+    return launch_cap_cols<64, 8>(a, s);
+  }
   if (a.sinv32) return launch_cap_cols<128, 16>(a, s);
   if (n2 == 32) return launch_cap_reg<32>(a, s);
   if (n2 == 64) return launch_cap_reg<64>(a, s);

@@ -2708,7 +2708,7 @@ int hodlr_batch_stats(hodlr_batch b, int *nforests, double *factor_ms, double *s
 // sweeps on the handle's own inputs with a seeded scratch right-hand side.
 static const int kRedCands[] = {2, 4, 8};
 static const int kUpdCands[] = {0, 64};
-static const int kCapWarpCands[] = {8, 16};
+static const int kCapWarpCands[] = {0, 8, 16};
 static const int kUpdTcCands[] = {0, 1, 2};
 
 template <typename Measure>
@@ -2752,7 +2752,8 @@ static int tune_search(Tuning &cur, double &cur_ms, Measure measure) {
 static bool valid_tuning(const hodlr_tuning &t) {
   return (t.red_ctas_per_sm == 2 || t.red_ctas_per_sm == 4 || t.red_ctas_per_sm == 8) &&
          (t.update_tile_rows == 0 || t.update_tile_rows == 64 || t.update_tile_rows == 128) &&
-         (t.cap_warps == 0 || t.cap_warps == 8 || t.cap_warps == 16) && t.update_tc_shape >= 0 &&
+         (t.cap_warps == 0 || t.cap_warps == 8 || t.cap_warps == 16 || t.cap_warps == 32) &&
+         t.update_tc_shape >= 0 &&
          t.update_tc_shape <= 2;
 }
 
@@ -2762,7 +2763,7 @@ int hodlr_set_tuning(hodlr_handle h, const hodlr_tuning *t) {
   if (!h || !t || !valid_tuning(*t)) return set_err(HODLR_ERR_INVALID_ARG, "bad tuning");
   h->tune.red_ctas_per_sm = t->red_ctas_per_sm;
   h->tune.upd_bm = t->update_tile_rows == 128 ? 0 : t->update_tile_rows;
-  h->tune.cap_warps = t->cap_warps == 0 ? 8 : t->cap_warps;
+  h->tune.cap_warps = t->cap_warps;
   h->tune.upd_tc_shape = t->update_tc_shape;
   clear_graphs(h);
   h->factored = false;

@@ -15,7 +15,7 @@ int set_last_error(int code, const char *msg);
 struct Tuning {
   int red_ctas_per_sm = 4;  // split-K target of the row reductions, CTAs per SM (2, 4 or 8)
   int upd_bm = 0;           // FP32 update tile rows: 0 = 128 when the block allows, else 64
-  int cap_warps = 8;        // mixed-path capacitance LU (2r <= 64): warps per node, 8 or 16
+  int cap_warps = 0;        // mixed-path capacitance LU (2r <= 64): warps per node, 8, 16 or 32 (0: by level)
   int upd_tc_shape = 0;     // tcgen05 update: 0 = 128x64 tiles, 3-stage ring; 1 = 128x64, 2 stages; 2 = 128x32, 5 stages
 };
 constexpr int kMaxRedCtasPerSm = 8;

@@ -448,7 +448,7 @@ def test_autotune_picks_valid_shapes_and_keeps_results(hodlr, precision):
     s = make_solver(hodlr, pr, precision=precision)
     t = s.autotune(nrhs=4)
     assert t["red_ctas_per_sm"] in (2, 4, 8) and t["update_tile_rows"] in (0, 64) and t["ms"] > 0
-    assert t["cap_warps"] in (8, 16) and t["update_tc_shape"] in (0, 1, 2)
+    assert t["cap_warps"] in (0, 8, 16) and t["update_tc_shape"] in (0, 1, 2)
     got = s.get_tuning()
     assert all(got[key] == t[key] for key in ("red_ctas_per_sm", "update_tile_rows", "cap_warps", "update_tc_shape"))
     B = to_dev(pr.B)
@@ -473,7 +473,7 @@ def test_capacitance_and_update_shapes_keep_results(hodlr, r):
     pr = P.gaussian_problem(128, 5, r, nrhs=5, seed=40 + r, orthonormal=True, decay=3.0, shift=1.5)
     s = make_solver(hodlr, pr, precision=hodlr.PREC_MIXED, refine_tol=1e-12)
     Xo, _, _ = O.hsolve_general(pr, pr.B)
-    for warps in (8, 16):
+    for warps in (0, 8, 16, 32):
         for shape in (0, 1, 2):
             s.set_tuning(cap_warps=warps, update_tc_shape=shape)
             assert s.get_tuning()["cap_warps"] == warps and s.get_tuning()["update_tc_shape"] == shape
