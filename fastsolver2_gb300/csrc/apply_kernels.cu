@@ -607,11 +607,11 @@ cudaError_t launch_cap_factor(const CapFactorArgs &a, cudaStream_t s) {
   const int n2 = 2 * a.r;
   if (a.sinv32 && n2 <= 32) return launch_cap_cols<32, 8>(a, s);
   if (a.sinv32 && n2 <= 64) {
-    // warps per system: the tuned value, or by level -- the few-node levels run
-    // one pivot chain per SM, so more warps shorten it; the wide levels keep
-    // three 8-warp systems per SM
+    // warps per system: the tuned value, or by level -- a level with at most one
+    // system per SM runs each pivot chain with 32 warps (one CTA per SM), up to
+    // two per SM with 16, the wide levels keep three 8-warp systems per SM
     int w = current_tuning().cap_warps;
-    if (w == 0) w = a.nnode <= 64 ? 32 : (a.nnode <= 256 ? 16 : 8);
+    if (w == 0) w = a.nnode <= kNumSMs ? 32 : (a.nnode <= 2 * kNumSMs ? 16 : 8);
     if (w == 32) return launch_cap_cols<64, 32>(a, s);
     if (w == 16) return launch_cap_cols<64, 16>(a, s);
     return launch_cap_cols<64, 8>(a, s);

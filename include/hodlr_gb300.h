@@ -426,7 +426,7 @@ typedef struct hodlr_tuning {
   int32_t red_ctas_per_sm;   /* 2, 4 or 8 */
   int32_t update_tile_rows;  /* 0 (128 where the blocks allow it, else 64) or 64 */
   int32_t cap_warps;         /* mixed path, 2r <= 64: warps per capacitance system, 8, 16 or 32
-                                (0 = by level: 32 up to 64 systems, 16 up to 256, else 8) */
+                                (0 = by level: 32 up to one system per SM, 16 up to two, else 8) */
   int32_t update_tc_shape;   /* tensor-core update: 0 = 128x64 tiles through a 3-stage ring,
                                 1 = 128x64 tiles, 2 stages, 2 = 128x32 tiles, 5 stages */
   double ms;                 /* autotune: factor + solve milliseconds with these shapes */
