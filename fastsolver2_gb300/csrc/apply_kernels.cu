@@ -145,6 +145,9 @@ leaf_apply_kernel(const T *__restrict__ Dinv, T *X, long long ldx, int ncols, co
 constexpr int kLa128Threads = 128, kLa128CT = 64, kLa128LD = kLa128CT + 4;
 constexpr size_t kLa128Smem = (size_t)(128 * kLa128LD + 32 * 128) * sizeof(float);
 
+__device__ __forceinline__ float to_f32(float x) { return x; }
+__device__ __forceinline__ float to_f32(double x) { return f64_to_f32_rn(x); }
+
 // The source tile may be another matrix, of FP32 or FP64 (rounded to FP32
 // as it is staged): the factorisation's first application reads U in FP64
 // and writes Utilde in FP32 with no separate conversion pass.
@@ -168,7 +171,7 @@ leaf_apply128_f32_kernel(const float *__restrict__ Dinv, const S *Xs, long long 
     const int i = e % M, j = 4 * (e / M);
     float v[4];
 #pragma unroll
-    for (int u = 0; u < 4; ++u) v[u] = j + u < nc ? (float)Xsg[i + (long long)(j + u) * lds] : 0.f;
+    for (int u = 0; u < 4; ++u) v[u] = j + u < nc ? to_f32(Xsg[i + (long long)(j + u) * lds]) : 0.f;
     *reinterpret_cast<float4 *>(sXt + i * LD + j) = make_float4(v[0], v[1], v[2], v[3]);
   }
   // column pairs (8 tj + 2 p, + 1) in packed FP32x2 accumulators: one packed
@@ -251,9 +254,11 @@ static cudaError_t leaf_apply_m(const T *Dinv, int nleaf, T *X, long long ldx, i
 bool leaf_apply_supported(int m) { return m == 64 || m == 128 || m == 256; }
 
 cudaError_t launch_leaf_apply_f64src(const float *Dinv, int m, int nleaf, const double *Xs, long long lds, float *X,
-                                     long long ldx, int ncols, cudaStream_t s) {
+                                     long long ldx, int ncols, DevStatus *st, cudaStream_t s) {
   if (m != 128) return cudaErrorNotSupported;
   if (ncols <= 0 || nleaf <= 0) return cudaSuccess;
+  cudaError_t err = cudaSuccess;
+  if (leaf_apply_tc_try(Dinv, nleaf, Xs, lds, X, ldx, ncols, st, s, err)) return err;
   auto k = leaf_apply128_f32_kernel<double>;
   cudaError_t e = set_smem(k, kLa128Smem);
   if (e != cudaSuccess) return e;

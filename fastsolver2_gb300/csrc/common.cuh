@@ -23,6 +23,29 @@ __device__ __forceinline__ void report_error(DevStatus *st, int code, long long 
 
 template <typename T> __device__ __forceinline__ T dabs(T x) { return x < T(0) ? -x : x; }
 
+// FP64 -> FP32, round to nearest even, on the integer pipes.  GB300 runs
+// FP64 instructions -- the double -> float conversion among them -- at a
+// small fraction of the FP32 rate, so kernels that turn FP64 data into FP32
+// were paced by the conversion.  For magnitudes in the FP32 normal range
+// (double exponent 897 .. 1150) the float is the double's sign, its exponent
+// rebased from 1023 to 127 and the top 23 of its 52 fraction bits, rounded on
+// the 29 bits dropped with ties to even; a carry out of the fraction moves
+// into the exponent, up to infinity past the largest float, as the rounding
+// rule asks.  Zeros keep their sign; results in the subnormal range,
+// infinities and NaNs take the hardware conversion.
+__device__ __forceinline__ float f64_to_f32_rn(double d) {
+  const unsigned hi = static_cast<unsigned>(__double2hiint(d)), lo = static_cast<unsigned>(__double2loint(d));
+  const unsigned ahi = hi & 0x7FFFFFFFu;
+  if (ahi - (897u << 20) < ((1151u - 897u) << 20)) {
+    // (e << 23 | fraction) mod 2^32, less (896 << 23) mod 2^32 = 0xC0000000
+    const unsigned bits = __funnelshift_l(lo, ahi, 3) - 0xC0000000u;
+    const unsigned up = ((lo & 0x1FFFFFFFu) + 0x0FFFFFFFu + (bits & 1u)) >> 29;
+    return __uint_as_float((bits + up) | (hi & 0x80000000u));
+  }
+  if ((ahi | lo) == 0) return __uint_as_float(hi);
+  return __double2float_rn(d);
+}
+
 // Host-side launch accounting (every kernel launch of the library goes
 // through HODLR_LAUNCH so hodlr_kernel_launches() can report it).
 void count_launch();

@@ -58,6 +58,20 @@ bool make_tensor_map_f32(CUtensorMap *map, const float *base, long long rows, lo
            CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
+bool make_tensor_map_f64(CUtensorMap *map, const double *base, long long rows, long long cols, long long ld,
+                         int box_rows, int box_cols) {
+  EncodeTiledFn f = encode_fn();
+  if (!f || !base || rows < 1 || cols < 1) return false;
+  if ((reinterpret_cast<uintptr_t>(base) & 15) || (ld * 8) % 16 || ld < rows) return false;
+  cuuint64_t dims[2] = {(cuuint64_t)rows, (cuuint64_t)cols};
+  cuuint64_t strides[1] = {(cuuint64_t)ld * 8};
+  cuuint32_t box[2] = {(cuuint32_t)box_rows, (cuuint32_t)box_cols};
+  cuuint32_t es[2] = {1, 1};
+  return f(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 2, const_cast<double *>(base), dims, strides, box, es,
+           CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+           CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
 bool make_tensor_map_f32_rowblocks(CUtensorMap *map, const float *base, long long rows, long long cols, long long ld,
                                    int row_blocks, int box_cols) {
   EncodeTiledFn f = encode_fn();

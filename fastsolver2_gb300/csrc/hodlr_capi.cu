@@ -598,7 +598,7 @@ template <typename T> static int factor_sweep(hodlr_ctx *h, bool leaves_done = f
     // Utilde = D^{-1} U straight from the FP64 U (rounded as it is staged)
     PHASE(h, HODLR_PHASE_LEAF_SOLVE,
           launch_leaf_apply_f64src(reinterpret_cast<const float *>(Dinv), m, h->nleaf, h->U, n,
-                                   reinterpret_cast<float *>(Ut), n, L * r, s));
+                                   reinterpret_cast<float *>(Ut), n, L * r, h->dst, s));
   } else {
     if (sizeof(T) == 8)
       CK(cudaMemcpyAsync(Ut, h->U, sizeof(double) * n * L * r, cudaMemcpyDeviceToDevice, s));

@@ -131,9 +131,13 @@ cudaError_t launch_leaf_apply(const T *Dinv, int m, int nleaf, T *X, long long l
                               const int *skip, cudaStream_t s);
 // X := Dinv X for leaf size 128 with the source read from Xs (FP64, leading
 // dimension lds) and rounded to FP32 as it is staged (the factorisation's
-// U -> Utilde); cudaErrorNotSupported for other leaf sizes.
+// U -> Utilde): on the tcgen05 tensor cores where the tensor map can be made,
+// else on the FMA pipe; cudaErrorNotSupported for other leaf sizes.
 cudaError_t launch_leaf_apply_f64src(const float *Dinv, int m, int nleaf, const double *Xs, long long lds, float *X,
-                                     long long ldx, int ncols, cudaStream_t s);
+                                     long long ldx, int ncols, DevStatus *st, cudaStream_t s);
+// The tcgen05 path of the above (false: preconditions not met, nothing launched).
+bool leaf_apply_tc_try(const float *Dinv, int nleaf, const double *U, long long lds, float *Y, long long ldy,
+                       int ncols, DevStatus *st, cudaStream_t s, cudaError_t &err);
 
 // Capacitance factorisation of the nodes of one depth: S from the T blocks'
 // columns [ucol, ucol + r), FP64 LU (stored in cap_lu / cap_ipiv) and the FP64

@@ -10,9 +10,12 @@
 namespace hodlr {
 
 // --------------------------------------------------------------- helpers
+template <typename Tout, typename Tin> __device__ __forceinline__ Tout convert_one(Tin x) { return (Tout)x; }
+template <> __device__ __forceinline__ float convert_one<float, double>(double x) { return f64_to_f32_rn(x); }
+
 template <typename Tin, typename Tout>
 __global__ void convert_kernel(const Tin *X, long long ldx, Tout *Y, long long ldy, long long n, int c) {
-  HODLR_FOR_2D(i, j, n, c) Y[i + j * ldy] = (Tout)X[i + j * ldx];
+  HODLR_FOR_2D(i, j, n, c) Y[i + j * ldy] = convert_one<Tout>(X[i + j * ldx]);
 }
 
 static int grid_for(long long total) {
@@ -266,7 +269,7 @@ __global__ void rhs_prepare_kernel(const double *B, long long ldb, long long n, 
   for (long long i = lo + threadIdx.x; i < hi; i += blockDim.x) {
     const double v = B[i + (long long)j * ldb];
     B64[i + (long long)j * n] = v;
-    X32[i + (long long)j * n] = (float)v;
+    X32[i + (long long)j * n] = f64_to_f32_rn(v);
     acc += v * v;
   }
   block_sumsq_store(acc, work, (long long)j * P + pb);

@@ -77,45 +77,8 @@ struct RcShared {
   int abort;
 };
 
-__device__ __forceinline__ void rc_arrive(uint64_t *bar) {
-  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
-}
-
 __device__ __forceinline__ bool rc_wait(uint64_t *bar, unsigned parity, RcShared *sh) {
-  if (mbar_try_wait(bar, parity)) return true;
-  const long long t0 = clock64(), budget = sh->budget;
-  while (!mbar_try_wait(bar, parity)) {
-    if (*(volatile int *)&sh->abort) return false;
-    if (clock64() - t0 > budget) {
-      *(volatile int *)&sh->abort = 1;
-      return false;
-    }
-  }
-  return true;
-}
-
-// Three bf16 planes of 4 consecutive K values of one row (8 bytes of each
-// plane), two values per conversion: x = h + m + l exactly (the two
-// subtractions are exact).
-__device__ __forceinline__ void put_planes4(unsigned char *p0, int plane_bytes, int off, const float4 &v) {
-  const float x[4] = {v.x, v.y, v.z, v.w};
-  uint2 ph, pm, pl;
-  unsigned *h = &ph.x, *m = &pm.x, *l = &pl.x;
-#pragma unroll
-  for (int e = 0; e < 2; ++e) {
-    const __nv_bfloat162 hb = __floats2bfloat162_rn(x[2 * e], x[2 * e + 1]);
-    const float2 hf = __bfloat1622float2(hb);
-    const float r0 = x[2 * e] - hf.x, r1 = x[2 * e + 1] - hf.y;
-    const __nv_bfloat162 mb = __floats2bfloat162_rn(r0, r1);
-    const float2 mf = __bfloat1622float2(mb);
-    const __nv_bfloat162 lb = __floats2bfloat162_rn(r0 - mf.x, r1 - mf.y);
-    h[e] = *reinterpret_cast<const unsigned *>(&hb);
-    m[e] = *reinterpret_cast<const unsigned *>(&mb);
-    l[e] = *reinterpret_cast<const unsigned *>(&lb);
-  }
-  *reinterpret_cast<uint2 *>(p0 + off) = ph;
-  *reinterpret_cast<uint2 *>(p0 + plane_bytes + off) = pm;
-  *reinterpret_cast<uint2 *>(p0 + 2 * plane_bytes + off) = pl;
+  return mbar_wait_or_abort(bar, parity, &sh->abort, sh->budget);
 }
 
 struct RcArgs {
@@ -291,10 +254,10 @@ reduce_tc_kernel(const __grid_constant__ CUtensorMap mapX, const __grid_constant
           }
           fence_proxy_async_smem();  // the planes are read by the tensor core (async proxy)
           __syncwarp();              // one arrival per warp, after every lane's writes
-          if (lane == 0) rc_arrive(&sh->planes_ready[pb]);
+          if (lane == 0) mbar_arrive(&sh->planes_ready[pb]);
         }
         __syncwarp();  // every lane's reads of the stage are done
-        if (ok && lane == 0) rc_arrive(&sh->slot_free[q]);
+        if (ok && lane == 0) mbar_arrive(&sh->slot_free[q]);
       }
     }
   } else {
@@ -324,7 +287,7 @@ reduce_tc_kernel(const __grid_constant__ CUtensorMap mapX, const __grid_constant
         tc_wait_ld(v);
         tc_fence_before();
         __syncwarp();
-        if (lane == 0) rc_arrive(&sh->acc_free[ac]);
+        if (lane == 0) mbar_arrive(&sh->acc_free[ac]);
 #pragma unroll
         for (int q = 0; q < kRcN; ++q)
           sum[q] += (__uint_as_float(v[0][q]) + __uint_as_float(v[1][q])) + __uint_as_float(v[2][q]);

@@ -90,14 +90,42 @@ __device__ __forceinline__ void tc_wait_ld(unsigned (&v)[N][W]) {
     for (int b = 0; b < W; ++b) asm volatile("" : "+r"(v[a][b]));
 }
 
-// Exact three-way bf16 split of an FP32 value, x = h + m + l (24 significant
-// bits; both subtractions are exact), for FP32-class products on the bf16
-// tensor cores from the six partial products down to 2^-16.
-__device__ __forceinline__ void split3(float x, __nv_bfloat16 &h, __nv_bfloat16 &m, __nv_bfloat16 &l) {
-  h = __float2bfloat16_rn(x);
-  const float r1 = x - __bfloat162float(h);
-  m = __float2bfloat16_rn(r1);
-  l = __float2bfloat16_rn(r1 - __bfloat162float(m));
+// Plain arrival on an mbarrier (warp-role kernels: one per thread of a role).
+__device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
+// Bounded wait of a warp-role kernel: false once the wait ran past `limit`
+// SM clocks (it then sets *abort) or another role set *abort, so that every
+// role leaves its loop when one of them gave up.
+__device__ __forceinline__ bool mbar_wait_or_abort(uint64_t *bar, unsigned parity, int *abort, long long limit) {
+  if (mbar_try_wait(bar, parity)) return true;
+  const long long t0 = clock64();
+  while (!mbar_try_wait(bar, parity)) {
+    if (*(volatile int *)abort) return false;
+    if (clock64() - t0 > limit) {
+      *(volatile int *)abort = 1;
+      return false;
+    }
+  }
+  return true;
+}
+
+// Exact three-way bf16 split of two FP32 values, x = h + m + l (24
+// significant bits; both subtractions are exact), for FP32-class products on
+// the bf16 tensor cores from the six partial products down to 2^-16.  Each
+// plane's pair is one packed conversion (value a in the low half, the lower
+// address); widening a bf16 back to FP32 is exact.
+__device__ __forceinline__ void split3_pair(float a, float b, unsigned &h, unsigned &m, unsigned &l) {
+  const __nv_bfloat162 hb = __floats2bfloat162_rn(a, b);
+  const float2 hf = __bfloat1622float2(hb);
+  const float ra = a - hf.x, rb = b - hf.y;
+  const __nv_bfloat162 mb = __floats2bfloat162_rn(ra, rb);
+  const float2 mf = __bfloat1622float2(mb);
+  const __nv_bfloat162 lb = __floats2bfloat162_rn(ra - mf.x, rb - mf.y);
+  h = *reinterpret_cast<const unsigned *>(&hb);
+  m = *reinterpret_cast<const unsigned *>(&mb);
+  l = *reinterpret_cast<const unsigned *>(&lb);
 }
 
 // Byte offset of 16-byte chunk c (of 4) of row i in a K-major tile of 64-byte
@@ -105,14 +133,27 @@ __device__ __forceinline__ void split3(float x, __nv_bfloat16 &h, __nv_bfloat16 
 // base is 1024-byte aligned).
 __device__ __forceinline__ int swz64(int i, int c) { return i * 64 + ((c ^ ((i >> 1) & 3)) << 4); }
 
-// Writes the three planes of 8 consecutive K values of one row.
+// Writes the three planes of 8 consecutive K values of one row (16 bytes
+// of each plane).
 __device__ __forceinline__ void put_planes(unsigned char *p0, int plane_bytes, int off, const float (&x)[8]) {
-  __align__(16) __nv_bfloat16 h[8], m[8], l[8];
-#pragma unroll
-  for (int e = 0; e < 8; ++e) split3(x[e], h[e], m[e], l[e]);
-  *reinterpret_cast<uint4 *>(p0 + off) = *reinterpret_cast<const uint4 *>(h);
-  *reinterpret_cast<uint4 *>(p0 + plane_bytes + off) = *reinterpret_cast<const uint4 *>(m);
-  *reinterpret_cast<uint4 *>(p0 + 2 * plane_bytes + off) = *reinterpret_cast<const uint4 *>(l);
+  uint4 h, m, l;
+  split3_pair(x[0], x[1], h.x, m.x, l.x);
+  split3_pair(x[2], x[3], h.y, m.y, l.y);
+  split3_pair(x[4], x[5], h.z, m.z, l.z);
+  split3_pair(x[6], x[7], h.w, m.w, l.w);
+  *reinterpret_cast<uint4 *>(p0 + off) = h;
+  *reinterpret_cast<uint4 *>(p0 + plane_bytes + off) = m;
+  *reinterpret_cast<uint4 *>(p0 + 2 * plane_bytes + off) = l;
+}
+
+// The same for 4 consecutive K values (8 bytes of each plane).
+__device__ __forceinline__ void put_planes4(unsigned char *p0, int plane_bytes, int off, const float4 &v) {
+  uint2 h, m, l;
+  split3_pair(v.x, v.y, h.x, m.x, l.x);
+  split3_pair(v.z, v.w, h.y, m.y, l.y);
+  *reinterpret_cast<uint2 *>(p0 + off) = h;
+  *reinterpret_cast<uint2 *>(p0 + plane_bytes + off) = m;
+  *reinterpret_cast<uint2 *>(p0 + 2 * plane_bytes + off) = l;
 }
 
 }  // namespace hodlr

@@ -106,10 +106,9 @@ __device__ __forceinline__ int swz128(int row, int chunk) { return row * 128 + (
 // caller then takes its non-TMA path).
 bool make_tensor_map_f32(CUtensorMap *map, const float *base, long long rows, long long cols, long long ld,
                          int box_rows, int box_cols, bool swizzle128);
-// 2-D tensor map over a bf16 matrix stored with `inner` contiguous elements
-// per line (line pitch `ld` elements, `outer` lines); box box_inner x
-// box_outer, swizzle 0, 32, 64 or 128 bytes.  Out-of-range elements load as
-// zero.
+// The same over a column-major FP64 matrix, no swizzle.
+bool make_tensor_map_f64(CUtensorMap *map, const double *base, long long rows, long long cols, long long ld,
+                         int box_rows, int box_cols);
 // 3-D tensor map over the same column-major FP32 matrix seen as 32-row
 // blocks: (32 rows, rows / 32 blocks, cols), box (32, row_blocks, box_cols)
 // with the 128-byte swizzle -- a box of 32 * row_blocks rows whose 128-byte
@@ -117,6 +116,10 @@ bool make_tensor_map_f32(CUtensorMap *map, const float *base, long long rows, lo
 // rows are.  rows must be a multiple of 32.
 bool make_tensor_map_f32_rowblocks(CUtensorMap *map, const float *base, long long rows, long long cols, long long ld,
                                    int row_blocks, int box_cols);
+// 2-D tensor map over a bf16 matrix stored with `inner` contiguous elements
+// per line (line pitch `ld` elements, `outer` lines); box box_inner x
+// box_outer, swizzle 0, 32, 64 or 128 bytes.  Out-of-range elements load as
+// zero.
 bool make_tensor_map_bf16(CUtensorMap *map, const void *base, long long inner, long long outer, long long ld,
                           int box_inner, int box_outer, int swizzle_bytes);
 

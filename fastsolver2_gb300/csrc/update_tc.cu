@@ -66,21 +66,8 @@ struct WsShared {
   int abort;
 };
 
-__device__ __forceinline__ void ws_arrive(uint64_t *bar) {
-  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
-}
-
 __device__ __forceinline__ bool ws_wait(uint64_t *bar, unsigned parity, WsShared *sh) {
-  if (mbar_try_wait(bar, parity)) return true;
-  const long long t0 = clock64();
-  while (!mbar_try_wait(bar, parity)) {
-    if (*(volatile int *)&sh->abort) return false;
-    if (clock64() - t0 > kWsWait) {
-      *(volatile int *)&sh->abort = 1;
-      return false;
-    }
-  }
-  return true;
+  return mbar_wait_or_abort(bar, parity, &sh->abort, kWsWait);
 }
 
 }  // namespace
@@ -228,7 +215,7 @@ update_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant
         put_planes(pa, kPA, swz64(r, c), x);
       }
       fence_proxy_async_smem();  // the planes are read by the tensor core (async proxy)
-      ws_arrive(&sh->planes_ready);
+      mbar_arrive(&sh->planes_ready);
     }
   } else {
     // ------------------------------------------------------------ epilogue
@@ -246,7 +233,7 @@ update_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant
       for (int h = 0; h < kBN / 32; ++h) tc_ld32(tl + 32 * h, v[h]);
       asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
       tc_fence_before();
-      ws_arrive(&sh->acc_free[ac]);
+      mbar_arrive(&sh->acc_free[ac]);
       float *sC = reinterpret_cast<float *>(base + s * kStageBytes + kABytes32);  // [kBN][kBM]
 #pragma unroll
       for (int h = 0; h < kBN / 32; ++h)
@@ -256,7 +243,7 @@ update_tc_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant
           *cp = fmaf(alpha, __uint_as_float(v[h][c]), *cp);
         }
       fence_proxy_async_smem();  // the C tile is read by the TMA store (async proxy)
-      ws_arrive(&sh->tile_done[s]);
+      mbar_arrive(&sh->tile_done[s]);
     }
   }
   __syncthreads();

@@ -84,6 +84,34 @@ def test_factors_match_oracle(hodlr, m, L, r, decay):
     assert rel(cap, f["cap_lu"]) < 1e-12
 
 
+@pytest.mark.parametrize("L,r", [(3, 32), (5, 8), (2, 40), (4, 24), (1, 3), (1, 40)])
+def test_mixed_utilde_tensor_cores_match_fma_and_oracle(hodlr, L, r, monkeypatch):
+    """Utilde = D^{-1} U of the mixed factorisation for 128-row leaves (U read
+    in FP64): the tcgen05 kernel (exact three-way bf16 split, six partial
+    products) against the FP32-FMA kernel on the same FP32 inverse -- equal
+    to FP32 product rounding (a numpy emulation of both gives 2.4e-7) -- and
+    both against the oracle's FP64 Utilde, to the FP32 inverse's accuracy.
+    With one level the leaf application is all of Utilde; with more, the
+    factorisation's FP32 updates of the ancestors' columns (also switched
+    between tensor cores and FMA) add their own rounding.  Column counts L r
+    that are not multiples of the 32-column tile included."""
+    pr = P.gaussian_problem(128, L, r, nrhs=1, seed=23)
+    _, f, info = O.hsolve_general(pr, pr.B, keep_factors=True)
+    assert info == 0
+    ref = np.concatenate([f["utilde"][l] for l in range(L)], axis=1)
+    got = {}
+    for tc in ("1", "0"):
+        monkeypatch.setenv("HODLR_NO_TCGEN05", "0" if tc == "1" else "1")
+        s = make_solver(hodlr, pr, precision=hodlr.PREC_MIXED)
+        s.factor()
+        ut = torch.empty((L * r, pr.n), dtype=torch.float64, device="cuda").t()
+        s.get_factors(utilde=ut)
+        got[tc] = to_host(ut)
+    assert rel(got["1"], got["0"]) < (1e-6 if L == 1 else 1e-5)
+    for tc in got:
+        assert rel(got[tc], ref) < 1e-4
+
+
 @pytest.mark.parametrize("m,L,r", [(128, 4, 32), (64, 4, 20), (64, 3, 16), (32, 3, 5), (16, 2, 1)])
 def test_mixed_capacitance_lu_matches_fp64(hodlr, m, L, r):
     # the mixed path factors S (assembled from FP32 reductions) in FP64 with
