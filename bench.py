@@ -515,7 +515,10 @@ def run_ours(args, wl):
     resid_pipe = {0: "fp64", 1: "dw", 2: "mma"}[args.resid]
     work = {  # name: {pipe: flops}
         "leaf_lu": {"fp32": (2 / 3) * n * m * m + 2 * n * m * m},
-        "leaf_solve": {"fp32": 2 * n * m * L * r + nsw * 2 * n * m * k},
+        # the factorisation's application D^-1 U runs on the tensor cores and
+        # is bounded by its bytes (U in FP64, Utilde in FP32, Dinv); the
+        # solve's applications to the right-hand sides by the FFMA rate
+        "leaf_solve": {"hbm": n * L * r * (8 + 4) + n * m * 4, "fp32": nsw * 2 * n * m * k},
         "reduce": {"fp32": sum(2 * n * r * (l + 1) * r for l in range(L)) + nsw * 2 * n * r * k * L},
         "update": {"fp32": sum(2 * n * r * l * r for l in range(L)) + nsw * 2 * n * r * k * L},
         "capacitance": {"fp64": cap_lu, "fp32": cap_fp32},
@@ -524,7 +527,9 @@ def run_ours(args, wl):
         "resid_update": {resid_pipe: nsw * 2 * n * r * k * L},
     }
     dw_tf = ffma_tf / 12.0   # a double-word FMA is 12 FP32 instructions
-    pipe_peak = {"fp64": dfma_tf, "fp32": ffma_tf, "dw": dw_tf, "mma": mma_tf / OZ_PAIRS}
+    # "hbm" work is bytes and its peak TB/s (10^12 bytes / s), the others flops and TFLOP/s
+    pipe_peak = {"fp64": dfma_tf, "fp32": ffma_tf, "dw": dw_tf, "mma": mma_tf / OZ_PAIRS,
+                 "hbm": (_measured_peak("hbm_gbs") or 6800.0) / 1e3}
     phase_report = {}
     for name, (pms, pn) in phases.items():
         per_step = pms / args.steps
@@ -532,7 +537,8 @@ def run_ours(args, wl):
         if name in work and per_step > 0:
             w = work[name]
             t_bound = sum(f / (pipe_peak[pp] * 1e12) for pp, f in w.items()) * 1e3
-            ent.update(tflops=sum(w.values()) / (per_step * 1e-3) / 1e12, bound_ms=t_bound, frac=t_bound / per_step,
+            ent.update(tflops=sum(f for pp, f in w.items() if pp != "hbm") / (per_step * 1e-3) / 1e12,
+                       bound_ms=t_bound, frac=t_bound / per_step,
                        pipes={pp: pipe_peak[pp] for pp in w})
         phase_report[name] = ent
     # the kernels of the dominant phases: (phases, bound, peak, native work

@@ -16,19 +16,22 @@
 // products are below 2^-23 of |a b| together), the class of the FMA kernel
 // this replaces.
 //
-// One persistent CTA per SM walks a contiguous range of (leaf, 32-column)
-// tiles: the 96 KB of Dinv planes are cut once per leaf and serve all of its
-// ceil(L r / 32) tiles, and the producer prefetches the next leaf's Dinv into
-// L2 when a leaf starts.  The U tiles stream through a 2-stage TMA ring and
-// the U planes are double-buffered, so that the split of tile i + 1 runs
-// while the tensor cores multiply tile i.
-// Warp roles, joined by mbarriers: 16 splitters (Dinv and U tiles into
-// planes), 8 epilogue warps (tensor memory -> registers -> global, one row
-// and 16 columns a thread, coalesced along the rows), a producer and an MMA
-// issuer.  The splits are chains of dependent conversions, so it takes many
-// warps to keep them from pacing the tiles.  Every
-// wait is bounded; on timeout the CTA records HODLR_ERR_TIMEOUT, waits
-// (bounded) for its copies and products and frees its tensor memory.
+// A = Dinv lives in tensor memory: its three planes (128 lanes x 64 columns
+// each, two bf16 a column) are cut once per leaf and serve all of the leaf's
+// ceil(L r / 32) tiles, so the products read only the 24 KB of U planes from
+// shared memory -- shared-memory bandwidth, not the tensor cores, bounds a
+// kernel that re-reads a 96 KB operand for every 32 output columns.  One
+// persistent CTA per SM walks a contiguous range of (leaf, 32-column) tiles;
+// the producer prefetches the next leaf's Dinv into L2 when a leaf starts.
+// The U tiles stream through a 4-stage TMA ring and the U planes are
+// double-buffered, so that the split of tile i + 1 runs while the tensor
+// cores multiply tile i.  Warp roles, joined by mbarriers: 16 splitters,
+// 8 epilogue warps (tensor memory -> registers -> global, one row and 16
+// columns a thread, coalesced along the rows), a producer and an MMA issuer.
+// The splits are chains of dependent conversions, so it takes many warps to
+// keep them from pacing the tiles.  Every wait is bounded; on timeout the
+// CTA records HODLR_ERR_TIMEOUT, waits (bounded) for its copies and products
+// and frees its tensor memory.
 #include <cuda_bf16.h>
 
 #include <cstdlib>
@@ -43,10 +46,8 @@ namespace {
 
 constexpr int kLM = 128;                       // leaf rows = K of the product
 constexpr int kLBN = 32;                       // columns of U per tile
-constexpr int kLStages = 2;                    // U tiles in flight
+constexpr int kLStages = 4;                    // U tiles in flight
 constexpr int kLStageBytes = kLM * kLBN * 8;   // one FP64 U tile: 32 KB
-constexpr int kLChunkA = kLM * 64;             // 32 K values of the 128 Dinv rows, bf16: 8 KB
-constexpr int kLPlaneA = 4 * kLChunkA;         // one Dinv plane: 32 KB
 constexpr int kLPlaneB = kLBN * 64;            // 32 K values of one U plane's 32 rows: 2 KB
 constexpr int kLChunkB = 3 * kLPlaneB;         // the three U planes of one K chunk (96 rows)
 constexpr int kLSW = 16;                       // splitter warps
@@ -54,7 +55,10 @@ constexpr int kLEW = 8;                        // epilogue warps: 4 lane quarter
 constexpr int kLThreads = 32 * (kLSW + kLEW + 2);  // + producer, MMA
 constexpr int kLSplit = 32 * kLSW;
 constexpr int kLBufB = 4 * kLChunkB;           // one buffer of U planes: 24 KB
-constexpr size_t kLSmem = (size_t)kLStages * kLStageBytes + 3 * kLPlaneA + 2 * kLBufB + 1024;
+constexpr size_t kLSmem = (size_t)kLStages * kLStageBytes + 2 * kLBufB + 1024;
+// tensor-memory columns: accumulators at 0 and 128 (96 each), the Dinv
+// planes at 256, 320, 384 (64 each: 128 K values, two a column)
+constexpr unsigned kLTmemCols = 512, kLAcc = 128, kLTA = 256, kLTPlane = 64;
 constexpr long long kLWait = 2000000000LL;     // about one second of SM clocks
 
 struct LaShared {
@@ -76,8 +80,7 @@ leaf_apply_tc_kernel(const __grid_constant__ CUtensorMap mapX, const float *__re
   extern __shared__ unsigned char smem_raw[];
   unsigned char *base =
       reinterpret_cast<unsigned char *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
-  unsigned char *pa = base + kLStages * kLStageBytes;  // 3 Dinv planes, each 4 K chunks of 128 rows
-  unsigned char *pb = pa + 3 * kLPlaneA;               // 2 buffers of 4 K chunks of the 3 U planes' 96 rows
+  unsigned char *pb = base + kLStages * kLStageBytes;  // 2 buffers of 4 K chunks of the 3 U planes' 96 rows
   __shared__ LaShared shm;
   LaShared *sh = &shm;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -101,9 +104,9 @@ leaf_apply_tc_kernel(const __grid_constant__ CUtensorMap mapX, const float *__re
     mbar_fence_init();
   }
   constexpr int kProd = kLSW + kLEW, kMmaWarp = kProd + 1;
-  static_assert(kLSW % 4 == 0 && kLM * 16 % (32 * kLSW) == 0 && kLBN * 16 % (32 * kLSW) == 0, "warp roles");
+  static_assert(kLSW == 16 && kLBN * 16 == 32 * kLSW, "warp roles: 4 quarters x 4 K ranges; one U task a thread");
   if (warp == kMmaWarp) {
-    tc_alloc(&sh->tmem, 256);  // two accumulators of 96 columns, 128 apart
+    tc_alloc(&sh->tmem, kLTmemCols);
     tc_relinquish();
   }
   tc_fence_before();
@@ -132,27 +135,25 @@ leaf_apply_tc_kernel(const __grid_constant__ CUtensorMap mapX, const float *__re
     // ---------------------------------------------------------------- MMA
     if (lane == 0) {
       const unsigned id96 = tc_idesc_bf16(kLM, 96), id64 = tc_idesc_bf16(kLM, 64), id32 = tc_idesc_bf16(kLM, 32);
-      const unsigned a0 = smem_u32(pa), b0 = smem_u32(pb);
+      const unsigned b0 = smem_u32(pb);
       for (long long i = 0; i < nmine; ++i) {
         const int ac = (int)(i & 1);  // the accumulator and the plane buffer of tile i
         if (!wait(&sh->planes_ready[ac], (unsigned)((i >> 1) & 1))) break;
         if (i >= 2 && !wait(&sh->acc_free[ac], (unsigned)(((i >> 1) - 1) & 1))) break;
         tc_fence_after();
-        const unsigned d = tmem + (unsigned)(128 * ac);
-        // descriptors as base + offset (16-byte units; every shared address
-        // fits the 14-bit field), the bases opaque so that the 24 operand
-        // descriptors are formed per tile instead of held in registers
-        uint64_t da = desc_sw64(a0), db = desc_sw64(b0 + ac * kLBufB);
-        asm volatile("" : "+l"(da), "+l"(db));
+        const unsigned d = tmem + kLAcc * ac, ta = tmem + kLTA;
+        // B descriptors as base + offset (16-byte units; every shared address
+        // fits the 14-bit field), the base opaque so that the eight are formed
+        // per tile instead of held in registers
+        uint64_t db = desc_sw64(b0 + ac * kLBufB);
+        asm volatile("" : "+l"(db));
 #pragma unroll
-        for (int kc = 0; kc < 4; ++kc)
-#pragma unroll
-          for (int kk = 0; kk < 2; ++kk) {
-            const uint64_t bd = db + (kc * kLChunkB >> 4) + 2 * kk, ad = da + (kc * kLChunkA >> 4) + 2 * kk;
-            tc_mma(d, ad, bd, id96, (kc | kk) ? 1u : 0u);
-            tc_mma(d + 32, ad + (kLPlaneA >> 4), bd, id64, 1u);
-            tc_mma(d + 64, ad + (2 * kLPlaneA >> 4), bd, id32, 1u);
-          }
+        for (int ks = 0; ks < 8; ++ks) {  // K steps of 16: chunk ks / 2, half ks % 2
+          const uint64_t bd = db + ((ks >> 1) * kLChunkB >> 4) + 2 * (ks & 1);
+          tc_mma_ta(d, ta + 8 * ks, bd, id96, ks ? 1u : 0u);
+          tc_mma_ta(d + 32, ta + kLTPlane + 8 * ks, bd, id64, 1u);
+          tc_mma_ta(d + 64, ta + 2 * kLTPlane + 8 * ks, bd, id32, 1u);
+        }
         tc_commit(&sh->acc_full[ac]);
         tc_commit(&sh->planes_free[ac]);
       }
@@ -175,51 +176,61 @@ leaf_apply_tc_kernel(const __grid_constant__ CUtensorMap mapX, const float *__re
       if (i >= 2 && !wait(&sh->planes_free[pbuf], (unsigned)(((i >> 1) - 1) & 1))) break;
       if (leaf != cur && i >= 1 && !wait(&sh->planes_free[pbuf ^ 1], (unsigned)(((i - 1) >> 1) & 1))) break;
       if (leaf != cur) {
-        // Dinv planes: task (row r, 8 K values c); consecutive lanes take
-        // consecutive rows (coalesced loads, conflict-free swizzled stores);
-        // the loads of two tasks are issued before their split
+        // Dinv planes into tensor memory: warp w writes lanes 32 q .. 32 q + 31
+        // (q = w mod 4, the quarter its index allows) and K values 32 g ..
+        // 32 g + 31 (g = w / 4); the loads are coalesced along the rows, two
+        // tasks of 8 K values in flight at a time
         const float *A = Dinv + (long long)leaf * kLM * kLM;
-        constexpr int kTasks = kLM * 16 / kLSplit;
+        const int q = warp & 3, g = warp >> 2, r = 32 * q + lane;
+        const unsigned tl = tmem + ((unsigned)(32 * q) << 16) + kLTA;
 #pragma unroll
-        for (int u0 = 0; u0 < kTasks; u0 += 2) {
+        for (int u0 = 0; u0 < 4; u0 += 2) {
           float x[2][8];
 #pragma unroll
-          for (int u = 0; u < 2; ++u) {
-            const int task = tid + kLSplit * (u0 + u), r = task & (kLM - 1), c = task >> 7;
+          for (int u = 0; u < 2; ++u)
 #pragma unroll
-            for (int e = 0; e < 8; ++e) x[u][e] = __ldg(A + (long long)(8 * c + e) * kLM + r);
-          }
+            for (int e = 0; e < 8; ++e) x[u][e] = __ldg(A + (long long)(32 * g + 8 * (u0 + u) + e) * kLM + r);
 #pragma unroll
           for (int u = 0; u < 2; ++u) {
-            const int task = tid + kLSplit * (u0 + u), r = task & (kLM - 1), c = task >> 7;
-            put_planes(pa + (c >> 2) * kLChunkA, kLPlaneA, swz64(r, c & 3), x[u]);
+            uint4 h, m, l;
+            split3_pair(x[u][0], x[u][1], h.x, m.x, l.x);
+            split3_pair(x[u][2], x[u][3], h.y, m.y, l.y);
+            split3_pair(x[u][4], x[u][5], h.z, m.z, l.z);
+            split3_pair(x[u][6], x[u][7], h.w, m.w, l.w);
+            const unsigned col = (32 * g + 8 * (u0 + u)) / 2;
+            tc_st4(tl + col, h);
+            tc_st4(tl + kLTPlane + col, m);
+            tc_st4(tl + 2 * kLTPlane + col, l);
           }
         }
+        tc_wait_st();
         cur = leaf;
       }
       // U planes: task (column j, 8 K values c), FP64 -> FP32 (on the
-      // integer pipes) -> 3 x bf16
+      // integer pipes) -> 3 x bf16.  The eight lanes of a shared-memory
+      // phase take columns j0, j0 + 1 and four chunks of one 32-value K
+      // range, and start their four 16-byte reads at distinct offsets: the
+      // reads and the swizzled plane writes are free of bank conflicts.
       const double *sX = reinterpret_cast<const double *>(base + s * kLStageBytes);  // [kLBN][kLM]
 #pragma unroll
       for (int u = 0; u < kLBN * 16 / kLSplit; ++u) {
-        const int task = tid + kLSplit * u, j = task >> 4, c = task & 15;
-        // the four 16-byte pieces in rotated order (lanes 64 bytes apart
-        // then meet fewer bank conflicts), put back in order by selects
-        // with constant indices so that everything stays in registers
+        const int t = tid + kLSplit * u, kc = (t >> 3) & 3;
+        const int j = ((t >> 5) << 1) | ((t >> 2) & 1), c = 4 * kc + (t & 3);
+        const int d = (((c >> 1) & 1) + 2 * (j & 1)) & 3;  // the first 16-byte piece read
         double2 w[4];
 #pragma unroll
         for (int e2 = 0; e2 < 4; ++e2)
-          w[e2] = *reinterpret_cast<const double2 *>(sX + j * kLM + 8 * c + 2 * ((e2 + c) & 3));
-        const int d = c & 3;
+          w[e2] = *reinterpret_cast<const double2 *>(sX + j * kLM + 8 * c + 2 * ((e2 + d) & 3));
         float x[8];
 #pragma unroll
-        for (int q = 0; q < 4; ++q) {  // piece q sits in w[(q - d) & 3]
-          const double2 v = d == 0 ? w[q] : d == 1 ? w[(q + 3) & 3] : d == 2 ? w[(q + 2) & 3] : w[(q + 1) & 3];
-          x[2 * q] = f64_to_f32_rn(v.x);
-          x[2 * q + 1] = f64_to_f32_rn(v.y);
+        for (int p2 = 0; p2 < 4; ++p2) {  // piece p2 sits in w[(p2 - d) & 3]
+          const double2 v = d == 0 ? w[p2] : d == 1 ? w[(p2 + 3) & 3] : d == 2 ? w[(p2 + 2) & 3] : w[(p2 + 1) & 3];
+          x[2 * p2] = f64_to_f32_rn(v.x);
+          x[2 * p2 + 1] = f64_to_f32_rn(v.y);
         }
-        put_planes(pb + pbuf * kLBufB + (c >> 2) * kLChunkB, kLPlaneB, swz64(j, c & 3), x);
+        put_planes(pb + pbuf * kLBufB + kc * kLChunkB, kLPlaneB, swz64(j, c & 3), x);
       }
+      tc_fence_before();  // the tensor-memory writes above, before the arrival the MMA thread waits on
       mbar_arrive(&sh->stage_free[s]);
       fence_proxy_async_smem();  // the planes are read by the tensor core (async proxy)
       mbar_arrive(&sh->planes_ready[pbuf]);
@@ -272,7 +283,7 @@ leaf_apply_tc_kernel(const __grid_constant__ CUtensorMap mapX, const float *__re
   __syncthreads();
   if (warp == kMmaWarp) {
     tc_fence_after();
-    tc_dealloc(tmem, 256);
+    tc_dealloc(tmem, kLTmemCols);
   }
 }
 

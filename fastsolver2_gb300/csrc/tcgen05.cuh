@@ -50,6 +50,17 @@ __device__ __forceinline__ void tc_mma(unsigned d, uint64_t a, uint64_t b, unsig
       "l"(a), "l"(b), "r"(idesc), "r"(accumulate)
       : "memory");
 }
+// The same with A read from tensor memory: row i of A in lane i, two bf16
+// per 32-bit column (the lower K index in the low half), K 16 = 8 columns
+// from column `a` on.
+__device__ __forceinline__ void tc_mma_ta(unsigned d, unsigned a, uint64_t b, unsigned idesc, unsigned accumulate) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "setp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], [%1], %2, %3, p;\n\t}" ::"r"(d),
+      "r"(a), "l"(b), "r"(idesc), "r"(accumulate)
+      : "memory");
+}
 // The barrier receives one arrival when every tcgen05.mma this thread issued has completed.
 __device__ __forceinline__ void tc_commit(uint64_t *bar) {
   asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
@@ -79,6 +90,14 @@ __device__ __forceinline__ void tc_ld4(unsigned taddr, unsigned (&v)[4]) {
                : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3])
                : "r"(taddr));
 }
+// Each thread of the warp writes 4 consecutive columns of its lane (the
+// warp's quarter of the lanes); tc_wait_st makes the writes complete.
+__device__ __forceinline__ void tc_st4(unsigned taddr, const uint4 &v) {
+  asm volatile("tcgen05.st.sync.aligned.32x32b.x4.b32 [%0], {%1,%2,%3,%4};" ::"r"(taddr), "r"(v.x), "r"(v.y),
+               "r"(v.z), "r"(v.w)
+               : "memory");
+}
+__device__ __forceinline__ void tc_wait_st() { asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory"); }
 // Waits for this thread's tensor-memory loads; the registers pass through
 // so that no use of them is scheduled before the wait.
 template <int N, int W>
