@@ -20,7 +20,7 @@
 //   boxes of two 32-row blocks so that the 128-byte swizzle applies (boxes
 //   of 16 KB streamed at no more than ~4.7 TB/s on this GPU, of 32 KB at
 //   ~7.4 TB/s);
-// * eight warps cut each stage, one 32-row half at a time, into planes
+// * sixteen warps cut each stage, one 32-row half at a time, into planes
 //   (K-major, 64-byte swizzle, double buffered per half; 8 lanes read one
 //   128-byte line, so the reads are free of bank conflicts; one mbarrier
 //   arrival per warp);
@@ -59,7 +59,7 @@ constexpr int kRcK = 64, kRcH = 32;               // rows per stage, rows per ha
 constexpr int kRcStages = 3, kRcGroup = 4;        // ring depth; halves per accumulator use (128 rows)
 constexpr int kRcAcc = 3 * kRcN;                  // columns of one accumulator
 constexpr int kRcTmemCols = 256;                  // two accumulators, rounded up to a power of two
-constexpr int kRcSplitWarps = 8, kRcThreads = 32 * (kRcSplitWarps + 6);
+constexpr int kRcSplitWarps = 16, kRcThreads = 32 * (kRcSplitWarps + 6);
 constexpr int kRcXBytes = kRcK * kRcM * 4;        // FP32 X stage: 32 KB
 constexpr int kRcVBytes = kRcK * kRcN * 4;        // FP32 V stage: 8 KB
 constexpr int kRcStageBytes = kRcXBytes + kRcVBytes;
@@ -247,7 +247,7 @@ reduce_tc_kernel(const __grid_constant__ CUtensorMap mapX, const __grid_constant
             const float4 v = *reinterpret_cast<const float4 *>(sx + swz128(2 * j + h, c));
             put_planes4(px, kRcPX, swz64(j, c >> 1) + 8 * (c & 1), v);
           }
-          {  // V: rank qq, the same cut (one task per thread)
+          if (tid < 8 * kRcN) {  // V: rank qq, the same cut (one task per thread of the first 256)
             const int c = tid & 7, qq = tid >> 3;
             const float4 v = *reinterpret_cast<const float4 *>(sv + swz128(2 * qq + h, c));
             put_planes4(pv, kRcPV, swz64(qq, c >> 1) + 8 * (c & 1), v);
@@ -280,17 +280,20 @@ reduce_tc_kernel(const __grid_constant__ CUtensorMap mapX, const __grid_constant
           break;
         }
         tc_fence_after();
-        unsigned v[3][32];
         const unsigned tl = tmem + ((unsigned)(32 * w) << 16) + (unsigned)(kRcAcc * ac);
 #pragma unroll
-        for (int blk = 0; blk < 3; ++blk) tc_ld32(tl + kRcN * blk, v[blk]);
-        tc_wait_ld(v);
+        for (int hf = 0; hf < 2; ++hf) {  // ranks 16 hf .. 16 hf + 15 of the three blocks
+          unsigned v[3][16];
+#pragma unroll
+          for (int blk = 0; blk < 3; ++blk) tc_ld16(tl + kRcN * blk + 16 * hf, v[blk]);
+          tc_wait_ld(v);
+#pragma unroll
+          for (int q = 0; q < 16; ++q)
+            sum[16 * hf + q] += (__uint_as_float(v[0][q]) + __uint_as_float(v[1][q])) + __uint_as_float(v[2][q]);
+        }
         tc_fence_before();
         __syncwarp();
         if (lane == 0) mbar_arrive(&sh->acc_free[ac]);
-#pragma unroll
-        for (int q = 0; q < kRcN; ++q)
-          sum[q] += (__uint_as_float(v[0][q]) + __uint_as_float(v[1][q])) + __uint_as_float(v[2][q]);
       }
       if (!ok) break;
       const int jg = ct * kRcM + j;
