@@ -62,11 +62,13 @@ class Grads(ctypes.Structure):
 
 class Tuning(ctypes.Structure):
     _fields_ = [("red_ctas_per_sm", ctypes.c_int32), ("update_tile_rows", ctypes.c_int32),
-                ("cap_warps", ctypes.c_int32), ("update_tc_shape", ctypes.c_int32), ("ms", ctypes.c_double)]
+                ("cap_warps", ctypes.c_int32), ("update_tc_shape", ctypes.c_int32), ("leaf_apply", ctypes.c_int32),
+                ("ms", ctypes.c_double)]
 
     def as_dict(self):
         return {"red_ctas_per_sm": self.red_ctas_per_sm, "update_tile_rows": self.update_tile_rows,
-                "cap_warps": self.cap_warps, "update_tc_shape": self.update_tc_shape, "ms": self.ms}
+                "cap_warps": self.cap_warps, "update_tc_shape": self.update_tc_shape, "leaf_apply": self.leaf_apply,
+                "ms": self.ms}
 
 
 class System(ctypes.Structure):
@@ -299,8 +301,8 @@ class Solver:
         check(lib().hodlr_autotune(self.h, nrhs, ctypes.byref(t)))
         return t.as_dict()
 
-    def set_tuning(self, red_ctas_per_sm=4, update_tile_rows=0, cap_warps=0, update_tc_shape=0):
-        t = Tuning(red_ctas_per_sm, update_tile_rows, cap_warps, update_tc_shape, -1.0)
+    def set_tuning(self, red_ctas_per_sm=4, update_tile_rows=0, cap_warps=0, update_tc_shape=0, leaf_apply=0):
+        t = Tuning(red_ctas_per_sm, update_tile_rows, cap_warps, update_tc_shape, leaf_apply, -1.0)
         check(lib().hodlr_set_tuning(self.h, ctypes.byref(t)))
 
     def get_tuning(self):

@@ -2746,6 +2746,14 @@ static int tune_search(Tuning &cur, double &cur_ms, Measure measure) {
     CKS(measure(t, ms));
     if (ms < cur_ms) cur = t, cur_ms = ms;
   }
+  for (int la : {0, 1}) {
+    if (la == cur.leaf_apply) continue;
+    Tuning t = cur;
+    t.leaf_apply = la;
+    double ms = 0.0;
+    CKS(measure(t, ms));
+    if (ms < cur_ms) cur = t, cur_ms = ms;
+  }
   return HODLR_OK;
 }
 
@@ -2753,8 +2761,7 @@ static bool valid_tuning(const hodlr_tuning &t) {
   return (t.red_ctas_per_sm == 2 || t.red_ctas_per_sm == 4 || t.red_ctas_per_sm == 8) &&
          (t.update_tile_rows == 0 || t.update_tile_rows == 64 || t.update_tile_rows == 128) &&
          (t.cap_warps == 0 || t.cap_warps == 8 || t.cap_warps == 16 || t.cap_warps == 32) &&
-         t.update_tc_shape >= 0 &&
-         t.update_tc_shape <= 2;
+         t.update_tc_shape >= 0 && t.update_tc_shape <= 2 && (t.leaf_apply == 0 || t.leaf_apply == 1);
 }
 
 extern "C" {
@@ -2765,6 +2772,7 @@ int hodlr_set_tuning(hodlr_handle h, const hodlr_tuning *t) {
   h->tune.upd_bm = t->update_tile_rows == 128 ? 0 : t->update_tile_rows;
   h->tune.cap_warps = t->cap_warps;
   h->tune.upd_tc_shape = t->update_tc_shape;
+  h->tune.leaf_apply = t->leaf_apply;
   clear_graphs(h);
   h->factored = false;
   return HODLR_OK;
@@ -2776,6 +2784,7 @@ int hodlr_get_tuning(hodlr_handle h, hodlr_tuning *t) {
   t->update_tile_rows = h->tune.upd_bm;
   t->cap_warps = h->tune.cap_warps;
   t->update_tc_shape = h->tune.upd_tc_shape;
+  t->leaf_apply = h->tune.leaf_apply;
   t->ms = -1.0;
   return HODLR_OK;
 }
@@ -2816,6 +2825,7 @@ int hodlr_autotune(hodlr_handle h, int nrhs, hodlr_tuning *best) {
     best->update_tile_rows = cur.upd_bm;
     best->cap_warps = cur.cap_warps;
     best->update_tc_shape = cur.upd_tc_shape;
+    best->leaf_apply = cur.leaf_apply;
     best->ms = cur_ms;
   }
   return HODLR_OK;
@@ -2862,6 +2872,7 @@ int hodlr_batch_autotune(hodlr_batch b, hodlr_tuning *per_forest, int capacity) 
       per_forest[fi].update_tile_rows = cur.upd_bm;
       per_forest[fi].cap_warps = cur.cap_warps;
       per_forest[fi].update_tc_shape = cur.upd_tc_shape;
+      per_forest[fi].leaf_apply = cur.leaf_apply;
       per_forest[fi].ms = cur_ms;
     }
   }
@@ -2886,7 +2897,7 @@ int hodlr_batch_autotune(hodlr_batch b, hodlr_tuning *per_forest, int capacity) 
 namespace {
 
 constexpr char kCkMagic[8] = {'H', 'O', 'D', 'L', 'R', 'C', 'K', '1'};
-constexpr uint32_t kCkVersion = 2;
+constexpr uint32_t kCkVersion = 3;
 
 struct CkHeader {
   char magic[8];
@@ -2895,7 +2906,7 @@ struct CkHeader {
   int32_t leaf, levels, rank, nrhs_max, precision, residual;
   double refine_tol;
   int32_t refine_max_iter, flags;
-  int32_t red_ctas_per_sm, update_tile_rows, cap_warps, update_tc_shape;
+  int32_t red_ctas_per_sm, update_tile_rows, cap_warps, update_tc_shape, leaf_apply, reserved;
   uint64_t payload, checksum;
 };
 
@@ -2981,6 +2992,7 @@ int hodlr_checkpoint_save(hodlr_handle h, void *buf, int64_t bytes) {
   hd.update_tile_rows = h->tune.upd_bm;
   hd.cap_warps = h->tune.cap_warps;
   hd.update_tc_shape = h->tune.upd_tc_shape;
+  hd.leaf_apply = h->tune.leaf_apply;
   hd.payload = (uint64_t)(p - out) - sizeof(CkHeader);
   uint64_t a = 1, c = 0;
   ck_sum(out + sizeof(CkHeader), hd.payload, a, c);
@@ -3014,7 +3026,7 @@ int hodlr_checkpoint_load(const void *buf, int64_t bytes, void *stream, hodlr_ha
   d.refine_max_iter = hd.refine_max_iter;
   d.flags = hd.flags;
   d.stream = stream;
-  hodlr_tuning t{hd.red_ctas_per_sm, hd.update_tile_rows, hd.cap_warps, hd.update_tc_shape, -1.0};
+  hodlr_tuning t{hd.red_ctas_per_sm, hd.update_tile_rows, hd.cap_warps, hd.update_tc_shape, hd.leaf_apply, -1.0};
   if (!valid_tuning(t)) return set_err(HODLR_ERR_INVALID_ARG, "checkpoint holds unknown launch shapes");
   hodlr_handle h = nullptr;
   CKS(hodlr_create(&d, &h));

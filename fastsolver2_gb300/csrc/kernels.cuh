@@ -17,6 +17,7 @@ struct Tuning {
   int upd_bm = 0;           // FP32 update tile rows: 0 = 128 when the block allows, else 64
   int cap_warps = 0;        // mixed-path capacitance LU (2r <= 64): warps per node, 8, 16 or 32 (0: by level)
   int upd_tc_shape = 0;     // tcgen05 update: 0 = 128x64 tiles, 3-stage ring; 1 = 128x64, 2 stages; 2 = 128x32, 5 stages
+  int leaf_apply = 0;       // mixed factorisation's D^-1 U, leaf 128: 0 = tcgen05 kernel, 1 = FP32-FMA kernel
 };
 constexpr int kMaxRedCtasPerSm = 8;
 constexpr int kNumSMs = 152;

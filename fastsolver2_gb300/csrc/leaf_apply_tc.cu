@@ -294,7 +294,7 @@ bool leaf_apply_tc_try(const float *Dinv, int nleaf, const double *U, long long 
                        int ncols, DevStatus *st, cudaStream_t s, cudaError_t &err) {
   err = cudaSuccess;
   const char *off = getenv("HODLR_NO_TCGEN05");
-  if (off && off[0] == '1') return false;
+  if ((off && off[0] == '1') || current_tuning().leaf_apply == 1) return false;
   if (nleaf < 1 || ncols < 1 || (reinterpret_cast<uintptr_t>(Dinv) & 15)) return false;
   CUtensorMap mx;
   if (!make_tensor_map_f64(&mx, U, (long long)nleaf * kLM, ncols, lds, kLM, kLBN)) return false;

@@ -411,8 +411,9 @@ HODLR_API int hodlr_batch_stats(hodlr_batch b, int *nforests, double *factor_ms,
 /* ------------------------------------------------------------ autotuner
  * Launch shapes of the tunable kernels: the split-K target of the row
  * reductions (CTAs per SM), the row tile of the FP32-FMA low-rank update,
- * the tile and ring depth of the tensor-core update and the warps per
- * capacitance system of the mixed path.
+ * the tile and ring depth of the tensor-core update, the warps per
+ * capacitance system of the mixed path and the kernel of its leaf
+ * application (tensor cores or FP32-FMA tiles).
  * No counterpart in the reference (its BLAS calls have no launch shapes).
  * hodlr_autotune times complete factor + solve sweeps of the handle's own
  * inputs (a seeded scratch right-hand side of nrhs columns) for a coordinate
@@ -429,6 +430,8 @@ typedef struct hodlr_tuning {
                                 (0 = by level: 32 up to one system per SM, 16 up to two, else 8) */
   int32_t update_tc_shape;   /* tensor-core update: 0 = 128x64 tiles through a 3-stage ring,
                                 1 = 128x64 tiles, 2 stages, 2 = 128x32 tiles, 5 stages */
+  int32_t leaf_apply;        /* mixed path, leaf 128: the factorisation's application D^-1 U on
+                                the tensor cores (0) or on the FP32 FMA pipe (1) */
   double ms;                 /* autotune: factor + solve milliseconds with these shapes */
 } hodlr_tuning;
 

@@ -76,7 +76,7 @@ def test_null_handle_calls_fail_cleanly(fs):
     assert L.hodlr_factor(None) == fs.HODLR_ERR_INVALID_ARG
     assert L.hodlr_solve(None, None, 0, 1, None) == fs.HODLR_ERR_INVALID_ARG
     assert L.hodlr_destroy(None) == fs.HODLR_OK
-    t = fs.Tuning(4, 0, 8, 0, -1.0)
+    t = fs.Tuning(4, 0, 8, 0, 0, -1.0)
     assert L.hodlr_set_tuning(None, t) == fs.HODLR_ERR_INVALID_ARG
     assert L.hodlr_autotune(None, 1, None) == fs.HODLR_ERR_INVALID_ARG
     assert L.hodlr_batch_autotune(None, None, 0) == fs.HODLR_ERR_INVALID_ARG

@@ -149,7 +149,7 @@ def test_batch_autotune_then_solve(hodlr):
     assert len(tunes) == b.stats()[0]
     for t in tunes:
         assert t["red_ctas_per_sm"] in (2, 4, 8) and t["update_tile_rows"] in (0, 64) and t["ms"] > 0
-        assert t["cap_warps"] in (0, 8, 16) and t["update_tc_shape"] in (0, 1, 2)
+        assert t["cap_warps"] in (0, 8, 16) and t["update_tc_shape"] in (0, 1, 2) and t["leaf_apply"] in (0, 1)
     b.factor()
     Bs = [to_dev(p.B) for p in probs]
     torch.cuda.synchronize()

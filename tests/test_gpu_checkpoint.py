@@ -19,13 +19,14 @@ pytestmark = pytest.mark.gpu
 def test_checkpoint_round_trip_gives_identical_solves(hodlr, precision, resid, trans):
     pr = P.gaussian_problem(128, 4, 32, nrhs=8, seed=31, orthonormal=True, decay=4.0, shift=1.5)
     s = make_solver(hodlr, pr, precision=precision, residual=resid, refine_tol=1e-12)
-    s.set_tuning(red_ctas_per_sm=8, update_tile_rows=64, cap_warps=16, update_tc_shape=2)
+    s.set_tuning(red_ctas_per_sm=8, update_tile_rows=64, cap_warps=16, update_tc_shape=2, leaf_apply=1)
     s.factor()
     data = s.checkpoint()
     t = hodlr.Solver.from_checkpoint(data)
     assert (t.n, t.leaf, t.levels, t.rank) == (pr.n, pr.leaf, pr.levels, pr.rank)
     assert t.get_tuning()["red_ctas_per_sm"] == 8
     assert t.get_tuning()["cap_warps"] == 16 and t.get_tuning()["update_tc_shape"] == 2
+    assert t.get_tuning()["leaf_apply"] == 1
     B0, B1 = to_dev(pr.B), to_dev(pr.B)
     i0 = s.solve(B0, transpose=trans)
     s.close()  # the loaded handle owns its own copies

@@ -100,14 +100,20 @@ def test_mixed_utilde_tensor_cores_match_fma_and_oracle(hodlr, L, r, monkeypatch
     assert info == 0
     ref = np.concatenate([f["utilde"][l] for l in range(L)], axis=1)
     got = {}
-    for tc in ("1", "0"):
-        monkeypatch.setenv("HODLR_NO_TCGEN05", "0" if tc == "1" else "1")
+    for tc in ("1", "0", "tuned-fma"):
+        monkeypatch.setenv("HODLR_NO_TCGEN05", "1" if tc == "0" else "0")
         s = make_solver(hodlr, pr, precision=hodlr.PREC_MIXED)
+        if tc == "tuned-fma":  # the tuning knob: only the leaf application leaves the tensor cores
+            s.set_tuning(leaf_apply=1)
+            assert s.get_tuning()["leaf_apply"] == 1
         s.factor()
         ut = torch.empty((L * r, pr.n), dtype=torch.float64, device="cuda").t()
         s.get_factors(utilde=ut)
         got[tc] = to_host(ut)
     assert rel(got["1"], got["0"]) < (1e-6 if L == 1 else 1e-5)
+    assert rel(got["1"], got["tuned-fma"]) < (1e-6 if L == 1 else 1e-5)
+    if L == 1:  # no updates: the knob and the switch run the same FMA kernel
+        assert np.array_equal(got["0"], got["tuned-fma"])
     for tc in got:
         assert rel(got[tc], ref) < 1e-4
 
@@ -476,9 +482,10 @@ def test_autotune_picks_valid_shapes_and_keeps_results(hodlr, precision):
     s = make_solver(hodlr, pr, precision=precision)
     t = s.autotune(nrhs=4)
     assert t["red_ctas_per_sm"] in (2, 4, 8) and t["update_tile_rows"] in (0, 64) and t["ms"] > 0
-    assert t["cap_warps"] in (0, 8, 16) and t["update_tc_shape"] in (0, 1, 2)
+    assert t["cap_warps"] in (0, 8, 16) and t["update_tc_shape"] in (0, 1, 2) and t["leaf_apply"] in (0, 1)
     got = s.get_tuning()
-    assert all(got[key] == t[key] for key in ("red_ctas_per_sm", "update_tile_rows", "cap_warps", "update_tc_shape"))
+    assert all(got[key] == t[key]
+               for key in ("red_ctas_per_sm", "update_tile_rows", "cap_warps", "update_tc_shape", "leaf_apply"))
     B = to_dev(pr.B)
     s.solve(B)   # autotune left the handle factored
     Xo, _, _ = O.hsolve_general(pr, pr.B)
