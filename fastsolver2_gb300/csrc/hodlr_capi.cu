@@ -595,7 +595,8 @@ template <typename T> static int factor_sweep(hodlr_ctx *h, bool leaves_done = f
   }
   if (L == 0) return HODLR_OK;
   if (sizeof(T) == 4 && Dinv && m == 128) {
-    // Utilde = D^{-1} U straight from the FP64 U (rounded as it is staged)
+    // Utilde = D^{-1} U straight from the FP64 U (rounded as it is split or
+    // staged): on the tensor cores, or the FMA tiles when the tuning asks
     PHASE(h, HODLR_PHASE_LEAF_SOLVE,
           launch_leaf_apply_f64src(reinterpret_cast<const float *>(Dinv), m, h->nleaf, h->U, n,
                                    reinterpret_cast<float *>(Ut), n, L * r, h->dst, s));
